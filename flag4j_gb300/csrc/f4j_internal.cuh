@@ -1,0 +1,102 @@
+// f4j_internal.cuh -- shared declarations of libflag4j_cuda.so (not installed).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/flag4j_cuda.h"
+
+struct f4j_buf_s {
+    void* ptr;
+    size_t bytes;
+};
+
+struct f4j_csr_s {
+    int64_t rows, cols, nnz;
+    f4j_buf rowptr, colidx, vals;
+    bool owns;  // true when the handle frees its three buffers
+    // Cached transpose structure, built on first f4j_spmm_t / transpose use:
+    //   t_rowptr int32[cols+1], t_perm int32[nnz] (source nnz of each S^T slot),
+    //   t_rowidx int32[nnz] (row of S for each S^T slot, i.e. S^T's colidx).
+    void* t_rowptr;
+    void* t_perm;
+    void* t_rowidx;
+};
+
+struct f4j_ctx {
+    int device;
+    int sm_count;
+    cudaStream_t stream;
+    bool own_stream;
+    void* ws[4];       // grow-only workspaces (slot 0: bulk, 1: small/stats, 2-3: sparse)
+    size_t ws_bytes[4];
+    int* d_status;     // device status words (bounded-wait timeouts, validation)
+    cudaEvent_t ev[16];
+    bool ev_init[16];
+    int64_t launches;
+};
+
+// ---------------------------------------------------------------- errors
+int f4j_fail(int code, const char* fmt, ...);
+int f4j_cuda_fail(cudaError_t e, const char* what);
+
+#define F4J_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e__ = (call);                                   \
+        if (e__ != cudaSuccess) return f4j_cuda_fail(e__, #call);   \
+    } while (0)
+
+// After a kernel launch: record it and surface launch errors.
+#define F4J_LAUNCHED(ctx)                                                    \
+    do {                                                                     \
+        (ctx)->launches++;                                                   \
+        cudaError_t e__ = cudaGetLastError();                                \
+        if (e__ != cudaSuccess) return f4j_cuda_fail(e__, "kernel launch");  \
+    } while (0)
+
+#define F4J_CHECK_CTX(ctx) \
+    do { if (!(ctx)) return f4j_fail(F4J_ERR_ARG, "null context"); } while (0)
+
+// Workspace slot of at least `bytes` (stream-ordered reuse; growing syncs the
+// stream and discards the slot's previous contents).
+int f4j_workspace(f4j_ctx* ctx, int slot, size_t bytes, void** out);
+// Device allocation helpers (stream-ordered pool).
+int f4j_dev_alloc(f4j_ctx* ctx, size_t bytes, void** out);
+void f4j_dev_free(f4j_ctx* ctx, void* p);
+// Reads and clears status word `idx` (synchronises the stream).
+int f4j_status_take(f4j_ctx* ctx, int idx, int* value);
+
+// Shape error text of Flag4j's ErrorMessages.matMultShapeErrMsg
+// (src/main/java/org/flag4j/util/ErrorMessages.java:52-53, :162-164).
+int f4j_shape_error(int64_t r1, int64_t c1, int64_t r2, int64_t c2);
+
+// Status word slots.
+enum { F4J_ST_TIMEOUT = 0, F4J_ST_CSR_ROW = 1, F4J_ST_CSR_COL = 2, F4J_ST_NONFINITE = 3,
+       F4J_ST_CSR_NEG = 4, F4J_ST_COO_ROW = 5, F4J_ST_COO_COL = 6, F4J_ST_WORDS = 16 };
+
+// TMA descriptor encode (driver entry point, no libcuda link).
+typedef CUresult (*f4j_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                        const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                        const cuuint32_t*, CUtensorMapInterleave,
+                                        CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                        CUtensorMapFloatOOBfill);
+f4j_encode_tiled_fn f4j_encode_fn();
+
+static inline int64_t f4j_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+static inline bool f4j_aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Internal GEMM entry points shared by the dense front ends.
+int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
+                  int opA, const double* B, int opB, double* C, int mode, f4j_report* rep);
+int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
+                  int opA, const double* B, int opB, double* C);
+int f4j_gemm_exact(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
+                   int opA, const double* B, int opB, double* C);
+int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
+                   int opA, const double* B, int opB, double* C, int slices_req,
+                   f4j_report* rep, bool* nonfinite);

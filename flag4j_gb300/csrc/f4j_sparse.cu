@@ -1,0 +1,785 @@
+// f4j_sparse.cu -- CSR products and sparse structure on sm_103a.
+//
+// Products follow the reference loops' per-element order exactly (storage
+// order over a row's nonzeros, product and sum rounded separately), so the
+// results are bit-identical to Flag4j:
+//   SpMV  RealCsrDenseMatMult.standardVector
+//         (src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/real/RealCsrDenseMatMult.java:172-192)
+//   SpMM  RealCsrDenseMatMult.standard (same file :55-82)
+//   S^T X RealCsrOps.transpose + standard (…/sparse/csr/real/RealCsrOps.java:195-225)
+// Structure (COO->CSR, stable COO sort, transpose permutation) is integer
+// work done with histograms, scans and a stable LSD radix sort.
+#include <vector>
+
+#include "f4j_internal.cuh"
+
+namespace {
+
+// ------------------------------------------------------------------ SpMV
+// Thread per row (bit-exact sequential sum); each warp stages its rows'
+// nonzeros through shared memory in coalesced chunks.
+constexpr int SPMV_WARPS = 8, SPMV_CHUNK = 128;
+
+__global__ void __launch_bounds__(SPMV_WARPS * 32)
+    k_spmv(int64_t rows, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+           const double* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
+    __shared__ int scol[SPMV_WARPS][SPMV_CHUNK];
+    __shared__ double sval[SPMV_WARPS][SPMV_CHUNK];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int64_t wrow0 = ((int64_t)blockIdx.x * SPMV_WARPS + warp) * 32;
+    if (wrow0 >= rows) return;
+    const int64_t row = wrow0 + lane;
+    const int64_t wrow1 = wrow0 + 32 < rows ? wrow0 + 32 : rows;
+    const int p0 = rowptr[wrow0], p1 = rowptr[wrow1];
+    int q = 0, qend = 0;
+    if (row < rows) {
+        q = rowptr[row];
+        qend = rowptr[row + 1];
+    }
+    double acc = 0.0;
+    for (int c0 = p0; c0 < p1; c0 += SPMV_CHUNK) {
+        const int cn = (p1 - c0) < SPMV_CHUNK ? (p1 - c0) : SPMV_CHUNK;
+        for (int e = lane; e < cn; e += 32) {
+            scol[warp][e] = colidx[c0 + e];
+            sval[warp][e] = vals[c0 + e];
+        }
+        __syncwarp();
+        const int stop = qend < c0 + cn ? qend : c0 + cn;
+        for (; q < stop; q++) {
+            const int e = q - c0;
+            acc = __dadd_rn(acc, __dmul_rn(sval[warp][e], __ldg(&x[scol[warp][e]])));
+        }
+        __syncwarp();
+    }
+    if (row < rows) y[row] = acc;
+}
+
+// ------------------------------------------------------------------ SpMM
+// A group of G lanes owns one row; each lane owns 2 adjacent columns
+// (128-bit loads of X rows) and sums over the row's nonzeros in storage order.
+// For S^T products the same kernel reads values through the transpose
+// permutation and row indices from the cached S^T structure.
+template <bool VEC2, bool PERM>
+__global__ void __launch_bounds__(256)
+    k_spmm(int64_t rows, int64_t ncols, int G, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+           const double* __restrict__ vals, const int* __restrict__ perm, const double* __restrict__ X,
+           double* __restrict__ Y) {
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x % G;
+    const int64_t row = gid;
+    if (row >= rows) return;
+    const int q0 = rowptr[row], q1 = rowptr[row + 1];
+    constexpr int W = VEC2 ? 2 : 1;
+    for (int64_t cbase = (int64_t)lane * W; cbase < ncols; cbase += (int64_t)G * W) {
+        double a0 = 0.0, a1 = 0.0;
+        int q = q0;
+        for (; q + 4 <= q1; q += 4) {
+            int c[4];
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = __ldg(&colidx[q + u]);
+                v[u] = PERM ? __ldg(&vals[__ldg(&perm[q + u])]) : __ldg(&vals[q + u]);
+            }
+            if (VEC2) {
+                double2 xv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) xv[u] = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c[u] * ncols + cbase));
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u].x));
+                    a1 = __dadd_rn(a1, __dmul_rn(v[u], xv[u].y));
+                }
+            } else {
+                double xv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) xv[u] = __ldg(X + (int64_t)c[u] * ncols + cbase);
+#pragma unroll
+                for (int u = 0; u < 4; u++) a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u]));
+            }
+        }
+        for (; q < q1; q++) {
+            const int c = __ldg(&colidx[q]);
+            const double v = PERM ? __ldg(&vals[__ldg(&perm[q])]) : __ldg(&vals[q]);
+            if (VEC2) {
+                const double2 xv = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c * ncols + cbase));
+                a0 = __dadd_rn(a0, __dmul_rn(v, xv.x));
+                a1 = __dadd_rn(a1, __dmul_rn(v, xv.y));
+            } else {
+                a0 = __dadd_rn(a0, __dmul_rn(v, __ldg(X + (int64_t)c * ncols + cbase)));
+            }
+        }
+        if (VEC2) *reinterpret_cast<double2*>(Y + row * ncols + cbase) = make_double2(a0, a1);
+        else Y[row * ncols + cbase] = a0;
+    }
+}
+
+// ------------------------------------------------------------------ SDDMM
+// Warp per row of S; half-warps take alternate nonzeros; a lane owns 4
+// columns of each 64-column pass (sequential), then a 16-lane tree sum.
+__global__ void __launch_bounds__(256)
+    k_sddmm(int64_t rows, int64_t ncols, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+            const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ out) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32, half = lane / 16, l16 = lane % 16;
+    if (row >= rows) return;
+    const int q0 = rowptr[row], q1 = rowptr[row + 1];
+    const double* arow = A + row * ncols;
+    for (int qb = q0; qb < q1; qb += 2) {
+        const int q = qb + half;
+        double s = 0.0;
+        if (q < q1) {
+            const double* brow = B + (int64_t)__ldg(&colidx[q]) * ncols;
+            for (int64_t c0 = 0; c0 < ncols; c0 += 64) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int64_t c = c0 + l16 * 4 + u;
+                    if (c < ncols) s = fma(__ldg(&arow[c]), __ldg(&brow[c]), s);
+                }
+            }
+        }
+        for (int off = 8; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (q < q1 && l16 == 0) out[q] = s;
+    }
+}
+
+// ------------------------------------------------------------------ structure
+__global__ void k_count(int64_t n, const int* __restrict__ idx, int* __restrict__ counts_plus1) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&counts_plus1[idx[i] + 1], 1);
+}
+
+// Range check of COO indices: records the first offending position.
+__global__ void k_check_range(int64_t n, const int* __restrict__ idx, int64_t limit, int* __restrict__ first_bad) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int v = idx[i];
+        if (v < 0 || v >= limit) atomicMin(first_bad, (int)i);
+    }
+}
+
+// SparseValidation.validateCsr checks (src/main/java/org/flag4j/arrays/sparse/SparseValidation.java:151-206):
+// first row with negative start or decreasing pointers, first bad column.
+__global__ void k_validate_csr(int64_t rows, int64_t cols, int64_t nnz, const int* __restrict__ rowptr,
+                               const int* __restrict__ colidx, int* __restrict__ bad_row,
+                               int* __restrict__ bad_col) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+        int s = rowptr[i], e = rowptr[i + 1];
+        if (s < 0 || s > e) {
+            atomicMin(bad_row, (int)i);
+            continue;
+        }
+        for (int q = s; q < e && q < nnz; q++) {
+            int c = colidx[q];
+            if (c < 0 || c >= cols) {
+                atomicMin(bad_col, q);
+                break;
+            }
+        }
+    }
+}
+
+__global__ void k_expand_rows(int64_t rows, const int* __restrict__ rowptr, int* __restrict__ rowidx) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= rows) return;
+    for (int q = rowptr[row] + lane; q < rowptr[row + 1]; q += 32) rowidx[q] = (int)row;
+}
+
+__global__ void k_iota(int64_t n, int* __restrict__ v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = (int)i;
+}
+
+template <typename T>
+__global__ void k_gather(int64_t n, const int* __restrict__ perm, const T* __restrict__ src, T* __restrict__ dst) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+// ---------------- inclusive scan (int32), 1024 threads x 4 items per block
+constexpr int SCAN_T = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_T * SCAN_IPT;
+
+__device__ __forceinline__ int block_scan_incl(int v, int* sh) {
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    for (int off = 1; off < 32; off <<= 1) {
+        int o = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += o;
+    }
+    if (lane == 31) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        int w = sh[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            int o = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += o;
+        }
+        sh[lane] = w;
+    }
+    __syncthreads();
+    if (warp > 0) v += sh[warp - 1];
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_tiles(int64_t n, int* __restrict__ data, int* __restrict__ sums) {
+    __shared__ int sh[32];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+    int v[SCAN_IPT];
+    int t = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        v[i] = (base + i < n) ? data[base + i] : 0;
+        t += v[i];
+    }
+    int incl = block_scan_incl(t, sh);
+    int run = incl - t;
+#pragma unroll
+    for (int i = 0; i < SCAN_IPT; i++) {
+        run += v[i];
+        if (base + i < n) data[base + i] = run;
+    }
+    if (threadIdx.x == SCAN_T - 1) sums[blockIdx.x] = incl;
+}
+
+__global__ void k_scan_add(int64_t n, int* __restrict__ data, const int* __restrict__ sums) {
+    if (blockIdx.x == 0) return;
+    const int add = sums[blockIdx.x - 1];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    for (int i = threadIdx.x; i < SCAN_TILE; i += blockDim.x)
+        if (base + i < n) data[base + i] += add;
+}
+
+// ---------------- stable LSD radix sort of (key, value) pairs, 8-bit digits
+constexpr int RS_T = 256, RS_SUB = 16, RS_TILE = RS_T * RS_SUB;  // 4096 items per block
+
+__global__ void __launch_bounds__(RS_T) k_radix_hist(int64_t n, const unsigned* __restrict__ keys, int shift,
+                                                     int* __restrict__ hist, int nblocks) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int i = threadIdx.x; i < RS_TILE; i += RS_T)
+        if (base + i < n) atomicAdd(&h[(keys[base + i] >> shift) & 255], 1);
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// hist holds inclusive scan over [digit][block]; block b's start for digit d
+// is incl[d*nb + b] - count.  Items are ranked stably: sub-tile order, then
+// warp order, then lane order.
+__global__ void __launch_bounds__(RS_T) k_radix_scatter(int64_t n, const unsigned* __restrict__ keys_in,
+                                                        const int* __restrict__ vals_in, int shift,
+                                                        const int* __restrict__ incl, const int* __restrict__ cnt,
+                                                        int nblocks, unsigned* __restrict__ keys_out,
+                                                        int* __restrict__ vals_out) {
+    __shared__ int run[256];       // running output position per digit
+    __shared__ int wcount[8][256];  // per-warp digit counts of the current sub-tile
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    {
+        const int64_t idx = (int64_t)threadIdx.x * nblocks + blockIdx.x;
+        run[threadIdx.x] = incl[idx] - cnt[idx];
+    }
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int sub = 0; sub < RS_SUB; sub++) {
+        for (int w = 0; w < 8; w++) wcount[w][threadIdx.x] = 0;
+        __syncthreads();
+        const int64_t i = base + (int64_t)sub * RS_T + threadIdx.x;
+        const bool valid = i < n;
+        unsigned key = valid ? keys_in[i] : 0u;
+        int val = valid ? vals_in[i] : 0;
+        int d = valid ? (int)((key >> shift) & 255) : 256 + lane;  // invalid lanes get unique dummies
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int rank_in_warp = __popc(peers & ((1u << lane) - 1));
+        if (valid && rank_in_warp == 0) wcount[warp][d] = __popc(peers);
+        __syncthreads();
+        int pos = 0;
+        if (valid) {
+            int before = 0;
+            for (int w = 0; w < warp; w++) before += wcount[w][d];
+            pos = run[d] + before + rank_in_warp;
+        }
+        __syncthreads();
+        {
+            int tot = 0;
+            for (int w = 0; w < 8; w++) tot += wcount[w][threadIdx.x];
+            run[threadIdx.x] += tot;
+        }
+        if (valid) {
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host helpers
+static int grid1(int64_t n, int t = 256) {
+    int64_t b = (n + t - 1) / t;
+    if (b < 1) b = 1;
+    if (b > 1 << 20) b = 1 << 20;
+    return (int)b;
+}
+
+// In-place inclusive scan of int32 data[n] (recursive over tile sums).
+static int scan_inclusive(f4j_ctx* ctx, int* data, int64_t n) {
+    if (n <= 0) return F4J_OK;
+    const int64_t tiles = f4j_cdiv(n, SCAN_TILE);
+    int* sums = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)tiles * sizeof(int), (void**)&sums);
+    if (rc) return rc;
+    k_scan_tiles<<<(unsigned)tiles, SCAN_T, 0, ctx->stream>>>(n, data, sums);
+    F4J_LAUNCHED(ctx);
+    if (tiles > 1) {
+        rc = scan_inclusive(ctx, sums, tiles);
+        if (rc) {
+            f4j_dev_free(ctx, sums);
+            return rc;
+        }
+        k_scan_add<<<(unsigned)tiles, 256, 0, ctx->stream>>>(n, data, sums);
+        F4J_LAUNCHED(ctx);
+    }
+    f4j_dev_free(ctx, sums);
+    return F4J_OK;
+}
+
+// Stable sort of (keys, vals) by the low `bits` bits of keys; result in place.
+static int radix_sort_pairs(f4j_ctx* ctx, unsigned* keys, int* vals, int64_t n, int bits) {
+    if (n <= 1 || bits <= 0) return F4J_OK;
+    const int nb = (int)f4j_cdiv(n, RS_TILE);
+    unsigned* k2 = nullptr;
+    int* v2 = nullptr;
+    int *hist = nullptr, *cnt = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)n * 4, (void**)&k2);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)n * 4, (void**)&v2);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)256 * nb * 4, (void**)&hist);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)256 * nb * 4, (void**)&cnt);
+    unsigned *ka = keys, *kb = k2;
+    int *va = vals, *vb = v2;
+    for (int shift = 0; !rc && shift < bits; shift += 8) {
+        k_radix_hist<<<nb, RS_T, 0, ctx->stream>>>(n, ka, shift, hist, nb);
+        F4J_LAUNCHED(ctx);
+        cudaMemcpyAsync(cnt, hist, (size_t)256 * nb * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        rc = scan_inclusive(ctx, hist, (int64_t)256 * nb);
+        if (rc) break;
+        k_radix_scatter<<<nb, RS_T, 0, ctx->stream>>>(n, ka, va, shift, hist, cnt, nb, kb, vb);
+        F4J_LAUNCHED(ctx);
+        unsigned* tk = ka; ka = kb; kb = tk;
+        int* tv = va; va = vb; vb = tv;
+    }
+    if (!rc && ka != keys) {
+        cudaMemcpyAsync(keys, ka, (size_t)n * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(vals, va, (size_t)n * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    f4j_dev_free(ctx, k2);
+    f4j_dev_free(ctx, v2);
+    f4j_dev_free(ctx, hist);
+    f4j_dev_free(ctx, cnt);
+    return rc;
+}
+
+static int bits_for(int64_t maxval) {
+    int b = 0;
+    while (b < 31 && (1ll << b) <= maxval) b++;
+    return b;
+}
+
+// Builds the cached transpose structure of S (RealCsrOps.transpose order).
+static int ensure_transpose(f4j_ctx* ctx, f4j_csr S) {
+    if (S->t_perm) return F4J_OK;
+    const int64_t nnz = S->nnz, rows = S->rows, cols = S->cols;
+    int *trp = nullptr, *perm = nullptr, *trow = nullptr;
+    unsigned* keys = nullptr;
+    int* rowidx = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)(cols + 1) * 4, (void**)&trp);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&perm);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&trow);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&keys);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&rowidx);
+    if (rc) goto fail;
+    // pointers of S^T: column counts, inclusive scan (as RealCsrOps.transpose :203-211)
+    F4J_CUDA(cudaMemsetAsync(trp, 0, (size_t)(cols + 1) * 4, ctx->stream));
+    if (nnz) {
+        k_count<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)S->colidx->ptr, trp);
+        F4J_LAUNCHED(ctx);
+        rc = scan_inclusive(ctx, trp + 1, cols);
+        if (rc) goto fail;
+        // stable order by column == scatter in storage order (:216-222)
+        F4J_CUDA(cudaMemcpyAsync(keys, S->colidx->ptr, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        k_iota<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm);
+        F4J_LAUNCHED(ctx);
+        rc = radix_sort_pairs(ctx, keys, perm, nnz, bits_for(cols - 1));
+        if (rc) goto fail;
+        k_expand_rows<<<grid1(rows * 32), 256, 0, ctx->stream>>>(rows, (const int*)S->rowptr->ptr, rowidx);
+        F4J_LAUNCHED(ctx);
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, rowidx, trow);
+        F4J_LAUNCHED(ctx);
+    }
+    f4j_dev_free(ctx, keys);
+    f4j_dev_free(ctx, rowidx);
+    S->t_rowptr = trp;
+    S->t_perm = perm;
+    S->t_rowidx = trow;
+    return F4J_OK;
+fail:
+    f4j_dev_free(ctx, trp);
+    f4j_dev_free(ctx, perm);
+    f4j_dev_free(ctx, trow);
+    f4j_dev_free(ctx, keys);
+    f4j_dev_free(ctx, rowidx);
+    return rc;
+}
+
+static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp, const int* ci, const double* v,
+                       const int* perm, const double* X, double* Y) {
+    if (rows == 0 || ncols == 0) return F4J_OK;
+    const bool vec2 = (ncols % 2 == 0) && f4j_aligned16(X) && f4j_aligned16(Y);
+    const int64_t per_lane = vec2 ? 2 : 1;
+    int G = 1;
+    while (G < 32 && G * per_lane < ncols) G *= 2;
+    const int64_t threads = rows * G;
+    const unsigned blocks = (unsigned)f4j_cdiv(threads, 256);
+    if (vec2) {
+        if (perm) k_spmm<true, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+        else k_spmm<true, false><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+    } else {
+        if (perm) k_spmm<false, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+        else k_spmm<false, false><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+    }
+    F4J_LAUNCHED(ctx);
+    return F4J_OK;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowptr, f4j_buf colidx,
+                            f4j_buf vals, int validate, f4j_csr* out) {
+    F4J_CHECK_CTX(ctx);
+    if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!rowptr || !colidx || !vals) return f4j_fail(F4J_ERR_ARG, "null CSR buffer");
+    if (rows < 0 || cols < 0 || nnz < 0) return f4j_fail(F4J_ERR_ARG, "negative CSR size");
+    if (rows > INT32_MAX || cols > INT32_MAX || nnz > INT32_MAX)
+        return f4j_fail(F4J_ERR_ARG, "CSR sizes exceed Flag4j's int range");
+    if ((int64_t)rows * cols < nnz)
+        return f4j_fail(F4J_ERR_CSR,
+                        "The number of non-zero entries cannot be greater than the total number of entries in the "
+                        "matrix but got nnz=%lld and totalEntries=%lld",
+                        (long long)nnz, (long long)(rows * cols));
+    if (rowptr->bytes < (size_t)(rows + 1) * 4)
+        return f4j_fail(F4J_ERR_CSR, "Expecting rowPointers to have length (numRows + 1)=%lld", (long long)(rows + 1));
+    if (colidx->bytes < (size_t)nnz * 4 || vals->bytes < (size_t)nnz * 8)
+        return f4j_fail(F4J_ERR_CSR, "column index / value buffers shorter than nnz=%lld", (long long)nnz);
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    if (validate) {
+        void* ws;
+        int rc = f4j_workspace(ctx, 2, 64, &ws);
+        if (rc) return rc;
+        int h[4] = {INT32_MAX, INT32_MAX, 0, 0};
+        F4J_CUDA(cudaMemcpyAsync(ws, h, 8, cudaMemcpyHostToDevice, ctx->stream));
+        if (rows) {
+            k_validate_csr<<<grid1(rows), 256, 0, ctx->stream>>>(rows, cols, nnz, (const int*)rowptr->ptr,
+                                                                 (const int*)colidx->ptr, (int*)ws, (int*)ws + 1);
+            F4J_LAUNCHED(ctx);
+        }
+        int first_last[2] = {0, 0};
+        F4J_CUDA(cudaMemcpyAsync(h, ws, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaMemcpyAsync(&first_last[0], rowptr->ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaMemcpyAsync(&first_last[1], (int*)rowptr->ptr + rows, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (h[0] != INT32_MAX) {
+            int p[2];
+            cudaMemcpy(p, (int*)rowptr->ptr + h[0], 8, cudaMemcpyDeviceToHost);
+            if (p[0] < 0)
+                return f4j_fail(F4J_ERR_CSR, "All rowPointers must be positive but got %d at index %d.", p[0], h[0]);
+            return f4j_fail(F4J_ERR_CSR,
+                            "rowPointers must be monotonically increasing but got values %d and %d at indices %d "
+                            "and %d.",
+                            p[0], p[1], h[0], h[0] + 1);
+        }
+        if (h[1] != INT32_MAX) {
+            int c = 0;
+            cudaMemcpy(&c, (int*)colidx->ptr + h[1], 4, cudaMemcpyDeviceToHost);
+            return f4j_fail(F4J_ERR_CSR, "Invalid column index [%d] encountered for CSR matrix of shape (%lld, %lld)", c,
+                            (long long)rows, (long long)cols);
+        }
+        if ((int64_t)first_last[1] - first_last[0] != nnz)
+            return f4j_fail(F4J_ERR_CSR, "rowIndices specifies %lld elements but nnz=%lld. These values must be equal.",
+                            (long long)((int64_t)first_last[1] - first_last[0]), (long long)nnz);
+    }
+    *out = new f4j_csr_s{rows, cols, nnz, rowptr, colidx, vals, false, nullptr, nullptr, nullptr};
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_free(f4j_ctx* ctx, f4j_csr S) {
+    F4J_CHECK_CTX(ctx);
+    if (!S) return F4J_OK;
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(S->t_rowptr);
+    cudaFree(S->t_perm);
+    cudaFree(S->t_rowidx);
+    if (S->owns) {
+        f4j_buf_free(ctx, S->rowptr);
+        f4j_buf_free(ctx, S->colidx);
+        f4j_buf_free(ctx, S->vals);
+    }
+    delete S;
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_info(f4j_csr S, int64_t* rows, int64_t* cols, int64_t* nnz) {
+    if (!S) return f4j_fail(F4J_ERR_ARG, "null CSR handle");
+    if (rows) *rows = S->rows;
+    if (cols) *cols = S->cols;
+    if (nnz) *nnz = S->nnz;
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_buffers(f4j_csr S, f4j_buf* rowptr, f4j_buf* colidx, f4j_buf* vals) {
+    if (!S) return f4j_fail(F4J_ERR_ARG, "null CSR handle");
+    if (rowptr) *rowptr = S->rowptr;
+    if (colidx) *colidx = S->colidx;
+    if (vals) *vals = S->vals;
+    return F4J_OK;
+}
+
+static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_csr* out) {
+    f4j_buf rp = nullptr, ci = nullptr, v = nullptr;
+    int rc = f4j_buf_alloc(ctx, (size_t)(rows + 1) * 4, &rp);
+    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 4, &ci);
+    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 8, &v);
+    if (rc) {
+        f4j_buf_free(ctx, rp);
+        f4j_buf_free(ctx, ci);
+        f4j_buf_free(ctx, v);
+        return rc;
+    }
+    *out = new f4j_csr_s{rows, cols, nnz, rp, ci, v, true, nullptr, nullptr, nullptr};
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowidx, f4j_buf colidx,
+                                f4j_buf vals, f4j_csr* out) {
+    F4J_CHECK_CTX(ctx);
+    if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!rowidx || !colidx || !vals) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
+    if (rows < 0 || cols < 0 || nnz < 0 || rows > INT32_MAX || cols > INT32_MAX || nnz > INT32_MAX)
+        return f4j_fail(F4J_ERR_ARG, "bad COO sizes");
+    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || vals->bytes < (size_t)nnz * 8)
+        return f4j_fail(F4J_ERR_CSR,
+                        "The number of non-zero entries must match the number of row and column indices");
+    if ((int64_t)rows * cols < nnz)
+        return f4j_fail(F4J_ERR_CSR, "The number of non-zero entries cannot be greater than the total number of entries");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    // SparseValidation.validateCoo (…/SparseValidation.java:70-98): indices in range.
+    void* ws;
+    int rc = f4j_workspace(ctx, 2, 64, &ws);
+    if (rc) return rc;
+    int h[2] = {INT32_MAX, INT32_MAX};
+    F4J_CUDA(cudaMemcpyAsync(ws, h, 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (nnz) {
+        k_check_range<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)rowidx->ptr, rows, (int*)ws);
+        F4J_LAUNCHED(ctx);
+        k_check_range<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)colidx->ptr, cols, (int*)ws + 1);
+        F4J_LAUNCHED(ctx);
+    }
+    F4J_CUDA(cudaMemcpyAsync(h, ws, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h[0] != INT32_MAX || h[1] != INT32_MAX) {
+        int at = h[0] < h[1] ? h[0] : h[1];
+        int rc2[2];
+        cudaMemcpy(&rc2[0], (int*)rowidx->ptr + at, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&rc2[1], (int*)colidx->ptr + at, 4, cudaMemcpyDeviceToHost);
+        return f4j_fail(F4J_ERR_CSR, "Invalid index [%d, %d] encountered for COO matrix of shape (%lld, %lld)", rc2[0],
+                        rc2[1], (long long)rows, (long long)cols);
+    }
+    f4j_csr S;
+    rc = alloc_owned_csr(ctx, rows, cols, nnz, &S);
+    if (rc) return rc;
+    int* rp = (int*)S->rowptr->ptr;
+    // CooMatrix.toCsr (…/CooMatrix.java:457-470): count per row into rp[r+1], inclusive scan.
+    F4J_CUDA(cudaMemsetAsync(rp, 0, (size_t)(rows + 1) * 4, ctx->stream));
+    if (nnz) {
+        k_count<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)rowidx->ptr, rp);
+        F4J_LAUNCHED(ctx);
+    }
+    rc = scan_inclusive(ctx, rp + 1, rows);
+    if (rc) {
+        f4j_csr_free(ctx, S);
+        return rc;
+    }
+    F4J_CUDA(cudaMemcpyAsync(S->colidx->ptr, colidx->ptr, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    F4J_CUDA(cudaMemcpyAsync(S->vals->ptr, vals->ptr, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    *out = S;
+    return F4J_OK;
+}
+
+extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
+    F4J_CHECK_CTX(ctx);
+    if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
+    if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
+    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || (vals && vals->bytes < (size_t)nnz * 8))
+        return f4j_fail(F4J_ERR_ARG, "COO buffers shorter than nnz");
+    if (nnz <= 1) return F4J_OK;
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    unsigned* keys = nullptr;
+    int *perm = nullptr, *tmp = nullptr;
+    double* vtmp = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&keys);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&perm);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&tmp);
+    if (!rc && vals) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&vtmp);
+    if (!rc) {
+        // LSD: stable by column, then stable by row == stable lexicographic (row, col).
+        k_iota<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm);
+        cudaMemcpyAsync(keys, colidx->ptr, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        rc = radix_sort_pairs(ctx, keys, perm, nnz, 31);
+    }
+    if (!rc) {
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)rowidx->ptr, (int*)keys);
+        rc = radix_sort_pairs(ctx, keys, perm, nnz, 31);
+    }
+    if (!rc) {
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)rowidx->ptr, tmp);
+        cudaMemcpyAsync(rowidx->ptr, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)colidx->ptr, tmp);
+        cudaMemcpyAsync(colidx->ptr, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (vals) {
+            k_gather<double><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const double*)vals->ptr, vtmp);
+            cudaMemcpyAsync(vals->ptr, vtmp, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+        }
+        ctx->launches += vals ? 5 : 4;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
+    }
+    f4j_dev_free(ctx, keys);
+    f4j_dev_free(ctx, perm);
+    f4j_dev_free(ctx, tmp);
+    f4j_dev_free(ctx, vtmp);
+    return rc;
+}
+
+extern "C" int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int rc = ensure_transpose(ctx, S);
+    if (rc) return rc;
+    f4j_csr T;
+    rc = alloc_owned_csr(ctx, S->cols, S->rows, S->nnz, &T);
+    if (rc) return rc;
+    F4J_CUDA(cudaMemcpyAsync(T->rowptr->ptr, S->t_rowptr, (size_t)(S->cols + 1) * 4, cudaMemcpyDeviceToDevice,
+                             ctx->stream));
+    F4J_CUDA(cudaMemcpyAsync(T->colidx->ptr, S->t_rowidx, (size_t)S->nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (S->nnz) {
+        k_gather<double><<<grid1(S->nnz), 256, 0, ctx->stream>>>(S->nnz, (const int*)S->t_perm,
+                                                                 (const double*)S->vals->ptr, (double*)T->vals->ptr);
+        F4J_LAUNCHED(ctx);
+    }
+    *out = T;
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !perm_out) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (perm_out->bytes < (size_t)S->nnz * 4) return f4j_fail(F4J_ERR_ARG, "perm buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int rc = ensure_transpose(ctx, S);
+    if (rc) return rc;
+    F4J_CUDA(cudaMemcpyAsync(perm_out->ptr, S->t_perm, (size_t)S->nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    return F4J_OK;
+}
+
+extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !x || !y) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (x->bytes < (size_t)S->cols * 8)
+        return f4j_fail(F4J_ERR_ARG, "Expecting values to be equal but got: [%lld, %lld]", (long long)S->cols,
+                        (long long)(x->bytes / 8));
+    if (y->bytes < (size_t)S->rows * 8) return f4j_fail(F4J_ERR_ARG, "y buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    if (S->rows) {
+        const unsigned blocks = (unsigned)f4j_cdiv(S->rows, SPMV_WARPS * 32);
+        k_spmv<<<blocks, SPMV_WARPS * 32, 0, ctx->stream>>>(S->rows, (const int*)S->rowptr->ptr,
+                                                            (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
+                                                            (const double*)x->ptr, (double*)y->ptr);
+        F4J_LAUNCHED(ctx);
+    }
+    if (rep) {
+        *rep = f4j_report{};
+        rep->flops = 2.0 * S->nnz;
+        rep->bytes = 12.0 * S->nnz + 4.0 * (S->rows + 1) + 8.0 * S->cols + 8.0 * S->rows;
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}
+
+extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !X || !Y) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
+    if (X->bytes < (size_t)S->cols * ncols * 8) return f4j_fail(F4J_ERR_ARG, "X buffer too small");
+    if (Y->bytes < (size_t)S->rows * ncols * 8) return f4j_fail(F4J_ERR_ARG, "Y buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    int rc = launch_spmm(ctx, S->rows, ncols, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr,
+                         (const double*)S->vals->ptr, nullptr, (const double*)X->ptr, (double*)Y->ptr);
+    if (rc) return rc;
+    if (rep) {
+        *rep = f4j_report{};
+        rep->flops = 2.0 * S->nnz * ncols;
+        rep->bytes = 12.0 * S->nnz + 4.0 * (S->rows + 1) + 8.0 * ncols * (S->cols + S->rows);
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}
+
+extern "C" int f4j_spmm_t(f4j_ctx* ctx, f4j_csr S, f4j_buf dC, int64_t ncols, f4j_buf dX, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !dC || !dX) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
+    if (dC->bytes < (size_t)S->rows * ncols * 8) return f4j_fail(F4J_ERR_ARG, "dC buffer too small");
+    if (dX->bytes < (size_t)S->cols * ncols * 8) return f4j_fail(F4J_ERR_ARG, "dX buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    int rc = ensure_transpose(ctx, S);
+    if (rc) return rc;
+    rc = launch_spmm(ctx, S->cols, ncols, (const int*)S->t_rowptr, (const int*)S->t_rowidx,
+                     (const double*)S->vals->ptr, (const int*)S->t_perm, (const double*)dC->ptr, (double*)dX->ptr);
+    if (rc) return rc;
+    if (rep) {
+        *rep = f4j_report{};
+        rep->flops = 2.0 * S->nnz * ncols;
+        rep->bytes = 16.0 * S->nnz + 4.0 * (S->cols + 1) + 8.0 * ncols * (S->cols + S->rows);
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}
+
+extern "C" int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t ncols, f4j_buf out,
+                         f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !A || !B || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
+    if (A->bytes < (size_t)S->rows * ncols * 8) return f4j_fail(F4J_ERR_ARG, "A buffer too small");
+    if (B->bytes < (size_t)S->cols * ncols * 8) return f4j_fail(F4J_ERR_ARG, "B buffer too small");
+    if (out->bytes < (size_t)S->nnz * 8) return f4j_fail(F4J_ERR_ARG, "output buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    if (S->rows && S->nnz) {
+        k_sddmm<<<(unsigned)f4j_cdiv(S->rows * 32, 256), 256, 0, ctx->stream>>>(
+            S->rows, ncols, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)A->ptr,
+            (const double*)B->ptr, (double*)out->ptr);
+        F4J_LAUNCHED(ctx);
+    }
+    if (rep) {
+        *rep = f4j_report{};
+        rep->flops = 2.0 * S->nnz * ncols;
+        rep->bytes = 12.0 * S->nnz + 4.0 * (S->rows + 1) + 8.0 * ncols * (S->rows + S->cols);
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}

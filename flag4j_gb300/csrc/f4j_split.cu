@@ -1,0 +1,645 @@
+// f4j_split.cu -- FP64-accurate split-precision GEMM on tcgen05 FP8 tensor cores.
+//
+// Scheme (Ozaki-style error-free slicing):
+//  1. k_stats_*: per row of op(A) and per column of op(B), the power-of-two
+//     bound 2^e > max|x| and the exponent spread (bits between the largest and
+//     the mean element exponent).  The host picks the slice count s from the
+//     spread.
+//  2. k_split: every element becomes a fixed-point integer Y = round(x 2^(F-e))
+//     (F = 4 + 5(s-1) bits, pure integer arithmetic on the IEEE bits), cut
+//     into s balanced digits d_1 in [-16,16], d_2..d_s in [-16,15]; each digit
+//     is exactly representable in E4M3.  Slices are written K-major
+//     (rows x Kp bytes), one plane per slice.
+//  3. k_split_gemm: for each output tile, the products A_i B_j with
+//     i + j <= s + 1 run as tcgen05.mma kind::f8f6f4 with FP32 accumulation in
+//     TMEM.  Products of one "round" share a weight; a round is sized so that
+//     its sum of |d_a d_b| <= 2^24, so the FP32 accumulator holds the exact
+//     integer.  Epilogue warps read each round from TMEM, convert to int64 and
+//     add it (shifted by the round weight) into 64-bit fixed-point registers;
+//     the only FP64 work is the final int64 -> double and the 2^(e_i + e_j)
+//     scale.
+// Complex: op(A)_cat = [Re op(A) | Im op(A)], op(B)_cat = [[Re, Im], [-Im, Re]]
+// so one real product of size m x 2n x 2k gives [Cr | Ci] (the four real
+// products of Complex128.mult, src/main/java/org/flag4j/numbers/Complex128.java:336-341).
+#include <cstdlib>
+#include <vector>
+
+#include "f4j_internal.cuh"
+#include "f4j_ptx.cuh"
+
+namespace {
+
+constexpr int S_MAX = 14;          // at most 14 slices (4 + 65 = 69 bits)
+constexpr int BM = 128, BN = 128;  // output tile
+constexpr int BKB = 128;           // K bytes per stage (one 128B swizzle row)
+constexpr int STAGES = 6;
+constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns
+constexpr int TILE_BYTES = BM * BKB;  // 16 KB (A) and 16 KB (B) per stage
+constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
+constexpr int MAX_ROUNDS = 256;
+
+struct Round {
+    uint8_t level;   // t = i + j
+    uint8_t i0, i1;  // A slices i0..i1-1 (1-based), B slice t - i
+    int8_t shift;    // left shift of this round's integer into the fixed-point accumulator
+    int32_t kb0, kb1;  // K blocks [kb0, kb1)
+};
+
+struct SplitGemmParams {
+    int M, N, Kp;           // cat sizes; Kp multiple of 128
+    int nrounds;
+    int cplx;               // 1: C interleaved complex, N = 2n
+    int n_out;              // n (complex output columns) or N
+    int ubits;              // fixed-point unit exponent: value = acc * 2^(ubits + ea + eb)
+    const int* ea;          // [M]
+    const int* eb;          // [N]
+    double* C;
+    int* status;
+    Round rounds[MAX_ROUNDS];
+};
+
+// ------------------------------------------------------------------ stats
+__device__ __forceinline__ void stat_elem(double x, unsigned long long& mx, long long& esum, int& cnt, int& bad) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    int E = (int)(b >> 52);
+    if (E == 2047) bad = 1;
+    if (b > mx) mx = b;
+    if (b) {
+        esum += (E ? E : 1) - 1023;
+        cnt++;
+    }
+}
+
+// One warp per stored row: stats of stored rows.
+__global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
+                             unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
+                             int* __restrict__ cnt_out, int* __restrict__ bad_out) {
+    int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x % 32;
+    if (r >= rows) return;
+    unsigned long long mx = 0;
+    long long es = 0;
+    int cnt = 0, bad = 0;
+    int64_t w = cplx ? 2 * cols : cols;
+    const double* row = X + r * w;
+    for (int64_t c = lane; c < w; c += 32) stat_elem(row[c], mx, es, cnt, bad);
+    for (int off = 16; off; off >>= 1) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+        mx = o > mx ? o : mx;
+        es += __shfl_xor_sync(0xffffffffu, es, off);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, off);
+    }
+    if (lane == 0) {
+        mx_out[r] = mx;
+        esum_out[r] = es;
+        cnt_out[r] = cnt;
+        if (bad) atomicExch(bad_out, 1);
+    }
+}
+
+// Thread per stored column, blockIdx.y over 256-row chunks: stats of stored columns.
+__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
+                             unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
+                             int* __restrict__ cnt_out, int* __restrict__ bad_out) {
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    int64_t r0 = (int64_t)blockIdx.y * 256, r1 = r0 + 256 < rows ? r0 + 256 : rows;
+    unsigned long long mx = 0;
+    long long es = 0;
+    int cnt = 0, bad = 0;
+    for (int64_t r = r0; r < r1; r++) {
+        if (cplx) {
+            stat_elem(X[2 * (r * cols + c)], mx, es, cnt, bad);
+            stat_elem(X[2 * (r * cols + c) + 1], mx, es, cnt, bad);
+        } else {
+            stat_elem(X[r * cols + c], mx, es, cnt, bad);
+        }
+    }
+    if (mx) atomicMax(&mx_out[c], mx);
+    if (cnt) {
+        atomicAdd((unsigned long long*)&esum_out[c], (unsigned long long)es);
+        atomicAdd(&cnt_out[c], cnt);
+    }
+    if (bad) atomicExch(bad_out, 1);
+}
+
+// Exponent bound e (max|x| < 2^e) per target, spread (x256, max-reduced).
+__global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long long* __restrict__ mx,
+                                 const long long* __restrict__ esum, const int* __restrict__ cnt,
+                                 int* __restrict__ e_out, int* __restrict__ spread_x256) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int sp = 0;
+    if (t < targets) {
+        unsigned long long b = mx[t];
+        int e = 0;
+        if (b) {
+            int E = (int)(b >> 52);
+            e = E ? E - 1022 : -1022;
+            double mean = (double)esum[t] / (double)cnt[t];
+            double s = (double)(e - 1) - mean;
+            sp = s > 0 ? (int)(s * 256.0 + 0.5) : 0;
+        }
+        e_out[t] = e;
+        if (dup) e_out[t + targets] = e;
+    }
+    for (int off = 16; off; off >>= 1) {
+        int o = __shfl_xor_sync(0xffffffffu, sp, off);
+        sp = o > sp ? o : sp;
+    }
+    if ((threadIdx.x & 31) == 0 && sp) atomicMax(spread_x256, sp);
+}
+
+// ------------------------------------------------------------------ split
+__device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
+    int v = d < 0 ? -d : d;
+    if (v == 0) return 0u;
+    int e = 31 - __clz(v);
+    int mant = (e >= 3) ? ((v >> (e - 3)) & 7) : ((v << (3 - e)) & 7);
+    return (uint32_t)(((e + 7) << 3) | mant | (d < 0 ? 0x80 : 0));
+}
+
+// Fixed-point integer of x relative to 2^e with F fractional bits:
+// round(|x| 2^(F - e)) with the sign of x; |result| <= 2^F.
+__device__ __forceinline__ long long fixed_of(double x, int e, int F) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    bool neg = b >> 63;
+    int E = (int)((b >> 52) & 0x7FF);
+    unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+    if (E) M |= 1ull << 52;
+    else E = 1;
+    int sh = (E - 1075) - e + F;
+    unsigned long long Y;
+    if (M == 0) Y = 0;
+    else if (sh >= 0) Y = M << sh;
+    else if (sh <= -64) Y = 0;
+    else {
+        int rs = -sh;
+        Y = (rs >= 54) ? 0 : ((M + (1ull << (rs - 1))) >> rs);
+    }
+    return neg ? -(long long)Y : (long long)Y;
+}
+
+constexpr int SP_TR = 32, SP_TQ = 64;  // tile: 32 target rows x 64 k-indices
+
+// Writes slices of one operand.  Output plane p (0-based slice) is
+// rows_out x Kp bytes at out + p * rows_out * Kp.
+//   transposed == 0: target row r = stored row, q = stored column
+//   transposed == 1: target row r = stored column, q = stored row
+//   role 0 (A_cat): complex value (re, im) -> out[r][q] = re, out[r][Kh+q] = im
+//   role 1 (B_cat^T): -> out[r][q] = re, out[r][Kh+q] = -im,
+//                        out[n+r][q] = im, out[n+r][Kh+q] = re
+__global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int64_t srows, int64_t scols,
+                                               int transposed, int cplx, int conj, int role,
+                                               int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
+                                               int64_t rows_out, const int* __restrict__ e_t, int s,
+                                               uint8_t* __restrict__ out) {
+    __shared__ double sre[SP_TR][SP_TQ + 1];
+    __shared__ double sim[SP_TR][SP_TQ + 1];
+    const int64_t r0 = (int64_t)blockIdx.y * SP_TR, q0 = (int64_t)blockIdx.x * SP_TQ;
+    // ---- stage the tile (zeros outside the matrix)
+    for (int e = threadIdx.x; e < SP_TR * SP_TQ; e += 256) {
+        int rr, qq;
+        if (!transposed) { rr = e / SP_TQ; qq = e % SP_TQ; }
+        else { qq = e / SP_TR; rr = e % SP_TR; }
+        int64_t r = r0 + rr, q = q0 + qq;
+        double re = 0, im = 0;
+        if (r < targets && q < klen) {
+            int64_t idx = transposed ? (q * scols + r) : (r * scols + q);
+            if (cplx) {
+                re = X[2 * idx];
+                im = X[2 * idx + 1];
+                if (conj) im = -im;
+            } else {
+                re = X[idx];
+            }
+        }
+        sre[rr][qq] = re;
+        sim[rr][qq] = im;
+    }
+    __syncthreads();
+    // ---- each thread: one target row, 8 consecutive q
+    const int rr = threadIdx.x / 8, qs = (threadIdx.x % 8) * 8;
+    const int64_t r = r0 + rr;
+    if (r >= targets) return;
+    const int e = e_t[r];
+    const int F = 4 + 5 * (s - 1);
+    const int nparts = cplx ? (role == 0 ? 2 : 4) : 1;
+    for (int part = 0; part < nparts; part++) {
+        // part: 0 -> (row r, col q) ; 1 -> (row r, col Kh+q) ; 2 -> (row n+r, col q) ; 3 -> (row n+r, col Kh+q)
+        long long Y[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            double v;
+            double a = sre[rr][qs + j], b = sim[rr][qs + j];
+            if (role == 0) v = (part == 0) ? a : b;
+            else v = (part == 0) ? a : (part == 1) ? -b : (part == 2) ? b : a;
+            Y[j] = fixed_of(v, e, F);
+        }
+        const int64_t orow = (part >= 2) ? (targets + r) : r;
+        const int64_t ocol = ((part & 1) ? Kh : 0) + q0 + qs;
+        uint8_t* base = out + orow * Kp + ocol;
+        // digits from the least significant slice up
+        for (int p = s - 1; p >= 0; p--) {
+            uint32_t lo = 0, hi = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int d;
+                if (p == 0) d = (int)Y[j];
+                else {
+                    d = (int)(((Y[j] + 16) & 31) - 16);
+                    Y[j] = (Y[j] - d) >> 5;
+                }
+                uint32_t byte = e4m3_of_digit(d);
+                if (j < 4) lo |= byte << (8 * j);
+                else hi |= byte << (8 * (j - 4));
+            }
+            *reinterpret_cast<uint2*>(base + (int64_t)p * rows_out * Kp) = make_uint2(lo, hi);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ GEMM
+// v * 2^X without a libm call; two in-range factors when X leaves the normal range.
+__device__ __forceinline__ double scale_pow2(double v, int X) {
+    if (X >= -1022 && X <= 1023) return v * __longlong_as_double((long long)(X + 1023) << 52);
+    int X1 = X / 2, X2 = X - X1;
+    X1 = X1 < -1022 ? -1022 : (X1 > 1023 ? 1023 : X1);
+    X2 = X2 < -1022 ? -1022 : (X2 > 1023 ? 1023 : X2);
+    return (v * __longlong_as_double((long long)(X1 + 1023) << 52)) * __longlong_as_double((long long)(X2 + 1023) << 52);
+}
+
+__global__ void __maxnreg__(200)
+    k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 const __grid_constant__ SplitGemmParams p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte alignment for the 128B-swizzled TMA tiles
+    unsigned char* smem = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char* sA = smem;
+    unsigned char* sB = smem + STAGES * TILE_BYTES;
+    __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accfull[NBUF], accempty[NBUF], mma_done;
+    __shared__ uint32_t tmem_base_slot;
+    __shared__ int abort_flag;
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; i++) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < NBUF; i++) {
+            mbar_init(&accfull[i], 1);
+            mbar_init(&accempty[i], 8);
+        }
+        mbar_init(&mma_done, 1);
+        abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(&tmem_base_slot, NBUF * BN);
+        tmem_relinquish();
+    }
+    if (warp == 0 && lane == 0) {
+        prefetch_tmap(&tmA);
+        prefetch_tmap(&tmB);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_slot;
+
+    if (warp == 0) {
+        // ---------------- TMA producer
+        if (lane == 0) {
+            int it = 0;
+            for (int r = 0; r < p.nrounds && !abort_flag; r++) {
+                const Round rd = p.rounds[r];
+                for (int i = rd.i0; i < rd.i1 && !abort_flag; i++) {
+                    const int j = rd.level - i;
+                    for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
+                        const int s = it % STAGES;
+                        const uint32_t ph = (it / STAGES) & 1;
+                        if (it >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.status, 11)) {
+                            abort_flag = 1;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(&full[s], 2 * TILE_BYTES);
+                        tma_load_3d(sA + s * TILE_BYTES, &tmA, &full[s], kb * BKB, m0, i - 1);
+                        tma_load_3d(sB + s * TILE_BYTES, &tmB, &full[s], kb * BKB, n0, j - 1);
+                    }
+                }
+            }
+            // drain the copies still in flight (bounded)
+            int first = it > STAGES ? it - STAGES : 0;
+            for (int q = first; q < it; q++) mbar_wait(&full[q % STAGES], (q / STAGES) & 1, nullptr, 0);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer (one thread)
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
+            int it = 0;
+            for (int r = 0; r < p.nrounds && !abort_flag; r++) {
+                const Round rd = p.rounds[r];
+                const int buf = r % NBUF;
+                if (r >= NBUF && !mbar_wait(&accempty[buf], ((r / NBUF) & 1) ^ 1, p.status, 12)) {
+                    abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem + buf * BN;
+                bool first = true;
+                for (int i = rd.i0; i < rd.i1 && !abort_flag; i++) {
+                    for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
+                        const int s = it % STAGES;
+                        if (!mbar_wait(&full[s], (it / STAGES) & 1, p.status, 13)) {
+                            abort_flag = 1;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint64_t da = umma_desc_sw128(sA + s * TILE_BYTES);
+                        const uint64_t db = umma_desc_sw128(sB + s * TILE_BYTES);
+#pragma unroll
+                        for (int kk = 0; kk < BKB / 32; kk++) {
+                            // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
+                            umma_f8(d_tmem, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), idesc,
+                                    first ? 0u : 1u);
+                            first = false;
+                        }
+                        umma_commit(&empty[s]);
+                    }
+                }
+                umma_commit(&accfull[buf]);
+            }
+            umma_commit(&mma_done);
+            mbar_wait(&mma_done, 0, p.status, 14);
+        }
+    } else {
+        // ---------------- epilogue warps 2..9
+        const int q = warp % 4;          // TMEM lane quarter this warp may access
+        const int h = (warp - 2) / 4;    // column half of the tile
+        const int row = m0 + 32 * q + lane;
+        long long acc[64];
+#pragma unroll
+        for (int c = 0; c < 64; c++) acc[c] = 0;
+        bool ok = true;
+        for (int r = 0; r < p.nrounds; r++) {
+            const int buf = r % NBUF;
+            bool w = true;
+            if (lane == 0) w = mbar_wait(&accfull[buf], (r / NBUF) & 1, p.status, 15);
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (!w || *(volatile int*)&abort_flag) {
+                ok = false;
+                abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const int sh = p.rounds[r].shift;
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                uint32_t v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + buf * BN + h * 64 + half * 32, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    long long x = __float2ll_rn(__uint_as_float(v[c]));
+                    if (sh >= 0) acc[half * 32 + c] += x << sh;
+                    else acc[half * 32 + c] += (x + (1ll << (-sh - 1))) >> (-sh);
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&accempty[buf]);
+        }
+        if (ok && row < p.M) {
+            const int ea = p.ea[row];
+#pragma unroll
+            for (int c = 0; c < 64; c += 2) {
+                const int col = n0 + h * 64 + c;
+                double v0 = 0, v1 = 0;
+                if (col < p.N) v0 = scale_pow2((double)acc[c], p.ubits + ea + p.eb[col]);
+                if (col + 1 < p.N) v1 = scale_pow2((double)acc[c + 1], p.ubits + ea + p.eb[col + 1]);
+                if (!p.cplx) {
+                    double* dst = p.C + (int64_t)row * p.N + col;
+                    if (col + 1 < p.N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+                        *reinterpret_cast<double2*>(dst) = make_double2(v0, v1);
+                    } else {
+                        if (col < p.N) dst[0] = v0;
+                        if (col + 1 < p.N) dst[1] = v1;
+                    }
+                } else {
+                    for (int u = 0; u < 2; u++) {
+                        const int cc = col + u;
+                        if (cc >= p.N) break;
+                        const double v = u ? v1 : v0;
+                        const int jn = cc < p.n_out ? cc : cc - p.n_out;
+                        p.C[2 * ((int64_t)row * p.n_out + jn) + (cc < p.n_out ? 0 : 1)] = v;
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, NBUF * BN);
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+static int make_slice_map(CUtensorMap* map, const void* base, uint64_t Kp, uint64_t rows, uint64_t planes) {
+    f4j_encode_tiled_fn enc = f4j_encode_fn();
+    if (!enc) return f4j_fail(F4J_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3] = {Kp, rows, planes};
+    cuuint64_t strides[2] = {Kp, Kp * rows};
+    cuuint32_t box[3] = {BKB, BM, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<void*>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return f4j_fail(F4J_ERR_CUDA, "cuTensorMapEncodeTiled (slices) failed (%d)", (int)r);
+    return F4J_OK;
+}
+
+// Slice count from the measured exponent spread (bits): keep F >= 48 + spread
+// fixed-point bits so the truncation error stays below the plain FP64 product's.
+static int slices_for_spread(double spread) {
+    const char* env = getenv("F4J_SPLIT_SLICES");
+    if (env && atoi(env) > 0) {
+        int s = atoi(env);
+        return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
+    }
+    double need = 48.0 + (spread > 0 ? spread : 0.0);
+    int s = 1 + (int)ceil((need - 4.0) / 5.0);
+    return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
+}
+
+// Build the round table: rounds of one level whose FP32 sums stay exact.
+static int build_rounds(int s, int64_t Kp, int64_t klen_cat, std::vector<Round>& out, int& ubits) {
+    out.clear();
+    const int64_t nkb = Kp / BKB;
+    // exact budget: pairs * kchunk * 256 <= 2^24
+    int64_t kchunk_blocks = nkb;
+    while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
+    const int64_t kchunk = kchunk_blocks * BKB;
+    int64_t pairs_per_round = (1ll << 24) / (kchunk * 256);
+    if (pairs_per_round < 1) pairs_per_round = 1;
+    // fixed-point unit: finest level weight is 2^-(8 + 5(s-1)); drop D bits so
+    // the worst-case accumulator magnitude stays below 2^62.
+    double kbits = log2((double)(klen_cat > 0 ? klen_cat : 1));
+    int D = (int)ceil(kbits + 8.0 + 5.0 * (s - 1) + 0.2 - 62.0);
+    if (D < 0) D = 0;
+    ubits = -(8 + 5 * (s - 1)) + D;
+    for (int t = 2; t <= s + 1; t++) {
+        const int ilo = t - s > 1 ? t - s : 1, ihi = t - 1 < s ? t - 1 : s;  // inclusive
+        const int shift = 5 * (s + 1 - t) - D;
+        if (shift > 62 || shift < -62) return f4j_fail(F4J_ERR_UNSUPPORTED, "slice weight out of range");
+        for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
+            for (int i = ilo; i <= ihi; i += (int)pairs_per_round) {
+                Round rd;
+                rd.level = (uint8_t)t;
+                rd.i0 = (uint8_t)i;
+                rd.i1 = (uint8_t)((i + pairs_per_round - 1 < ihi ? i + pairs_per_round - 1 : ihi) + 1);
+                rd.shift = (int8_t)shift;
+                rd.kb0 = (int32_t)kb;
+                rd.kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
+                out.push_back(rd);
+            }
+        }
+    }
+    if ((int)out.size() > MAX_ROUNDS) return f4j_fail(F4J_ERR_UNSUPPORTED, "too many split rounds (%d)", (int)out.size());
+    return F4J_OK;
+}
+
+int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                   const double* B, int opB, double* C, int slices_req, f4j_report* rep, bool* nonfinite) {
+    *nonfinite = false;
+    const int64_t M = m, N = cplx ? 2 * n : n;
+    const int64_t Kh = f4j_cdiv(k, BKB) * BKB;  // K of one real part, padded to whole stages
+    const int64_t Kp = cplx ? 2 * Kh : Kh;      // cat K: [re | im], zero padded in between
+    const int64_t klen_cat = cplx ? 2 * k : k;
+    if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "split GEMM too large");
+
+    // ---- small workspace (slot 1): statistics and exponents
+    auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+    const size_t off_mxa = 0, off_esa = off_mxa + al(M * 8), off_cna = off_esa + al(M * 8);
+    const size_t off_mxb = off_cna + al(M * 4), off_esb = off_mxb + al(n * 8), off_cnb = off_esb + al(n * 8);
+    const size_t off_ea = off_cnb + al(n * 4), off_eb = off_ea + al(M * 4);
+    const size_t off_misc = off_eb + al(N * 4);
+    const size_t small_bytes = off_misc + 1024;
+    void* ws1;
+    int rc = f4j_workspace(ctx, 1, small_bytes, &ws1);
+    if (rc) return rc;
+    char* w = (char*)ws1;
+    F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, ctx->stream));
+    F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, ctx->stream));
+    unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
+    long long* esa = (long long*)(w + off_esa);
+    int* cna = (int*)(w + off_cna);
+    unsigned long long* mxb = (unsigned long long*)(w + off_mxb);
+    long long* esb = (long long*)(w + off_esb);
+    int* cnb = (int*)(w + off_cnb);
+    int* ea = (int*)(w + off_ea);
+    int* eb = (int*)(w + off_eb);
+    int* misc = (int*)(w + off_misc);  // [0] non-finite seen, [1] spread A x256, [2] spread B x256
+
+    const bool a_rows = (opA == F4J_OP_N);  // targets of A (rows of op(A)) are stored rows
+    if (a_rows) {
+        k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
+    } else {
+        dim3 g((unsigned)f4j_cdiv(M, 256), (unsigned)f4j_cdiv(k, 256));
+        k_stats_cols<<<g, 256, 0, ctx->stream>>>(A, k, M, cplx, mxa, esa, cna, misc);
+    }
+    F4J_LAUNCHED(ctx);
+    const bool b_rows = (opB != F4J_OP_N);  // targets of B (columns of op(B)) are stored rows
+    if (b_rows) {
+        k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, ctx->stream>>>(B, n, k, cplx, mxb, esb, cnb, misc);
+    } else {
+        dim3 g((unsigned)f4j_cdiv(n, 256), (unsigned)f4j_cdiv(k, 256));
+        k_stats_cols<<<g, 256, 0, ctx->stream>>>(B, k, n, cplx, mxb, esb, cnb, misc);
+    }
+    F4J_LAUNCHED(ctx);
+    k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, ctx->stream>>>(M, 0, mxa, esa, cna, ea, misc + 1);
+    F4J_LAUNCHED(ctx);
+    k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
+                                                                          misc + 2);
+    F4J_LAUNCHED(ctx);
+    int hmisc[3];
+    F4J_CUDA(cudaMemcpyAsync(hmisc, misc, sizeof hmisc, cudaMemcpyDeviceToHost, ctx->stream));
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hmisc[0]) {
+        *nonfinite = true;
+        return F4J_OK;
+    }
+    const double spread = (hmisc[1] > hmisc[2] ? hmisc[1] : hmisc[2]) / 256.0;
+    const int s = slices_req > 0 ? (slices_req > S_MAX ? S_MAX : slices_req) : slices_for_spread(spread);
+
+    std::vector<Round> rounds;
+    int ubits = 0;
+    rc = build_rounds(s, Kp, klen_cat, rounds, ubits);
+    if (rc) return rc;
+
+    // ---- bulk workspace (slot 0): slice planes
+    const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
+    void* ws0;
+    rc = f4j_workspace(ctx, 0, al(plane_a * s) + al(plane_b * s), &ws0);
+    if (rc) return rc;
+    uint8_t* slA = (uint8_t*)ws0;
+    uint8_t* slB = slA + al(plane_a * s);
+
+    {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
+        dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
+        k_split<<<g, 256, 0, ctx->stream>>>(A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, cplx,
+                                            opA == F4J_OP_C, 0, M, k, Kh, Kp, M, ea, s, slA);
+        F4J_LAUNCHED(ctx);
+    }
+    {   // B: targets = columns of op(B); stored k x n (N, transposed read) or n x k (T/C)
+        dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(n, SP_TR));
+        k_split<<<g, 256, 0, ctx->stream>>>(B, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, cplx,
+                                            opB == F4J_OP_C, 1, n, k, Kh, Kp, N, eb, s, slB);
+        F4J_LAUNCHED(ctx);
+    }
+
+    CUtensorMap ta{}, tb{};
+    rc = make_slice_map(&ta, slA, Kp, M, s);
+    if (rc) return rc;
+    rc = make_slice_map(&tb, slB, Kp, N, s);
+    if (rc) return rc;
+
+    SplitGemmParams* prm = new SplitGemmParams();
+    prm->M = (int)M;
+    prm->N = (int)N;
+    prm->Kp = (int)Kp;
+    prm->nrounds = (int)rounds.size();
+    prm->cplx = cplx ? 1 : 0;
+    prm->n_out = (int)n;
+    prm->ubits = ubits;
+    prm->ea = ea;
+    prm->eb = eb;
+    prm->C = C;
+    prm->status = ctx->d_status + F4J_ST_TIMEOUT;
+    for (size_t i = 0; i < rounds.size(); i++) prm->rounds[i] = rounds[i];
+
+    const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
+    cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+        delete prm;
+        return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
+    }
+    dim3 grid((unsigned)f4j_cdiv(N, BN), (unsigned)f4j_cdiv(M, BM));
+    k_split_gemm<<<grid, GEMM_THREADS, smem, ctx->stream>>>(ta, tb, *prm);
+    delete prm;
+    F4J_LAUNCHED(ctx);
+
+    if (rep) {
+        rep->slices = s;
+        rep->frac_bits = 4 + 5 * (s - 1);
+        rep->exp_spread = spread;
+    }
+    return F4J_OK;
+}

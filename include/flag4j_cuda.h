@@ -1,0 +1,193 @@
+/*
+ * flag4j_cuda.h -- C ABI of libflag4j_cuda.so, the GB300 (sm_103a) engine for
+ * Flag4j's product path: dense real / complex GEMM and CSR x dense products.
+ *
+ * Flag4j has no native layer; the seam this library replaces is the Java
+ * method + dispatcher pair for each product.  Each entry point below names the
+ * reference interface it stands in for (paths within the Flag4j project).
+ *
+ * Conventions
+ *  - Every function returns an int status: F4J_OK (0) or a negative F4J_ERR_*.
+ *    f4j_last_error() gives a thread-local message for the last failure on the
+ *    calling thread.  Shape errors carry Flag4j's own wording
+ *    ("Cannot multiply matrices/vector with shapes (m, k) and (k2, n).").
+ *  - Matrices are row-major float64; complex matrices are interleaved
+ *    (re, im) float64 pairs, i.e. Flag4j's Complex128[] marshalled to double[2n].
+ *  - Operands live in device buffers (f4j_buf) so forward operands can be kept
+ *    on the GPU across calls.  Inputs are never modified; outputs are written.
+ *  - All work of a context runs in order on that context's CUDA stream; calls
+ *    return once the work is queued (use f4j_sync or a download to wait).
+ *    Separate contexts are independent.  A context must not be used from two
+ *    threads at once.
+ *  - No CPU fallback: every product runs as CUDA kernels on the context's GPU.
+ */
+#ifndef FLAG4J_CUDA_H
+#define FLAG4J_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define F4J_OK 0
+#define F4J_ERR_ARG (-1)         /* bad argument -> IllegalArgumentException          */
+#define F4J_ERR_SHAPE (-2)       /* shape mismatch -> LinearAlgebraException           */
+#define F4J_ERR_CSR (-3)         /* invalid CSR/COO -> IllegalArgumentException        */
+#define F4J_ERR_OOM (-4)         /* device allocation failed                           */
+#define F4J_ERR_CUDA (-5)        /* CUDA runtime / launch error -> Flag4jDeviceException */
+#define F4J_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                 */
+#define F4J_ERR_UNSUPPORTED (-7) /* configuration not supported on this device        */
+
+/* ---- operand transforms and GEMM modes ---------------------------------- */
+#define F4J_OP_N 0 /* op(X) = X                        */
+#define F4J_OP_T 1 /* op(X) = X^T                      */
+#define F4J_OP_C 2 /* op(X) = X^H (complex only; = T for real) */
+
+#define F4J_MODE_PLAIN 0 /* FP64 DMMA tensor-core GEMM (mma.sync f64)                   */
+#define F4J_MODE_SPLIT 1 /* FP64-accurate split GEMM: FP8 slices on tcgen05, exact FP32 */
+#define F4J_MODE_AUTO 2  /* SPLIT for finite inputs, PLAIN when a NaN/Inf is present    */
+#define F4J_MODE_EXACT 3 /* Flag4j's own order: k-ascending, no FMA -> bit-identical     */
+
+typedef struct f4j_ctx f4j_ctx;
+typedef struct f4j_buf_s* f4j_buf;
+typedef struct f4j_csr_s* f4j_csr;
+
+/* Optional per-call report (pass NULL to skip). */
+typedef struct f4j_report {
+    int32_t mode_used;   /* F4J_MODE_* that actually ran                          */
+    int32_t slices;      /* SPLIT: slice count s per operand                      */
+    int32_t launches;    /* kernels this call launched                            */
+    int32_t frac_bits;   /* SPLIT: fixed-point bits kept per element (4 + 5(s-1)) */
+    double flops;        /* algorithmic flops: 2mnk real, 8mnk complex, 2*nnz*cols */
+    double bytes;        /* algorithmic (compulsory) bytes of sparse products     */
+    double exp_spread;   /* SPLIT: measured exponent spread of the operands (bits) */
+} f4j_report;
+
+/* ---- library / context --------------------------------------------------- */
+int f4j_version(void); /* 10000*major + 100*minor + patch */
+const char* f4j_last_error(void);
+int f4j_create(int device, f4j_ctx** out);
+int f4j_destroy(f4j_ctx* ctx);
+int f4j_sync(f4j_ctx* ctx);
+/* Run this context's work on an existing cudaStream_t (NULL = own stream). */
+int f4j_set_stream(f4j_ctx* ctx, void* cuda_stream);
+void* f4j_get_stream(f4j_ctx* ctx);
+/* Kernels launched by this context so far. */
+int64_t f4j_launch_count(f4j_ctx* ctx);
+/* CUDA-event timing on the context stream: record into slot (0..15), then
+ * read the elapsed ms between two recorded slots (synchronises the end slot). */
+int f4j_timer_record(f4j_ctx* ctx, int slot);
+int f4j_timer_elapsed(f4j_ctx* ctx, int slot_begin, int slot_end, float* ms);
+
+/* ---- device buffers ------------------------------------------------------ */
+int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out);
+int f4j_buf_free(f4j_ctx* ctx, f4j_buf buf);
+size_t f4j_buf_size(f4j_buf buf);
+void* f4j_buf_device_ptr(f4j_buf buf);
+/* Copies are stream-ordered.  Synchronous variants wait for completion;
+ * async variants return at once (host memory must stay valid, and should be
+ * pinned, until the stream reaches the copy). */
+int f4j_buf_upload(f4j_ctx* ctx, f4j_buf buf, const void* host, size_t bytes, size_t offset);
+int f4j_buf_download(f4j_ctx* ctx, f4j_buf buf, void* host, size_t bytes, size_t offset);
+int f4j_buf_upload_async(f4j_ctx* ctx, f4j_buf buf, const void* host, size_t bytes, size_t offset);
+int f4j_buf_download_async(f4j_ctx* ctx, f4j_buf buf, void* host, size_t bytes, size_t offset);
+int f4j_buf_zero(f4j_ctx* ctx, f4j_buf buf);
+/* Pin / unpin caller-owned host memory (e.g. a Java MemorySegment). */
+int f4j_host_register(void* host, size_t bytes);
+int f4j_host_unregister(void* host);
+
+/* ---- dense products ------------------------------------------------------ */
+/* C(m x n) = op(A) * op(B), op(A) m x k, op(B) k x n, real float64.
+ * Replaces Matrix.mult -> ReDeMatMultDispatcher.dispatch
+ *   (src/main/java/org/flag4j/arrays/dense/Matrix.java:638-640,
+ *    src/main/java/org/flag4j/linalg/ops/dispatch/ReDeMatMultDispatcher.java:157-237)
+ * and, with opB = F4J_OP_T, Matrix.multTranspose
+ *   (Matrix.java:655-663, RealDenseMatrixMultiplyDispatcher.java:148-154).
+ * A is stored m x k (opA N) or k x m (opA T); B k x n (N) or n x k (T). */
+int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA, f4j_buf B,
+              int opB, f4j_buf C, int mode, f4j_report* report);
+
+/* Complex128 C = op(A) * op(B), interleaved (re, im); op may be N, T or C.
+ * Replaces CMatrix.mult -> Cm128DeMatMultDispatcher.dispatch
+ *   (src/main/java/org/flag4j/arrays/dense/CMatrix.java:463-465,
+ *    src/main/java/org/flag4j/linalg/ops/dispatch/Cm128DeMatMultDispatcher.java:155-226). */
+int f4j_zgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA, f4j_buf B,
+              int opB, f4j_buf C, int mode, f4j_report* report);
+
+/* Reverse-mode adjoint of C = A * B (A m x k, B k x n, both op N):
+ *   dA = dC * B^T (m x k),  dB = A^T * dC (k x n)   (real)
+ *   dA = dC * B^H,          dB = A^H * dC           (complex: f4j_zgemm_adjoint)
+ * run on the same GEMM kernels with transposed operand descriptors (no
+ * transpose is materialised).  Either output may be NULL to skip it.
+ * No Flag4j counterpart (Flag4j has no autodiff); its CPU oracle is
+ * W.multTranspose(B) and A.T().mult(W). */
+int f4j_dgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, f4j_buf B,
+                      f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode, f4j_report* report);
+int f4j_zgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, f4j_buf B,
+                      f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode, f4j_report* report);
+
+/* Sampled accuracy check of a computed C = op(A) op(B): evaluates `samples`
+ * seeded entries in double-double (compensated Dot2) on the GPU and returns
+ * max |C - C_true| and max |C - C_true| / sum|a||b| over the samples. */
+int f4j_gemm_check(f4j_ctx* ctx, int cplx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
+                   f4j_buf B, int opB, f4j_buf C, int64_t samples, uint64_t seed,
+                   double* max_abs_err, double* max_rel_err);
+
+/* ---- CSR matrices ---------------------------------------------------------- */
+/* Wrap device arrays as a CSR matrix (rowptr int32[rows+1], colidx int32[nnz],
+ * vals float64[nnz]); the handle borrows the buffers.  validate != 0 runs
+ * SparseValidation.validateCsr's checks on the GPU
+ *   (src/main/java/org/flag4j/arrays/sparse/SparseValidation.java:151-206;
+ *    constructor CsrMatrix.java:175-185). */
+int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowptr,
+                 f4j_buf colidx, f4j_buf vals, int validate, f4j_csr* out);
+/* Build CSR from COO triplets exactly as CooMatrix.toCsr does
+ *   (src/main/java/org/flag4j/arrays/sparse/CooMatrix.java:457-470):
+ * rowptr = inclusive scan of per-row counts; colidx and vals are copied
+ * unchanged (so the COO must already be row-sorted).  The new handle owns
+ * its three buffers. */
+int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowidx,
+                     f4j_buf colidx, f4j_buf vals, f4j_csr* out);
+/* Stable lexicographic (row, col) sort of COO triplets in place, as
+ * CooMatrix.sortIndices -> CooDataSorter.sparseSort
+ *   (CooMatrix.java:476-479, src/main/java/org/flag4j/linalg/ops/sparse/coo/
+ *    CooDataSorter.java:176-259). vals may be NULL. */
+int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals);
+int f4j_csr_free(f4j_ctx* ctx, f4j_csr csr);
+int f4j_csr_info(f4j_csr csr, int64_t* rows, int64_t* cols, int64_t* nnz);
+int f4j_csr_buffers(f4j_csr csr, f4j_buf* rowptr, f4j_buf* colidx, f4j_buf* vals);
+/* Materialised transpose, CsrMatrix.T() -> RealCsrOps.transpose
+ *   (CsrMatrix.java:1431-1433, src/main/java/org/flag4j/linalg/ops/sparse/csr/real/
+ *    RealCsrOps.java:195-225); bit-identical structure and order. */
+int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out);
+/* Copy out the cached transpose permutation (int32[nnz]: for each position of
+ * S^T in RealCsrOps.transpose order, the source nnz index of S). */
+int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out);
+
+/* y = S x.  Replaces CsrMatrix.mult(Vector) -> RealCsrDenseMatMult.standardVector
+ *   (CsrMatrix.java:1170-1171, src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/
+ *    real/RealCsrDenseMatMult.java:172-192).  Bit-identical: each y[i] is summed in
+ * storage order with separately rounded products, like the reference. */
+int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* report);
+/* Y(rows x ncols) = S X, X cols x ncols row-major.  Replaces CsrMatrix.mult(Matrix)
+ * -> RealCsrDenseMatMult.standard (CsrMatrix.java:1498-1499,
+ * RealCsrDenseMatMult.java:55-82).  Bit-identical. */
+int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* report);
+/* dX(cols x ncols) = S^T dC without forming S^T: gathers through a cached
+ * transpose permutation (built on first use); atomic-free.  Bit-identical to
+ * S.T().mult(dC) in the reference. */
+int f4j_spmm_t(f4j_ctx* ctx, f4j_csr S, f4j_buf dC, int64_t ncols, f4j_buf dX,
+               f4j_report* report);
+/* SDDMM on S's pattern: out[q] = dot(A[row(q), :], B[col(q), :]) over ncols
+ * (A rows x ncols, B cols x ncols) -- the gradient dS = (dC X^T) restricted to
+ * pattern(S) for C = S X.  No Flag4j counterpart. */
+int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t ncols, f4j_buf out,
+              f4j_report* report);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLAG4J_CUDA_H */

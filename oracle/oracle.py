@@ -1,0 +1,201 @@
+"""ctypes front end for the CPU oracle (f4j_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, the smoke check and the benchmark's
+CPU-baseline leg as the checker.  The product library never imports this.
+
+``build()`` compiles f4j_oracle.c with gcc -O2 -ffp-contract=off so every
+product and sum rounds separately, as the JVM does.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "f4j_oracle.c")
+LIB = os.path.join(HERE, "libf4j_oracle.so")
+CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread", "-std=c11"]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle shared library (a second or two)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB)
+            i64, i32, p = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p
+            sig = {
+                "orc_dgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_dgemm_abt": [i64, i64, i64, p, p, p, i32],
+                "orc_dgemv_blocked": [i64, i64, p, p, p, i64],
+                "orc_zgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_spmv": [i64, p, p, p, p, p, i32],
+                "orc_spmm": [i64, i64, p, p, p, p, p, i32],
+                "orc_coo_to_csr": [i64, i64, p, p],
+                "orc_coo_sort": [i64, p, p, p, p],
+                "orc_csr_transpose": [i64, i64, p, p, p, p, p, p, p],
+                "orc_sddmm": [i64, i64, p, p, p, p, p],
+                "orc_truth_sampled": [i64, p, i64, i32, p, i64, i32, i32, i64, p, p, p, p, p],
+                "orc_absgemm": [i64, i64, i64, p, p, p, i32],
+            }
+            for name, args in sig.items():
+                f = getattr(L, name)
+                f.argtypes = args
+                f.restype = None
+            _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def threads_default():
+    return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------- dense
+def dgemm(A, B, threads=1):
+    """RealDenseMatMult.reordered order (bit-identical to the Java kernels)."""
+    A, B = _f64(A), _f64(B)
+    m, k = A.shape
+    k2, n = B.shape
+    assert k == k2
+    C = np.empty((m, n), np.float64)
+    lib().orc_dgemm(m, n, k, _p(A), _p(B), _p(C), threads)
+    return C
+
+
+def dgemm_abt(A, Bt, threads=1):
+    """RealDenseMatMultTranspose: A @ Bt.T with Bt given n x k."""
+    A, Bt = _f64(A), _f64(Bt)
+    m, k = A.shape
+    n, k2 = Bt.shape
+    assert k == k2
+    C = np.empty((m, n), np.float64)
+    lib().orc_dgemm_abt(m, n, k, _p(A), _p(Bt), _p(C), threads)
+    return C
+
+
+def dgemv_blocked(A, x, block=64):
+    A, x = _f64(A), _f64(x)
+    m, k = A.shape
+    y = np.empty(m, np.float64)
+    lib().orc_dgemv_blocked(m, k, _p(A), _p(x), _p(y), block)
+    return y
+
+
+def zgemm(A, B, threads=1):
+    """DenseSemiringMatMult over Complex128 (complex128 numpy arrays)."""
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    B = np.ascontiguousarray(B, dtype=np.complex128)
+    m, k = A.shape
+    k2, n = B.shape
+    assert k == k2
+    C = np.empty((m, n), np.complex128)
+    lib().orc_zgemm(m, n, k, _p(A), _p(B), _p(C), threads)
+    return C
+
+
+def absgemm(A, B, threads=1):
+    A, B = _f64(A), _f64(B)
+    m, k = A.shape
+    n = B.shape[1]
+    C = np.empty((m, n), np.float64)
+    lib().orc_absgemm(m, n, k, _p(A), _p(B), _p(C), threads)
+    return C
+
+
+def truth_sampled(A, B, si, sj, opA=0, opB=0):
+    """Compensated (Dot2) values of op(A) @ op(B) at (si, sj).
+
+    Returns (hi, lo, absref); complex inputs return complex hi/lo and a complex
+    absref whose real/imag parts bound the real/imag components.
+    """
+    cplx = np.iscomplexobj(A) or np.iscomplexobj(B)
+    dt = np.complex128 if cplx else np.float64
+    A = np.ascontiguousarray(A, dtype=dt)
+    B = np.ascontiguousarray(B, dtype=dt)
+    k = A.shape[1] if opA == 0 else A.shape[0]
+    si = np.ascontiguousarray(si, dtype=np.int64)
+    sj = np.ascontiguousarray(sj, dtype=np.int64)
+    ns = len(si)
+    hi = np.empty(ns, dt)
+    lo = np.empty(ns, dt)
+    ab = np.empty(ns, dt)
+    lib().orc_truth_sampled(k, _p(A), A.shape[1], opA, _p(B), B.shape[1], opB, int(cplx), ns,
+                            _p(si), _p(sj), _p(hi), _p(lo), _p(ab))
+    return hi, lo, ab
+
+
+# ------------------------------------------------------------- sparse
+def spmv(rowptr, colidx, vals, x, threads=1):
+    rowptr, colidx, vals, x = _i32(rowptr), _i32(colidx), _f64(vals), _f64(x)
+    rows = len(rowptr) - 1
+    y = np.empty(rows, np.float64)
+    lib().orc_spmv(rows, _p(rowptr), _p(colidx), _p(vals), _p(x), _p(y), threads)
+    return y
+
+
+def spmm(rowptr, colidx, vals, X, threads=1):
+    rowptr, colidx, vals, X = _i32(rowptr), _i32(colidx), _f64(vals), _f64(X)
+    rows = len(rowptr) - 1
+    nc = X.shape[1]
+    Y = np.empty((rows, nc), np.float64)
+    lib().orc_spmm(rows, nc, _p(rowptr), _p(colidx), _p(vals), _p(X), _p(Y), threads)
+    return Y
+
+
+def coo_to_csr(rows, rowidx):
+    rowidx = _i32(rowidx)
+    rowptr = np.empty(rows + 1, np.int32)
+    lib().orc_coo_to_csr(rows, len(rowidx), _p(rowidx), _p(rowptr))
+    return rowptr
+
+
+def coo_sort(rowidx, colidx, vals):
+    r, c, v = _i32(rowidx).copy(), _i32(colidx).copy(), _f64(vals).copy()
+    perm = np.empty(len(r), np.int64)
+    lib().orc_coo_sort(len(r), _p(r), _p(c), _p(v), _p(perm))
+    return r, c, v, perm
+
+
+def csr_transpose(rows, cols, rowptr, colidx, vals):
+    rowptr, colidx, vals = _i32(rowptr), _i32(colidx), _f64(vals)
+    nnz = int(rowptr[-1])
+    trp = np.empty(cols + 1, np.int32)
+    tci = np.empty(nnz, np.int32)
+    tv = np.empty(nnz, np.float64)
+    perm = np.empty(nnz, np.int32)
+    lib().orc_csr_transpose(rows, cols, _p(rowptr), _p(colidx), _p(vals), _p(trp), _p(tci),
+                            _p(tv), _p(perm))
+    return trp, tci, tv, perm
+
+
+def sddmm(rowptr, colidx, dC, X):
+    rowptr, colidx, dC, X = _i32(rowptr), _i32(colidx), _f64(dC), _f64(X)
+    out = np.empty(int(rowptr[-1]), np.float64)
+    lib().orc_sddmm(len(rowptr) - 1, dC.shape[1], _p(rowptr), _p(colidx), _p(dC), _p(X), _p(out))
+    return out

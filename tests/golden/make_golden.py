@@ -1,0 +1,190 @@
+"""Extract Flag4j's known-answer test vectors into JSON fixtures.
+
+Reads the reference's own JUnit sources as text (nothing is executed) and
+writes ``reference_golden.json`` next to this script.  Each case records the
+Java file, the test method, the line of the assertion that closes it, the
+inputs and (where the test states them as literals) the expected output.
+
+Files read (paths within the Flag4j project):
+  src/test/java/org/flag4j/linalg/ops/dense/real/MatrixMultiplyTests.java
+  src/test/java/org/flag4j/linalg/ops/dense/complex/CMatrixMultiplyTests.java
+  src/test/java/org/flag4j/arrays/dense/matrix/MatrixMultTests.java
+  src/test/java/org/flag4j/arrays/dense/complex_matrix/CMatrixMultTests.java
+  src/test/java/org/flag4j/arrays/dense/matrix/MatrixVectorTests.java
+  src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java
+  src/test/java/org/flag4j/arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java
+
+Usage:  python tests/golden/make_golden.py [/path/to/flag4j]
+The fixture is committed; the GPU machine never needs the reference tree.
+"""
+import json
+import math
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+T = "src/test/java/org/flag4j/"
+FILES = {
+    "real_kernels": T + "linalg/ops/dense/real/MatrixMultiplyTests.java",
+    "complex_kernels": T + "linalg/ops/dense/complex/CMatrixMultiplyTests.java",
+    "matrix_mult": T + "arrays/dense/matrix/MatrixMultTests.java",
+    "cmatrix_mult": T + "arrays/dense/complex_matrix/CMatrixMultTests.java",
+    "matrix_vector": T + "arrays/dense/matrix/MatrixVectorTests.java",
+    "csr_dense": T + "arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java",
+    "csr_transpose": T + "arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java",
+}
+
+# ---------------------------------------------------------------- parsing
+NUM = r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?[dDfF]?"
+
+
+def parse_complex_string(s):
+    """Complex128(String) literal: 'a+bi', 'a - bi', 'bi', 'a'."""
+    t = s.replace(" ", "")
+    if not t.endswith("i"):
+        return [float(t.rstrip("dD")), 0.0]
+    body = t[:-1]
+    # split at the last sign that is not part of an exponent and not leading
+    cut = None
+    for p in range(len(body) - 1, 0, -1):
+        if body[p] in "+-" and body[p - 1] not in "eE":
+            cut = p
+            break
+    if cut is None:  # pure imaginary
+        return [0.0, float(body) if body not in ("", "+", "-") else float(body + "1")]
+    re_part, im_part = body[:cut], body[cut:]
+    if im_part in ("+", "-"):
+        im_part += "1"
+    return [float(re_part), float(im_part)]
+
+
+class Lit:
+    """Tiny evaluator for the array / Complex128 literals used in the tests."""
+
+    def __init__(self, text):
+        self.s = text
+        self.p = 0
+
+    def ws(self):
+        while self.p < len(self.s) and self.s[self.p] in " \t\r\n":
+            self.p += 1
+
+    def peek(self, tok):
+        self.ws()
+        return self.s.startswith(tok, self.p)
+
+    def eat(self, tok):
+        self.ws()
+        if not self.s.startswith(tok, self.p):
+            raise ValueError("expected %r at %r" % (tok, self.s[self.p:self.p + 40]))
+        self.p += len(tok)
+
+    def value(self):
+        self.ws()
+        if self.peek("new double[]") or self.peek("new double[][]") or self.peek("new Complex128[]") \
+                or self.peek("new Complex128[][]") or self.peek("new int[]"):
+            self.p = self.s.index("{", self.p)
+            return self.array()
+        if self.peek("{"):
+            return self.array()
+        if self.peek("new Complex128("):
+            self.eat("new Complex128(")
+            if self.peek('"'):
+                self.eat('"')
+                end = self.s.index('"', self.p)
+                v = parse_complex_string(self.s[self.p:end])
+                self.p = end + 1
+                self.eat(")")
+                return v
+            a = self.scalar()
+            b = 0.0
+            if self.peek(","):
+                self.eat(",")
+                b = self.scalar()
+            self.eat(")")
+            return [a, b]
+        if self.peek("Complex128.ZERO"):
+            self.eat("Complex128.ZERO")
+            return [0.0, 0.0]
+        return self.scalar()
+
+    def scalar(self):
+        self.ws()
+        if self.peek("-Math.PI"):
+            self.eat("-Math.PI")
+            return -math.pi
+        if self.peek("Math.PI"):
+            self.eat("Math.PI")
+            return math.pi
+        m = re.compile(NUM).match(self.s, self.p)
+        if not m:
+            raise ValueError("bad scalar at %r" % self.s[self.p:self.p + 40])
+        self.p = m.end()
+        return float(m.group(0).rstrip("dDfF"))
+
+    def array(self):
+        self.eat("{")
+        out = []
+        while True:
+            self.ws()
+            if self.peek("}"):
+                self.eat("}")
+                return out
+            out.append(self.value())
+            self.ws()
+            if self.peek(","):
+                self.eat(",")
+
+
+def split_methods(src):
+    """Yield (name, body, body_start_line) for each @Test method."""
+    for m in re.finditer(r"@Test\s+void\s+(\w+)\s*\(\s*\)\s*\{", src):
+        depth, p = 1, m.end()
+        while depth:
+            c = src[p]
+            depth += (c == "{") - (c == "}")
+            p += 1
+        yield m.group(1), src[m.end():p - 1], src[:m.end()].count("\n") + 1
+
+
+ASSIGN = re.compile(r"^\s*(\w+)\s*=\s*(new\s+(?:double|Complex128)\[\]|\{|new double\[\]\[\]|"
+                    r"new Complex128\[\]\[\])", re.S)
+
+
+def cases_of(path, rel):
+    src = open(path).read()
+    out = []
+    for name, body, line0 in split_methods(src):
+        env = {}
+        pos = 0
+        for stmt in body.split(";"):
+            line = line0 + body[:pos].count("\n")
+            pos += len(stmt) + 1
+            s = stmt.strip()
+            if not s:
+                continue
+            s = re.sub(r"//[^\n]*", "", s).strip()
+            m = ASSIGN.match(s)
+            if m:
+                env[m.group(1)] = Lit(s[s.index("=") + 1:]).value()
+                continue
+            call = re.match(r"(assert\w+|build|makeMatrices)\s*\((.*)\)\s*$", s, re.S)
+            if call:
+                out.append({"file": rel, "method": name, "line": line + s.count("\n"),
+                            "call": call.group(1), "args": call.group(2).strip(),
+                            "vars": json.loads(json.dumps(env))})
+    return out
+
+
+def main(root):
+    golden = {}
+    for key, rel in FILES.items():
+        golden[key] = cases_of(os.path.join(root, rel), rel)
+    with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
+        json.dump(golden, f, indent=1)
+    print({k: len(v) for k, v in golden.items()})
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

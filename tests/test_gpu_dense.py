@@ -1,0 +1,310 @@
+"""Dense GEMM parity on the GPU through the C ABI (via the Flag4j-mirror API).
+
+Bars: EXACT mode is bit-identical to Flag4j's loops; PLAIN (FP64 DMMA) and
+SPLIT (FP8 slices on tcgen05) satisfy |C - C_ref| <= 2 k u |A||B|
+(u = 2^-53, k = inner dimension), componentwise.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import U, assert_within_bound
+
+pytestmark = pytest.mark.gpu
+
+
+def cplx(a):
+    a = np.asarray(a, dtype=np.float64)
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def opx(X, op):
+    return X if op == 0 else (X.T if op == 1 else X.conj().T)
+
+
+def run_gemm(f4j, A, B, opA=0, opB=0, mode="plain"):
+    """C = op(A) op(B) through f4j_dgemm / f4j_zgemm with stored A, B."""
+    from flag4j_gb300 import _lib
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    cp = np.iscomplexobj(A) or np.iscomplexobj(B)
+    dt = np.complex128 if cp else np.float64
+    A = np.ascontiguousarray(A, dt)
+    B = np.ascontiguousarray(B, dt)
+    m = A.shape[0] if opA == 0 else A.shape[1]
+    k = A.shape[1] if opA == 0 else A.shape[0]
+    n = B.shape[1] if opB == 0 else B.shape[0]
+    dA, dB = ctx.from_numpy(A if A.size else np.zeros(1, dt)), ctx.from_numpy(B if B.size else np.zeros(1, dt))
+    dC = ctx.alloc(max(m * n * (16 if cp else 8), 8))
+    rep = _lib.f4j_report()
+    fn = ctx.lib.f4j_zgemm if cp else ctx.lib.f4j_dgemm
+    check(fn(ctx.handle, m, n, k, dA.handle, opA, dB.handle, opB, dC.handle, _lib.MODES[mode], ctypes.byref(rep)))
+    C = dC.to_numpy(dt, m * n).reshape(m, n)
+    ctx.sync()
+    return C, rep
+
+
+def ref_bound(oracle, A, B, cp):
+    if not cp:
+        return oracle.dgemm(A, B), oracle.absgemm(A, B)
+    ref = oracle.zgemm(A, B)
+    ab = np.abs(A.real) @ np.abs(B.real) + np.abs(A.imag) @ np.abs(B.imag)
+    ab2 = np.abs(A.real) @ np.abs(B.imag) + np.abs(A.imag) @ np.abs(B.real)
+    return ref, ab + 1j * ab2
+
+
+def check_bound(C, ref, ab, k, what):
+    if np.iscomplexobj(C):
+        assert_within_bound(C.real, ref.real, ab.real, k, what + " (re)")
+        assert_within_bound(C.imag, ref.imag, ab.imag, k, what + " (im)")
+    else:
+        assert_within_bound(C, ref, ab, k, what)
+
+
+# ------------------------------------------------------------------ golden
+def test_exact_mode_reproduces_golden_vectors(f4j, golden):
+    # MatrixMultiplyTests.java / CMatrixMultiplyTests.java known answers, bit for bit
+    for c in golden["real_kernels"]:
+        v = c["vars"]
+        C = f4j.Matrix(v["entriesA"]).mult(f4j.Matrix(v["entriesB"]), mode="exact")
+        assert np.array_equal(C.data, np.array(v["exp"])), c["line"]
+    for c in golden["complex_kernels"]:
+        v = c["vars"]
+        C = f4j.CMatrix(cplx(v["entriesA"])).mult(f4j.CMatrix(cplx(v["entriesB"])), mode="exact")
+        assert np.array_equal(C.data, cplx(v["exp"]).ravel()), c["line"]
+
+
+@pytest.mark.parametrize("mode", ["plain", "split", "auto"])
+def test_fast_modes_on_golden_vectors(f4j, golden, oracle, mode):
+    for c in golden["real_kernels"]:
+        A, B = np.array(c["vars"]["entriesA"]), np.array(c["vars"]["entriesB"])
+        C = f4j.Matrix(A).mult(f4j.Matrix(B), mode=mode).toNumpy()
+        check_bound(C, *ref_bound(oracle, A, B, False), A.shape[1], "%s line %d" % (mode, c["line"]))
+    for c in golden["complex_kernels"]:
+        A, B = cplx(c["vars"]["entriesA"]), cplx(c["vars"]["entriesB"])
+        C = f4j.CMatrix(A).mult(f4j.CMatrix(B), mode=mode).toNumpy()
+        check_bound(C, *ref_bound(oracle, A, B, True), A.shape[1], "%s line %d" % (mode, c["line"]))
+
+
+def test_api_golden_and_shape_errors(f4j, golden):
+    c = [c for c in golden["matrix_mult"] if c["method"] == "matMultTestCase"]
+    v = c[0]["vars"]
+    A, B = f4j.Matrix(v["aEntries"]), f4j.Matrix(v["bEntries"])
+    assert A.mult(B, mode="exact") == f4j.Matrix(v["expEntries"])
+    v2 = c[1]["vars"]  # MatrixMultTests.java:61: mismatched shapes
+    with pytest.raises(f4j.LinearAlgebraException, match=r"Cannot multiply matrices/vector with shapes \(4, 3\) and \(4, 2\)"):
+        f4j.Matrix(v2["aEntries"]).mult(f4j.Matrix(v2["bEntries"]))
+    mv = [c for c in golden["matrix_vector"] if c["method"] == "matVecMultTestCase"]
+    A = f4j.Matrix(mv[0]["vars"]["aEntries"])
+    y = A.mult(f4j.Vector(mv[0]["vars"]["bEntries"]), mode="exact")
+    assert y == f4j.Vector(mv[0]["vars"]["expEntries"])
+    with pytest.raises(f4j.LinearAlgebraException):
+        A.mult(f4j.Vector(mv[1]["vars"]["bEntries"]))
+    mt = [c for c in golden["matrix_mult"] if c["method"] == "multTransposeTestCase"]
+    A, Bs = f4j.Matrix(mt[0]["vars"]["aEntries"]), np.array(mt[0]["vars"]["bEntries"])
+    B = f4j.Matrix(Bs.T.copy())
+    assert A.multTranspose(B, mode="exact") == A.mult(f4j.Matrix(Bs), mode="exact")
+    with pytest.raises(f4j.IllegalArgumentException):
+        A.multTranspose(f4j.Matrix(np.array(mt[1]["vars"]["bEntries"]).T.copy()))
+
+
+# ------------------------------------------------------------------ random sizes
+SIZES = [(1, 1, 1), (3, 5, 7), (17, 33, 65), (64, 64, 64), (130, 70, 257), (257, 129, 95), (200, 300, 1000)]
+
+
+@pytest.mark.parametrize("m,n,k", SIZES)
+@pytest.mark.parametrize("cp", [False, True])
+def test_exact_mode_bit_identical(f4j, oracle, m, n, k, cp):
+    from flag4j_gb300 import synth
+    A = synth.uniform(m, k, m + 1)
+    B = synth.uniform(k, n, n + 2)
+    if cp:
+        A = A + 1j * synth.uniform(m, k, 5)
+        B = B + 1j * synth.uniform(k, n, 6)
+    C, rep = run_gemm(f4j, A, B, mode="exact")
+    ref = oracle.zgemm(A, B) if cp else oracle.dgemm(A, B)
+    assert np.array_equal(C, ref)
+
+
+@pytest.mark.parametrize("mode", ["plain", "split"])
+@pytest.mark.parametrize("m,n,k", SIZES)
+@pytest.mark.parametrize("cp", [False, True])
+def test_fast_modes_within_bound(f4j, oracle, mode, m, n, k, cp):
+    from flag4j_gb300 import synth
+    A = synth.normal(m, k, 11)
+    B = synth.normal(k, n, 12)
+    if cp:
+        A = A + 1j * synth.normal(m, k, 13)
+        B = B + 1j * synth.normal(k, n, 14)
+    C, rep = run_gemm(f4j, A, B, mode=mode)
+    check_bound(C, *ref_bound(oracle, A, B, cp), k, mode)
+    if mode == "split":
+        assert rep.mode_used == 1 and 2 <= rep.slices <= 14
+
+
+@pytest.mark.parametrize("mode", ["exact", "plain", "split"])
+@pytest.mark.parametrize("opA,opB", [(0, 1), (1, 0), (1, 1), (2, 0), (0, 2), (2, 2)])
+def test_transposed_operands(f4j, oracle, mode, opA, opB):
+    from flag4j_gb300 import synth
+    m, n, k = 70, 45, 133
+    for cp in (False, True):
+        if not cp and (opA == 2 or opB == 2):
+            continue
+        As = synth.uniform(m, k, 1) if opA == 0 else synth.uniform(k, m, 1)
+        Bs = synth.uniform(k, n, 2) if opB == 0 else synth.uniform(n, k, 2)
+        if cp:
+            As = As + 1j * synth.uniform(*As.shape, 3)
+            Bs = Bs + 1j * synth.uniform(*Bs.shape, 4)
+        C, _ = run_gemm(f4j, As, Bs, opA, opB, mode)
+        A, B = np.ascontiguousarray(opx(As, opA)), np.ascontiguousarray(opx(Bs, opB))
+        ref, ab = ref_bound(oracle, A, B, cp)
+        if mode == "exact":
+            assert np.array_equal(C, ref)
+        else:
+            check_bound(C, ref, ab, k, "%s op(%d,%d)" % (mode, opA, opB))
+
+
+@pytest.mark.parametrize("mode", ["plain", "split", "exact"])
+def test_odd_leading_dimensions_and_empty(f4j, oracle, mode):
+    # odd real leading dimensions take the DMMA kernel's plain-load path
+    from flag4j_gb300 import synth
+    for (m, n, k) in [(33, 17, 9), (5, 3, 1), (1, 7, 3)]:
+        A, B = synth.uniform(m, k, 7), synth.uniform(k, n, 8)
+        C, _ = run_gemm(f4j, A, B, mode=mode)
+        check_bound(C, *ref_bound(oracle, A, B, False), k, mode)
+    C, _ = run_gemm(f4j, np.zeros((4, 0)), np.zeros((0, 3)), mode=mode)
+    assert C.shape == (4, 3) and not C.any()
+
+
+# ------------------------------------------------------------------ split specifics
+def test_split_fp8_accumulation_is_exact(f4j):
+    """Known-answer test of the tcgen05 FP32 accumulator: one-digit slices
+    (x = d/16, |d| <= 15) make C = sum d_a d_b / 256 exactly representable; an
+    adversarial K order (large partial sums first, then +-1 products) must give
+    the exact integer result."""
+    rng = np.random.default_rng(5)
+    m, n, k = 128, 256, 8192
+    da = np.empty((m, k), np.int64)
+    db = np.empty((k, n), np.int64)
+    da[:, : k // 2] = 15
+    db[: k // 2, :] = 15
+    da[:, k // 2:] = rng.choice([-1, 1], size=(m, k // 2))
+    db[k // 2:, :] = rng.choice([-1, 1], size=(k // 2, n))
+    da[:, 0] = rng.integers(-15, 16, size=m)
+    exact = (da @ db).astype(np.float64) / 256.0
+    C, rep = run_gemm(f4j, da / 16.0, db / 16.0, mode="split")
+    assert np.array_equal(C, exact)
+    # two-digit values: d1/16 + d2/512 -> also exactly representable results
+    a2 = rng.integers(-15, 16, (m, 512)) * 32 + rng.integers(-15, 16, (m, 512))
+    b2 = rng.integers(-15, 16, (512, n)) * 32 + rng.integers(-15, 16, (512, n))
+    a2[:, 0] = 15 * 32
+    b2[0, :] = 15 * 32
+    C2, _ = run_gemm(f4j, a2 / 512.0, b2 / 512.0, mode="split")
+    assert np.array_equal(C2, (a2 @ b2).astype(np.float64) / 512.0 ** 2)
+
+
+@pytest.mark.parametrize("phi", [0, 8, 32])
+def test_split_scaled_inputs(f4j, oracle, phi):
+    from flag4j_gb300 import synth
+    m = n = k = 384
+    A = synth.scaled(m, k, phi, 21, "row")
+    B = synth.scaled(k, n, phi, 22, "col")
+    C, rep = run_gemm(f4j, A, B, mode="split")
+    check_bound(C, *ref_bound(oracle, A, B, False), k, "split phi=%d" % phi)
+
+
+def test_split_with_wide_spread_picks_more_slices(f4j, oracle):
+    from flag4j_gb300 import synth
+    A = synth.uniform(64, 256, 1) * np.ldexp(1.0, np.random.default_rng(0).integers(-30, 1, (64, 256)))
+    B = synth.uniform(256, 64, 2)
+    C, rep = run_gemm(f4j, A, B, mode="split")
+    _, rep0 = run_gemm(f4j, synth.uniform(64, 256, 1), B, mode="split")
+    assert rep.slices > rep0.slices
+    check_bound(C, *ref_bound(oracle, A, B, False), 256, "wide spread")
+
+
+def test_auto_mode_routes_nonfinite_to_dmma(f4j):
+    A = np.ones((16, 16))
+    A[3, 4] = np.nan
+    A[5, 5] = np.inf
+    B = np.ones((16, 16))
+    C, rep = run_gemm(f4j, A, B, mode="auto")
+    assert rep.mode_used == 0
+    assert np.isnan(C[3]).all() and not np.isnan(C[0]).any()
+
+
+def test_gemm_check_agrees_with_oracle(f4j, oracle):
+    from flag4j_gb300 import synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    A, B = synth.normal(300, 500, 1), synth.normal(500, 200, 2)
+    C = A @ B + 1e-9  # a deliberately perturbed product
+    dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.from_numpy(C)
+    ea, er = ctypes.c_double(), ctypes.c_double()
+    check(ctx.lib.f4j_gemm_check(ctx.handle, 0, 300, 200, 500, dA.handle, 0, dB.handle, 0, dC.handle, 256, 99,
+                                 ctypes.byref(ea), ctypes.byref(er)))
+    ii, jj = np.meshgrid(np.arange(300), np.arange(200), indexing="ij")
+    hi, lo, ab = oracle.truth_sampled(A, B, ii.ravel(), jj.ravel())
+    full = np.abs((C.ravel() - hi) - lo)
+    assert 0 < ea.value <= full.max() * (1 + 1e-12)
+    assert ea.value >= 0.5e-9
+
+
+# ------------------------------------------------------------------ adjoint
+@pytest.mark.parametrize("mode", ["exact", "plain", "split"])
+def test_dense_adjoint_matches_reference_formulas(f4j, oracle, mode):
+    from flag4j_gb300 import synth
+    m, k, n = 96, 64, 80
+    A, B, W = synth.normal(m, k, 1), synth.normal(k, n, 2), synth.normal(m, n, 3)
+    node = f4j.MatMulNode(f4j.Matrix(A), f4j.Matrix(B), mode=mode)
+    dA, dB = node.backward(f4j.Matrix(W))
+    refA = oracle.dgemm_abt(W, B)             # W.multTranspose(B)
+    refB = oracle.dgemm(A.T.copy(), W)        # A.T().mult(W)
+    if mode == "exact":
+        assert np.array_equal(dA.toNumpy(), refA) and np.array_equal(dB.toNumpy(), refB)
+    else:
+        check_bound(dA.toNumpy(), refA, np.abs(W) @ np.abs(B.T), n, "dA")
+        check_bound(dB.toNumpy(), refB, np.abs(A.T) @ np.abs(W), m, "dB")
+
+
+def test_complex_hermitian_adjoint(f4j, oracle):
+    from flag4j_gb300 import synth
+    m, k, n = 48, 40, 56
+    A = synth.normal(m, k, 1) + 1j * synth.normal(m, k, 2)
+    B = synth.normal(k, n, 3) + 1j * synth.normal(k, n, 4)
+    W = synth.normal(m, n, 5) + 1j * synth.normal(m, n, 6)
+    node = f4j.MatMulNode(f4j.CMatrix(A), f4j.CMatrix(B), mode="exact")
+    dA, dB = node.backward(f4j.CMatrix(W))
+    assert np.array_equal(dA.toNumpy(), oracle.zgemm(W, B.conj().T.copy()))   # W.mult(B.H())
+    assert np.array_equal(dB.toNumpy(), oracle.zgemm(A.conj().T.copy(), W))   # A.H().mult(W)
+
+
+@pytest.mark.parametrize("mode", ["plain", "split"])
+def test_dense_adjoint_finite_differences(f4j, mode):
+    """L = sum(W o (A B)); central differences (h = 1e-6) on 64 seeded entries."""
+    from flag4j_gb300 import synth
+    m, k, n = 64, 48, 40
+    A, B, W = synth.normal(m, k, 1), synth.normal(k, n, 2), synth.normal(m, n, 3)
+    node = f4j.MatMulNode(f4j.Matrix(A), f4j.Matrix(B), mode=mode)
+    dA, dB = node.backward(f4j.Matrix(W))
+    dA, dB = dA.toNumpy(), dB.toNumpy()
+    rng = np.random.default_rng(9)
+    h = 1e-6
+
+    def loss(Am, Bm):
+        return float(np.sum(W * f4j.Matrix(Am).mult(f4j.Matrix(Bm), mode=mode).toNumpy()))
+
+    for _ in range(32):
+        i, j = rng.integers(0, m), rng.integers(0, k)
+        Ap, Am_ = A.copy(), A.copy()
+        Ap[i, j] += h
+        Am_[i, j] -= h
+        fd = (loss(Ap, B) - loss(Am_, B)) / (2 * h)
+        assert abs(fd - dA[i, j]) <= 1e-7 * max(1.0, abs(dA[i, j]))
+        i, j = rng.integers(0, k), rng.integers(0, n)
+        Bp, Bm_ = B.copy(), B.copy()
+        Bp[i, j] += h
+        Bm_[i, j] -= h
+        fd = (loss(A, Bp) - loss(A, Bm_)) / (2 * h)
+        assert abs(fd - dB[i, j]) <= 1e-7 * max(1.0, abs(dB[i, j]))

@@ -1,0 +1,206 @@
+"""CSR products and sparse structure on the GPU: bit-identical to the oracle's
+restatement of Flag4j's loops (RealCsrDenseMatMult, CooMatrix.toCsr,
+CooDataSorter, RealCsrOps.transpose); SDDMM within 2 k u sum|a||b|."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import U
+
+pytestmark = pytest.mark.gpu
+
+
+def csr_from_dense(f4j, a):
+    return f4j.Matrix(a).toCsr()
+
+
+def test_golden_csr_dense_products(f4j, golden):
+    # RealCsrDenseMatMultTests.java:27-88: A.toCsr().mult(B) equals aDense.mult(B)
+    cases = [c for c in golden["csr_dense"] if c["call"] == "assertEquals"]
+    for c in cases:
+        a, b = np.array(c["vars"]["aEntries"]), np.array(c["vars"]["bEntries"])
+        A = csr_from_dense(f4j, a)
+        exp = f4j.Matrix(a).mult(f4j.Matrix(b), mode="exact")
+        assert A.mult(f4j.Matrix(b)) == exp
+        for j in range(b.shape[1]):
+            assert np.array_equal(A.mult(f4j.Vector(b[:, j])).data, f4j.Matrix(a).mult(
+                f4j.Matrix(b[:, j:j + 1]), mode="exact").data)
+    bad = [c for c in golden["csr_dense"] if c["call"] == "assertThrows"]
+    a, b = np.array(bad[0]["vars"]["aEntries"]), np.array(bad[0]["vars"]["bEntries"])
+    with pytest.raises(f4j.LinearAlgebraException):
+        csr_from_dense(f4j, a).mult(f4j.Matrix(b))
+    with pytest.raises(f4j.IllegalArgumentException, match="Expecting values to be equal"):
+        csr_from_dense(f4j, a).mult(f4j.Vector(np.ones(3)))
+
+
+def test_golden_csr_transpose(f4j, golden):
+    # CsrMatrixTransposeTests.java:24-51: A.T() equals denseA.T().toCsr()
+    for c in [c for c in golden["csr_transpose"] if c["method"] == "transposeTest" and c["call"] == "assertEquals"]:
+        a = np.array(c["vars"]["aDenseEntries"])
+        T = csr_from_dense(f4j, a).T()
+        E = csr_from_dense(f4j, a.T.copy())
+        assert np.array_equal(T.rowPointers, E.rowPointers)
+        assert np.array_equal(T.colIndices, E.colIndices)
+        assert np.array_equal(T.data, E.data)
+
+
+@pytest.mark.parametrize("rows,cols,lam,hi", [(1, 1, 1.0, 1), (300, 500, 16.0, 256), (5000, 4000, 16.0, 256),
+                                              (2000, 3000, 200.0, 256), (40000, 40000, 3.0, 8)])
+@pytest.mark.parametrize("ncols", [1, 3, 32, 64, 100])
+def test_spmm_spmv_bit_identical(f4j, oracle, rows, cols, lam, hi, ncols):
+    from flag4j_gb300 import synth
+    rp, ci, v = synth.csr_poisson(rows, cols, lam=lam, hi=hi, seed=rows + ncols)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    X = synth.normal(cols, ncols, 3)
+    assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X))
+    if ncols == 1:
+        assert np.array_equal(S.mult(f4j.Vector(X[:, 0])).data, oracle.spmv(rp, ci, v, X[:, 0]))
+
+
+def test_empty_rows_and_empty_matrix(f4j, oracle):
+    a = np.zeros((70, 9))
+    a[3, 2] = 1.5
+    a[69, 8] = -2.0
+    a[40, :] = np.arange(1, 10)
+    S = csr_from_dense(f4j, a)
+    X = np.arange(9 * 5, dtype=np.float64).reshape(9, 5)
+    assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(S.rowPointers, S.colIndices, S.data, X))
+    Z = f4j.CsrMatrix((6, 4), np.zeros(0), np.zeros(7, np.int32), np.zeros(0, np.int32))
+    assert not Z.mult(f4j.Matrix(np.ones((4, 3)))).toNumpy().any()
+    assert not Z.mult(f4j.Vector(np.ones(4))).data.any()
+
+
+def test_full_config_csr_products(f4j, oracle):
+    """2^20 x 2^20, Poisson(16) row lengths: SpMV and SpMM (32 columns) bit-identical."""
+    from flag4j_gb300 import synth
+    n = 1 << 20
+    rp, ci, v = synth.csr_poisson(n, n, seed=2024)
+    S = f4j.CsrMatrix((n, n), v, rp, ci)
+    x = synth.normal(n, 1, 5).ravel()
+    assert np.array_equal(S.mult(f4j.Vector(x)).data, oracle.spmv(rp, ci, v, x, threads=8))
+    X = synth.normal(n, 32, 6)
+    assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X, threads=8))
+
+
+# ------------------------------------------------------------------ structure
+def test_coo_to_csr_bit_exact(f4j, oracle):
+    from flag4j_gb300 import synth
+    rp, ci, v = synth.csr_poisson(20000, 7000, seed=4)
+    r = np.repeat(np.arange(20000, dtype=np.int32), np.diff(rp))
+    S = f4j.CooMatrix((20000, 7000), v, r, ci).toCsr()
+    assert np.array_equal(S.rowPointers, oracle.coo_to_csr(20000, r))
+    assert np.array_equal(S.colIndices, ci) and np.array_equal(S.data, v)
+
+
+def test_coo_sort_stable_bit_exact(f4j, oracle):
+    from flag4j_gb300 import synth
+    rp, ci, v = synth.csr_poisson(3000, 2000, seed=5)
+    r, c, vv = synth.coo_shuffled(rp, ci, v, seed=6)
+    # duplicates (same (row, col) twice) must keep their input order
+    r = np.concatenate([r, r[:500]])
+    c = np.concatenate([c, c[:500]])
+    vv = np.concatenate([vv, -vv[:500]])
+    er, ec, ev, _ = oracle.coo_sort(r, c, vv)
+    coo = f4j.CooMatrix((3000, 2000), vv.copy(), r.copy(), c.copy()).sortIndices()
+    assert np.array_equal(coo.rowIndices, er) and np.array_equal(coo.colIndices, ec)
+    assert np.array_equal(coo.data, ev)
+
+
+def test_transpose_and_permutation_bit_exact(f4j, oracle):
+    from flag4j_gb300 import synth
+    rows, cols = 9000, 5000
+    rp, ci, v = synth.csr_poisson(rows, cols, seed=8)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    trp, tci, tv, perm = oracle.csr_transpose(rows, cols, rp, ci, v)
+    T = S.T()
+    assert np.array_equal(T.rowPointers, trp) and np.array_equal(T.colIndices, tci)
+    assert np.array_equal(T.data, tv)
+    assert np.array_equal(S.transposePermutation(), perm)
+
+
+@pytest.mark.parametrize("ncols", [1, 32, 64, 7])
+def test_spmm_transpose_bit_exact(f4j, oracle, ncols):
+    """dX = S^T dC without forming S^T equals S.T().mult(dC) of the reference."""
+    from flag4j_gb300 import synth
+    rows, cols = 12000, 9000
+    rp, ci, v = synth.csr_poisson(rows, cols, seed=9)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    dC = synth.normal(rows, ncols, 10)
+    trp, tci, tv, _ = oracle.csr_transpose(rows, cols, rp, ci, v)
+    assert np.array_equal(S.multTransposeLeft(f4j.Matrix(dC)).toNumpy(), oracle.spmm(trp, tci, tv, dC))
+
+
+@pytest.mark.parametrize("ncols", [64, 5, 130])
+def test_sddmm_within_bound(f4j, oracle, ncols):
+    from flag4j_gb300 import synth
+    from flag4j_gb300.device import check
+    rows, cols = 4000, 3000
+    rp, ci, v = synth.csr_poisson(rows, cols, seed=11)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    A, B = synth.normal(rows, ncols, 1), synth.normal(cols, ncols, 2)
+    ctx = f4j.default_context()
+    out = ctx.alloc(8 * len(v))
+    dA, dB = ctx.from_numpy(A), ctx.from_numpy(B)
+    check(ctx.lib.f4j_sddmm(ctx.handle, S.handle(ctx), dA.handle, dB.handle, ncols, out.handle, None))
+    got = out.to_numpy(np.float64, len(v))
+    ref = oracle.sddmm(rp, ci, A, B)
+    rows_of = np.repeat(np.arange(rows), np.diff(rp))
+    absab = np.sum(np.abs(A[rows_of]) * np.abs(B[ci]), axis=1)
+    assert np.all(np.abs(got - ref) <= 2 * ncols * U * absab)
+
+
+def test_sparse_adjoint_finite_differences(f4j):
+    """C = S X, L = sum(W o C): dX = S^T W, dS = (W X^T) on pattern(S); central FD."""
+    from flag4j_gb300 import synth
+    rows, cols, nc = 3000, 2000, 64
+    rp, ci, v = synth.csr_poisson(rows, cols, seed=12)
+    X, W = synth.normal(cols, nc, 1), synth.normal(rows, nc, 2)
+    node = f4j.SpMMNode(f4j.CsrMatrix((rows, cols), v, rp, ci), f4j.Matrix(X))
+    dS, dX = node.backward(f4j.Matrix(W))
+    dS, dX = dS.data, dX.toNumpy()
+    rng = np.random.default_rng(3)
+    h = 1e-6
+
+    def loss(vals, Xm):
+        return float(np.sum(W * f4j.CsrMatrix((rows, cols), vals, rp, ci).mult(f4j.Matrix(Xm)).toNumpy()))
+
+    for _ in range(16):
+        q = rng.integers(0, len(v))
+        vp, vm = v.copy(), v.copy()
+        vp[q] += h
+        vm[q] -= h
+        fd = (loss(vp, X) - loss(vm, X)) / (2 * h)
+        assert abs(fd - dS[q]) <= 1e-7 * max(1.0, abs(dS[q]))
+        i, j = rng.integers(0, cols), rng.integers(0, nc)
+        Xp, Xm_ = X.copy(), X.copy()
+        Xp[i, j] += h
+        Xm_[i, j] -= h
+        fd = (loss(v, Xp) - loss(v, Xm_)) / (2 * h)
+        assert abs(fd - dX[i, j]) <= 1e-7 * max(1.0, abs(dX[i, j]))
+
+
+# ------------------------------------------------------------------ validation (host-side faults only)
+def _wrap(f4j, rows, cols, rp, ci, v, validate=1):
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    bufs = [ctx.from_numpy(np.asarray(rp, np.int32)), ctx.from_numpy(np.asarray(ci, np.int32)),
+            ctx.from_numpy(np.asarray(v, np.float64))]
+    h = ctypes.c_void_p()
+    check(ctx.lib.f4j_csr_wrap(ctx.handle, rows, cols, len(v), bufs[0].handle, bufs[1].handle, bufs[2].handle,
+                               validate, ctypes.byref(h)))
+    ctx.lib.f4j_csr_free(ctx.handle, h)
+
+
+def test_device_csr_validation_messages(f4j):
+    _wrap(f4j, 3, 3, [0, 1, 2, 3], [0, 1, 2], [1.0, 2.0, 3.0])
+    with pytest.raises(f4j.IllegalArgumentException, match="monotonically increasing"):
+        _wrap(f4j, 3, 3, [0, 2, 1, 3], [0, 1, 2], [1.0, 2.0, 3.0])
+    with pytest.raises(f4j.IllegalArgumentException, match="Invalid column index"):
+        _wrap(f4j, 3, 3, [0, 1, 2, 3], [0, 5, 2], [1.0, 2.0, 3.0])
+    with pytest.raises(f4j.IllegalArgumentException, match="must be positive"):
+        _wrap(f4j, 3, 3, [-1, 1, 2, 3], [0, 1, 2], [1.0, 2.0, 3.0])
+    with pytest.raises(f4j.IllegalArgumentException, match="elements but nnz"):
+        _wrap(f4j, 3, 3, [0, 1, 2, 2], [0, 1, 2], [1.0, 2.0, 3.0])
+    with pytest.raises(f4j.IllegalArgumentException, match="Invalid index"):
+        f4j.CooMatrix((3, 3), [1.0, 2.0], [0, 3], [0, 1]).toCsr()

@@ -1,0 +1,110 @@
+"""Pins the CPU oracle to Flag4j's own known-answer tests (bit-exact).
+
+Fixtures: tests/golden/reference_golden.json, extracted from the reference's
+JUnit sources by tests/golden/make_golden.py.
+"""
+import numpy as np
+import pytest
+
+
+def cplx(a):
+    a = np.asarray(a, dtype=np.float64)
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def test_real_kernels_bit_exact(oracle, golden):
+    # src/test/java/org/flag4j/linalg/ops/dense/real/MatrixMultiplyTests.java:13-135
+    n = 0
+    for c in golden["real_kernels"]:
+        v = c["vars"]
+        A, B, exp = np.array(v["entriesA"]), np.array(v["entriesB"]), np.array(v["exp"])
+        assert np.array_equal(oracle.dgemm(A, B).ravel(), exp), c["line"]
+        if c["method"] == "columnVectorTestCase":
+            assert np.array_equal(oracle.dgemv_blocked(A, B[:, 0]), exp), c["line"]
+        n += 1
+    assert n == 20
+
+
+def test_complex_kernels_bit_exact(oracle, golden):
+    # src/test/java/org/flag4j/linalg/ops/dense/complex/CMatrixMultiplyTests.java:13-169
+    for c in golden["complex_kernels"]:
+        v = c["vars"]
+        A, B, exp = cplx(v["entriesA"]), cplx(v["entriesB"]), cplx(v["exp"])
+        assert np.array_equal(oracle.zgemm(A, B).ravel(), exp), c["line"]
+
+
+def test_api_level_products(oracle, golden):
+    # MatrixMultTests.java:25-62, CMatrixMultTests.java:62-101, MatrixVectorTests.java:26-58
+    mm = [c for c in golden["matrix_mult"] if c["method"] == "matMultTestCase" and c["call"] == "assertEquals"]
+    v = mm[0]["vars"]
+    assert np.array_equal(oracle.dgemm(np.array(v["aEntries"]), np.array(v["bEntries"])),
+                          np.array(v["expEntries"]))
+    cm = [c for c in golden["cmatrix_mult"] if c["method"] == "matMultComplexTestCase" and c["call"] == "assertEquals"]
+    v = cm[0]["vars"]
+    assert np.array_equal(oracle.zgemm(cplx(v["aEntries"]), cplx(v["bEntries"])), cplx(v["expEntries"]))
+    mv = [c for c in golden["matrix_vector"] if c["method"] == "matVecMultTestCase" and c["call"] == "assertEquals"]
+    v = mv[0]["vars"]
+    A, x = np.array(v["aEntries"]), np.array(v["bEntries"])
+    assert np.array_equal(oracle.dgemv_blocked(A, x), np.array(v["expEntries"]))
+
+
+def test_mult_transpose_matches_mult(oracle, golden):
+    # MatrixMultTests.java:249-265: A.multTranspose(B) == A.mult(B.T())
+    c = [c for c in golden["matrix_mult"] if c["method"] == "multTransposeTestCase"][0]
+    A, Bt = np.array(c["vars"]["aEntries"]), np.array(c["vars"]["bEntries"])
+    # the test's B = bEntries^T, so multTranspose multiplies by bEntries
+    assert np.array_equal(oracle.dgemm_abt(A, Bt.T.copy()), oracle.dgemm(A, Bt))
+
+
+def _csr_of_dense(a):
+    r, c = np.nonzero(a != 0.0)
+    rp = oracle_coo_to_csr_rows(a.shape[0], r)
+    return rp, c.astype(np.int32), a[r, c]
+
+
+def oracle_coo_to_csr_rows(rows, r):
+    from oracle import oracle as O
+    return O.coo_to_csr(rows, r.astype(np.int32))
+
+
+def test_csr_dense_products_equal_dense(oracle, golden):
+    # RealCsrDenseMatMultTests.java:27-88: A.toCsr().mult(B) equals aDense.mult(B) exactly
+    cases = [c for c in golden["csr_dense"] if c["call"] == "assertEquals"]
+    assert len(cases) == 2
+    for c in cases:
+        a, b = np.array(c["vars"]["aEntries"]), np.array(c["vars"]["bEntries"])
+        rp, ci, v = _csr_of_dense(a)
+        assert np.array_equal(oracle.spmm(rp, ci, v, b), oracle.dgemm(a, b))
+        for j in range(b.shape[1]):
+            assert np.array_equal(oracle.spmv(rp, ci, v, b[:, j].copy()), oracle.dgemm(a, b[:, j:j + 1]).ravel())
+
+
+def test_csr_transpose_matches_dense_transpose(oracle, golden):
+    # CsrMatrixTransposeTests.java:24-51: A.T() equals denseA.T().toCsr()
+    cases = [c for c in golden["csr_transpose"] if c["method"] == "transposeTest" and c["call"] == "assertEquals"]
+    assert len(cases) == 2
+    for c in cases:
+        a = np.array(c["vars"]["aDenseEntries"])
+        rp, ci, v = _csr_of_dense(a)
+        trp, tci, tv, perm = oracle.csr_transpose(a.shape[0], a.shape[1], rp, ci, v)
+        erp, eci, ev = _csr_of_dense(a.T.copy())
+        assert np.array_equal(trp, erp) and np.array_equal(tci, eci) and np.array_equal(tv, ev)
+        assert np.array_equal(v[perm], tv)
+
+
+def test_coo_sort_is_stable_lexicographic(oracle):
+    rng = np.random.default_rng(3)
+    r = rng.integers(0, 5, 400).astype(np.int32)
+    c = rng.integers(0, 4, 400).astype(np.int32)
+    vals = np.arange(400, dtype=np.float64)
+    rs, cs, vs, perm = oracle.coo_sort(r, c, vals)
+    exp = sorted(range(400), key=lambda i: (r[i], c[i], i))
+    assert np.array_equal(perm, exp) and np.array_equal(vs, vals[exp])
+
+
+def test_truth_oracle_is_compensated(oracle):
+    # Dot2 recovers a sum that plain FP64 loses entirely.
+    A = np.array([[1e16, 1.0, -1e16]])
+    B = np.array([[1.0], [1.0], [1.0]])
+    hi, lo, ab = oracle.truth_sampled(A, B, [0], [0])
+    assert hi[0] + lo[0] == 1.0 and oracle.dgemm(A, B)[0, 0] == 0.0
