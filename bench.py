@@ -1,0 +1,490 @@
+"""Benchmark of the GB300 engine for Flag4j's product path.
+
+One step = one FP64-accurate GEMM C = A B at 8192^3 (real float64, entries
+u 2^e, u ~ U[-1,1), integer e ~ U[-8, 8] per row of A / column of B) through
+the split path: exponent statistics, FP8 slicing and the tcgen05 slice GEMM.
+value = 2 m n k / step time (TFLOP/s, FP64-equivalent), inputs resident in
+HBM (A, B: 512 MiB each, larger than L2, so no flush is needed).  The same JSON
+line carries the plain DMMA path, errors against the double-double check for
+phi in {0, 8, 32}, the Complex128 4096^3 product, CSR SpMV/SpMM GB/s at 2^20
+rows (Poisson(16) row lengths), the dense adjoint step ratio, the roofline of
+the slice GEMM kernel, the CPU baseline and an end-to-end number through the
+host-buffer API (host<->device copies inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --case small        # 2048^3 / 2^16-row variant (profiling)
+Under torchrun each rank runs an independent replica on its own GPU
+(replicas only: the path does not shard); rank 0 prints the max-over-ranks line.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64-accurate GEMM TFLOP/s (split vs plain DMMA) at stated err; CSR SpMM GB/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--case", default="full", choices=["full", "small"])
+    p.add_argument("--skip-extras", action="store_true", help="headline GEMM only (for profiling)")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max over ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (median SM clock, reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+class Eng:
+    def __init__(self, device):
+        import flag4j_gb300 as f
+        from flag4j_gb300 import _lib
+        from flag4j_gb300.device import check
+        self.f, self.L, self.check = f, _lib, check
+        self.ctx = f.Context(device)
+        self.lib = self.ctx.lib
+
+    def dev(self, arr):
+        return self.ctx.from_numpy(arr)
+
+    def gemm(self, A, B, C, m, n, k, mode, cplx=False, opA=0, opB=0):
+        rep = self.L.f4j_report()
+        fn = self.lib.f4j_zgemm if cplx else self.lib.f4j_dgemm
+        self.check(fn(self.ctx.handle, m, n, k, A.handle, opA, B.handle, opB, C.handle, mode, ctypes.byref(rep)))
+        return rep
+
+    def check_err(self, A, B, C, m, n, k, cplx=False, samples=4096, seed=1234):
+        ea, er = ctypes.c_double(), ctypes.c_double()
+        self.check(self.lib.f4j_gemm_check(self.ctx.handle, int(cplx), m, n, k, A.handle, 0, B.handle, 0,
+                                           C.handle, samples, seed, ctypes.byref(ea), ctypes.byref(er)))
+        return ea.value, er.value
+
+    def kernel_ms(self, fn, steps):
+        """Average CUDA-event time of the main product kernel inside fn()."""
+        self.check(self.lib.f4j_set_profiling(self.ctx.handle, 1))
+        for _ in range(steps):
+            fn()
+        tot, cnt = ctypes.c_double(), ctypes.c_int64()
+        self.check(self.lib.f4j_profile_read(self.ctx.handle, ctypes.byref(tot), ctypes.byref(cnt)))
+        self.check(self.lib.f4j_set_profiling(self.ctx.handle, 0))
+        return tot.value / max(cnt.value, 1)
+
+    def timed(self, fn, steps, warmup):
+        """Average ms per call with CUDA events on the context stream."""
+        for _ in range(warmup):
+            fn()
+        self.ctx.sync()
+        self.ctx.timer_record(0)
+        for _ in range(steps):
+            fn()
+        self.ctx.timer_record(1)
+        ms = self.ctx.timer_elapsed(0, 1) / steps
+        self.ctx.sync()
+        return ms
+
+
+def fp8_peak_tflops():
+    """Dense E4M3 peak measured with cuBLASLt (torch._scaled_mm), 8192^3, best of 10."""
+    try:
+        import torch
+        n = 8192
+        a = torch.randn(n, n, device="cuda").to(torch.float8_e4m3fn)
+        b = torch.randn(n, n, device="cuda").to(torch.float8_e4m3fn).t()
+        one = torch.tensor(1.0, device="cuda")
+        for _ in range(3):
+            torch._scaled_mm(a, b, scale_a=one, scale_b=one, out_dtype=torch.bfloat16)
+        best = 1e9
+        for _ in range(10):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch._scaled_mm(a, b, scale_a=one, scale_b=one, out_dtype=torch.bfloat16)
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e))
+        del a, b
+        torch.cuda.empty_cache()
+        return 2 * n ** 3 / (best * 1e-3) / 1e12, "cuBLASLt e4m3 8192^3 via torch._scaled_mm, best of 10, this run"
+    except Exception as ex:  # noqa: BLE001
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+        return 2 * peaks["bf16_tflops"], "2 x measured bf16 (fp8 measurement failed: %s)" % type(ex).__name__
+
+
+def fp64_peak_tflops():
+    """FP64 GEMM peak measured with cuBLAS DGEMM (torch.matmul float64), 8192^3, best of 3."""
+    try:
+        import torch
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float64)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float64)
+        torch.matmul(a, b)
+        best = 1e9
+        for _ in range(3):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e))
+        del a, b
+        torch.cuda.empty_cache()
+        return 2 * n ** 3 / (best * 1e-3) / 1e12
+    except Exception:  # noqa: BLE001
+        return None
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "MEASURED_PEAKS.json hbm_gbs"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(n, k, seconds_target=15.0):
+    """Flag4j's GEMM loop order (C restatement of RealDenseMatMult.concurrentBlockedReordered,
+    bit-identical to the Java kernel) on all host cores, over a row sample of the
+    same 8192^3 product (C rows 0..r-1 need A rows 0..r-1 and all of B)."""
+    from oracle import oracle as O
+    from flag4j_gb300 import synth
+    threads = os.cpu_count() or 1
+    B = synth.scaled(k, n, 8, 2, "col")
+    rows = threads
+    A = synth.scaled(rows, k, 8, 1, "row")
+    t0 = time.perf_counter()
+    O.dgemm(A, B, threads=threads)
+    dt = time.perf_counter() - t0
+    rows = max(threads, int(rows * seconds_target / max(dt, 1e-3)) // threads * threads)
+    rows = min(rows, 4096)
+    A = synth.scaled(rows, k, 8, 1, "row")
+    t0 = time.perf_counter()
+    O.dgemm(A, B, threads=threads)
+    dt = time.perf_counter() - t0
+    flops = 2.0 * rows * n * k
+    return {"value": flops / dt / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d rows of C = A B (k = n = %d), C restatement of Flag4j's k-ascending no-FMA loop "
+                      "(g++ -O2 -ffp-contract=off), %d pthreads, %.1f s" % (rows, n, n, threads, dt)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    n = 8192 if args.case == "full" else 2048
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(n, n, seconds_target=8.0 if args.case == "full" else 2.0)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 2.0 * n ** 3 / (v * 1e12) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "impl": "reference",
+            "config": {"workload": "FP64 GEMM %d^3, u*2^e, e~U[-8,8] per row/col" % n, "cpu": "host cores"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "notes": "Flag4j is pure Java and neither machine has a JVM; the reference arm is the C "
+                     "restatement of its GEMM loop (bit-identical to the Java kernel on the golden vectors), "
+                     "timed on a row sample of the workload each step."}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    ws, rank, local = dist_env()
+    dist = Dist(ws)
+    from flag4j_gb300 import build, synth
+    build.build()
+    E = Eng(local)
+    L = E.L
+    full = args.case == "full"
+    n = 8192 if full else 2048
+    out = {}
+
+    # ---- headline: split GEMM n^3, phi = 8
+    A_h = synth.scaled(n, n, 8, 1, "row")
+    B_h = synth.scaled(n, n, 8, 2, "col")
+    A, B = E.dev(A_h), E.dev(B_h)
+    C = E.ctx.alloc(8 * n * n)
+    rep = E.gemm(A, B, C, n, n, n, L.MODE_SPLIT)
+    E.ctx.sync()
+    clk = Clocks(local)
+    dist.barrier()
+    E.ctx.sync()
+    l0 = E.ctx.launches()
+    clk.start()
+    for _ in range(args.warmup):
+        E.gemm(A, B, C, n, n, n, L.MODE_SPLIT)
+    E.ctx.sync()
+    dist.barrier()
+    E.ctx.sync()
+    l0 = E.ctx.launches()
+    E.ctx.timer_record(0)
+    for _ in range(args.steps):
+        E.gemm(A, B, C, n, n, n, L.MODE_SPLIT)
+    E.ctx.timer_record(1)
+    ms_local = E.ctx.timer_elapsed(0, 1) / args.steps
+    E.ctx.sync()
+    launches = E.ctx.launches() - l0
+    dist.barrier()
+    clocks = clk.stop()
+    ms = dist.max(ms_local)
+    flops = 2.0 * n ** 3
+    value = ws * flops / (ms * 1e-3) / 1e12
+    abs_err, rel_err = E.check_err(A, B, C, n, n, n)
+
+    # dominant kernel time: the tcgen05 slice GEMM alone (same inputs), for the roofline
+    s = rep.slices
+    prods = s * (s + 1) // 2
+    kp = math.ceil(n / 128) * 128
+    fp8_flops = prods * 2.0 * n * n * kp
+    out["split"] = {"slices": s, "frac_bits": rep.frac_bits, "exp_spread_bits": round(rep.exp_spread, 3),
+                    "launches_per_step": launches / args.steps, "max_abs_err": abs_err, "max_rel_err": rel_err,
+                    "ms": ms_local, "fp8_products": prods}
+
+    if not args.skip_extras:
+        # ---- plain DMMA path on the same inputs
+        pms = E.timed(lambda: E.gemm(A, B, C, n, n, n, L.MODE_PLAIN), 1 if full else 3, 1)
+        pa, pr = E.check_err(A, B, C, n, n, n)
+        out["plain_dmma"] = {"tflops": flops / (pms * 1e-3) / 1e12, "ms": pms, "max_abs_err": pa, "max_rel_err": pr}
+        out["split_vs_plain_speedup"] = pms / ms_local
+        # ---- errors for phi in {0, 8, 32}: split vs plain (double-double sampled check)
+        errs = {}
+        for phi in (0, 8, 32):
+            Ap, Bp = E.dev(synth.scaled(n, n, phi, 10 + phi, "row")), E.dev(synth.scaled(n, n, phi, 20 + phi, "col"))
+            r = E.gemm(Ap, Bp, C, n, n, n, L.MODE_SPLIT)
+            se = E.check_err(Ap, Bp, C, n, n, n)
+            E.gemm(Ap, Bp, C, n, n, n, L.MODE_PLAIN)
+            pe = E.check_err(Ap, Bp, C, n, n, n)
+            errs[str(phi)] = {"slices": r.slices, "split_max_rel_err": se[1], "plain_max_rel_err": pe[1],
+                              "split_max_abs_err": se[0], "plain_max_abs_err": pe[0]}
+            del Ap, Bp
+        out["errors_by_phi"] = errs
+        del A, B
+        # ---- Complex128 n/2 ^3 (8mnk basis)
+        nz = n // 2
+        Az = synth.scaled(nz, nz, 8, 3, "row", cplx=True)
+        Bz = synth.scaled(nz, nz, 8, 4, "col", cplx=True)
+        dAz, dBz, dCz = E.dev(Az), E.dev(Bz), E.ctx.alloc(16 * nz * nz)
+        zr = E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_SPLIT, cplx=True)
+        zms = E.timed(lambda: E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_SPLIT, cplx=True), 3, 1)
+        zs = E.check_err(dAz, dBz, dCz, nz, nz, nz, cplx=True)
+        zpms = E.timed(lambda: E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_PLAIN, cplx=True), 1, 1)
+        zp = E.check_err(dAz, dBz, dCz, nz, nz, nz, cplx=True)
+        zf = 8.0 * nz ** 3
+        out["complex"] = {"n": nz, "split_tflops": zf / (zms * 1e-3) / 1e12, "split_ms": zms, "slices": zr.slices,
+                          "split_max_rel_err": zs[1], "plain_tflops": zf / (zpms * 1e-3) / 1e12,
+                          "plain_max_rel_err": zp[1]}
+        del dAz, dBz, dCz
+        # ---- dense adjoint step: A (n/2 x n/4), B (n/4 x n/2), split
+        ma, ka = n // 2, n // 4
+        Aa, Ba, Wa = (E.dev(synth.normal(ma, ka, 5)), E.dev(synth.normal(ka, ma, 6)),
+                      E.dev(synth.normal(ma, ma, 7)))
+        Ca, dA, dB = E.ctx.alloc(8 * ma * ma), E.ctx.alloc(8 * ma * ka), E.ctx.alloc(8 * ka * ma)
+        fwd = E.timed(lambda: E.gemm(Aa, Ba, Ca, ma, ma, ka, L.MODE_SPLIT), 3, 1)
+
+        def step():
+            E.gemm(Aa, Ba, Ca, ma, ma, ka, L.MODE_SPLIT)
+            E.check(E.lib.f4j_dgemm_adjoint(E.ctx.handle, ma, ma, ka, Aa.handle, Ba.handle, Wa.handle, dA.handle,
+                                            dB.handle, L.MODE_SPLIT, None))
+        fb = E.timed(step, 3, 1)
+        out["adjoint"] = {"shape": [ma, ka, ma], "forward_ms": fwd, "fwd_bwd_ms": fb, "ratio": fb / fwd}
+        del Aa, Ba, Wa, Ca, dA, dB
+        # ---- CSR SpMV / SpMM at 2^20 rows
+        rows = (1 << 20) if full else (1 << 16)
+        rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
+        nnz = len(v)
+        S = E.f.CsrMatrix((rows, rows), v, rp, ci)
+        hS = S.handle(E.ctx)
+        x = E.dev(synth.normal(rows, 1, 5).ravel())
+        y = E.ctx.alloc(8 * rows)
+        X = E.dev(synth.normal(rows, 32, 6))
+        Y = E.ctx.alloc(8 * rows * 32)
+        t_spmv = E.timed(lambda: E.check(E.lib.f4j_spmv(E.ctx.handle, hS, x.handle, y.handle, None)), 20, 3)
+        t_spmm = E.timed(lambda: E.check(E.lib.f4j_spmm(E.ctx.handle, hS, X.handle, 32, Y.handle, None)), 20, 3)
+        b_spmv = 12.0 * nnz + 4.0 * (rows + 1) + 16.0 * rows
+        b_spmm = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 32 * rows
+        b_spmm_g = 12.0 * nnz + 8.0 * 32 * nnz + 8.0 * 32 * rows
+        hbm, hbm_src = measured_peaks()
+        out["spmm"] = {"rows": rows, "nnz": nnz, "spmm_ms": t_spmm, "spmm_gbs_compulsory": b_spmm / t_spmm / 1e6,
+                       "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm / 1e6,
+                       "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
+                       "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
+                       "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True}
+        del x, y, X, Y, S
+
+    # ---- roofline of the dominant kernel (the tcgen05 slice GEMM), timed alone
+    # with CUDA events around its launch on the context stream
+    A, B = E.dev(A_h), E.dev(B_h)
+    kms = E.kernel_ms(lambda: E.gemm(A, B, C, n, n, n, L.MODE_SPLIT), max(3, args.steps // 2))
+    del A, B
+    fp8_peak, fp8_src = fp8_peak_tflops() if not args.skip_extras else (2 * 1927.7, "2 x measured bf16")
+    achieved = fp8_flops / (kms * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp8_peak, "traffic": None, "kernel": "k_split_gemm (tcgen05 kind::f8f6f4)",
+                "kernel_ms": kms, "kernel_share_of_step": kms / ms_local,
+                "basis": "FP8 MMA flops per launch: s(s+1)/2 slice products x 2 n n Kp",
+                "peak_source": fp8_src}
+    fp64_peak = fp64_peak_tflops() if not args.skip_extras else None
+    if fp64_peak:
+        out["fp64_dgemm_peak_tflops"] = fp64_peak
+
+    # ---- end to end through the host-buffer API (pinned host memory)
+    Ah = np.ascontiguousarray(A_h)
+    Bh = np.ascontiguousarray(B_h)
+    Ch = np.empty((n, n))
+    for arr in (Ah, Bh, Ch):
+        E.check(E.lib.f4j_host_register(arr.ctypes.data, arr.nbytes))
+    A2, B2, C2 = E.ctx.alloc(Ah.nbytes), E.ctx.alloc(Bh.nbytes), E.ctx.alloc(Ch.nbytes)
+
+    def e2e():
+        A2.upload(Ah, sync=False)
+        B2.upload(Bh, sync=False)
+        E.gemm(A2, B2, C2, n, n, n, L.MODE_SPLIT)
+        C2.download(Ch, sync=False)
+    e2e_ms = E.timed(e2e, max(3, args.steps // 3), 2)
+    e2e_ms = dist.max(e2e_ms)
+    for arr in (Ah, Bh, Ch):
+        E.lib.f4j_host_unregister(arr.ctypes.data)
+
+    cb = None
+    if rank == 0 and ws == 1:
+        from oracle import oracle as O
+        O.build()
+        cb = cpu_baseline(n, n, seconds_target=15.0 if full else 3.0)
+
+    dist.close()
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (FP8 E4M3 slices, exact FP32/int64 accumulation)",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": "FP64-accurate GEMM %d^3 (split path), A u*2^e per row, B per column, "
+                                   "u~U[-1,1), e~U[-8,8]" % n,
+                       "l2": "inputs larger than L2 (A, B 512 MiB each), no flush",
+                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "roofline": roofline, "cpu_baseline": cb,
+            "e2e": {"value": ws * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes},
+            "gpu_launches": launches, "clocks": clocks}
+    line.update(out)
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -422,10 +422,12 @@ int f4j_gemm_exact(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     int64_t ldb = (opB == F4J_OP_N) ? n : k;
     dim3 grid((unsigned)f4j_cdiv(n, EX_BN), (unsigned)f4j_cdiv(m, EX_BM));
     if (grid.y > 65535) return f4j_fail(F4J_ERR_ARG, "m too large for the exact kernel grid");
+    f4j_prof_begin(ctx);
     if (cplx)
         k_gemm_exact<true><<<grid, EX_T, 0, ctx->stream>>>(m, n, k, A, lda, opA, B, ldb, opB, C);
     else
         k_gemm_exact<false><<<grid, EX_T, 0, ctx->stream>>>(m, n, k, A, lda, opA, B, ldb, opB, C);
+    f4j_prof_end(ctx);
     F4J_LAUNCHED(ctx);
     return F4J_OK;
 }
@@ -472,11 +474,14 @@ int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     size_t smem = (size_t)DM_ST * (cplx ? DmTile<true>::STAGE_BYTES : DmTile<false>::STAGE_BYTES);
     if (cplx) {
         F4J_CUDA(cudaFuncSetAttribute(k_gemm_dmma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        f4j_prof_begin(ctx);
         k_gemm_dmma<true><<<grid, DM_THREADS, smem, ctx->stream>>>(ta, tb, p);
     } else {
         F4J_CUDA(cudaFuncSetAttribute(k_gemm_dmma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        f4j_prof_begin(ctx);
         k_gemm_dmma<false><<<grid, DM_THREADS, smem, ctx->stream>>>(ta, tb, p);
     }
+    f4j_prof_end(ctx);
     F4J_LAUNCHED(ctx);
     return F4J_OK;
 }

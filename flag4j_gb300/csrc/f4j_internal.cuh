@@ -39,7 +39,17 @@ struct f4j_ctx {
     cudaEvent_t ev[16];
     bool ev_init[16];
     int64_t launches;
+    // Opt-in profiling: CUDA events around each main product kernel.
+    bool prof;
+    int prof_n;
+    cudaEvent_t prof_ev[2 * 256];
+    bool prof_init;
 };
+
+// Bracket the main kernel of a product with profiling events (no-ops unless
+// profiling is on).
+void f4j_prof_begin(f4j_ctx* ctx);
+void f4j_prof_end(f4j_ctx* ctx);
 
 // ---------------------------------------------------------------- errors
 int f4j_fail(int code, const char* fmt, ...);

@@ -440,6 +440,7 @@ static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp,
     while (G < 32 && G * per_lane < ncols) G *= 2;
     const int64_t threads = rows * G;
     const unsigned blocks = (unsigned)f4j_cdiv(threads, 256);
+    f4j_prof_begin(ctx);
     if (vec2) {
         if (perm) k_spmm<true, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
         else k_spmm<true, false><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
@@ -447,6 +448,7 @@ static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp,
         if (perm) k_spmm<false, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
         else k_spmm<false, false><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
     }
+    f4j_prof_end(ctx);
     F4J_LAUNCHED(ctx);
     return F4J_OK;
 }
@@ -703,9 +705,11 @@ extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_repor
     int64_t l0 = ctx->launches;
     if (S->rows) {
         const unsigned blocks = (unsigned)f4j_cdiv(S->rows, SPMV_WARPS * 32);
+        f4j_prof_begin(ctx);
         k_spmv<<<blocks, SPMV_WARPS * 32, 0, ctx->stream>>>(S->rows, (const int*)S->rowptr->ptr,
                                                             (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
                                                             (const double*)x->ptr, (double*)y->ptr);
+        f4j_prof_end(ctx);
         F4J_LAUNCHED(ctx);
     }
     if (rep) {
@@ -770,9 +774,11 @@ extern "C" int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t 
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     if (S->rows && S->nnz) {
+        f4j_prof_begin(ctx);
         k_sddmm<<<(unsigned)f4j_cdiv(S->rows * 32, 256), 256, 0, ctx->stream>>>(
             S->rows, ncols, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)A->ptr,
             (const double*)B->ptr, (double*)out->ptr);
+        f4j_prof_end(ctx);
         F4J_LAUNCHED(ctx);
     }
     if (rep) {

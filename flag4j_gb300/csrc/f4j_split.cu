@@ -29,7 +29,7 @@
 
 namespace {
 
-constexpr int S_MAX = 14;          // at most 14 slices (4 + 65 = 69 bits)
+constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits keeps Y < 2^62 in int64
 constexpr int BM = 128, BN = 128;  // output tile
 constexpr int BKB = 128;           // K bytes per stage (one 128B swizzle row)
 constexpr int STAGES = 6;
@@ -269,7 +269,9 @@ __device__ __forceinline__ double scale_pow2(double v, int X) {
     return (v * __longlong_as_double((long long)(X1 + 1023) << 52)) * __longlong_as_double((long long)(X2 + 1023) << 52);
 }
 
-__global__ void __maxnreg__(200)
+// 10 warps land 3-deep on two of the four SM sub-partitions, so the register
+// file allows at most ~168 registers per thread; launch bounds enforce that.
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ SplitGemmParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -404,7 +406,8 @@ __global__ void __maxnreg__(200)
                 tmem_ld_wait();
 #pragma unroll
                 for (int c = 0; c < 32; c++) {
-                    long long x = __float2ll_rn(__uint_as_float(v[c]));
+                    // rounds are sized so |value| <= 2^24: an int32 holds it exactly
+                    long long x = (long long)__float2int_rn(__uint_as_float(v[c]));
                     if (sh >= 0) acc[half * 32 + c] += x << sh;
                     else acc[half * 32 + c] += (x + (1ll << (-sh - 1))) >> (-sh);
                 }
@@ -466,15 +469,20 @@ static int make_slice_map(CUtensorMap* map, const void* base, uint64_t Kp, uint6
     return F4J_OK;
 }
 
-// Slice count from the measured exponent spread (bits): keep F >= 48 + spread
-// fixed-point bits so the truncation error stays below the plain FP64 product's.
-static int slices_for_spread(double spread) {
+// Slice count from the measured exponent spread sigma (bits between a row's
+// largest and its mean element exponent) and the inner dimension k.  The
+// truncation error of an element is 2^-F of its row's 2^e; it must stay below
+// the plain FP64 product's error, which grows with k while the truncation
+// error grows only with sqrt(k):  F >= max(48 + sigma, 54 + sigma - log2 k).
+static int slices_for_spread(double spread, int64_t k) {
     const char* env = getenv("F4J_SPLIT_SLICES");
     if (env && atoi(env) > 0) {
         int s = atoi(env);
         return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
     }
-    double need = 48.0 + (spread > 0 ? spread : 0.0);
+    const double sg = spread > 0 ? spread : 0.0;
+    const double lk = floor(log2((double)(k > 1 ? k : 1)));
+    const double need = fmax(48.0 + sg, 54.0 + sg - lk);
     int s = 1 + (int)ceil((need - 4.0) / 5.0);
     return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
 }
@@ -577,7 +585,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
         return F4J_OK;
     }
     const double spread = (hmisc[1] > hmisc[2] ? hmisc[1] : hmisc[2]) / 256.0;
-    const int s = slices_req > 0 ? (slices_req > S_MAX ? S_MAX : slices_req) : slices_for_spread(spread);
+    const int s = slices_req > 0 ? (slices_req > S_MAX ? S_MAX : slices_req) : slices_for_spread(spread, k);
 
     std::vector<Round> rounds;
     int ubits = 0;
@@ -632,9 +640,21 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
         return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     }
     dim3 grid((unsigned)f4j_cdiv(N, BN), (unsigned)f4j_cdiv(M, BM));
+    f4j_prof_begin(ctx);
     k_split_gemm<<<grid, GEMM_THREADS, smem, ctx->stream>>>(ta, tb, *prm);
+    f4j_prof_end(ctx);
     delete prm;
-    F4J_LAUNCHED(ctx);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, k_split_gemm);
+        return f4j_fail(F4J_ERR_CUDA,
+                        "k_split_gemm launch: %s (regs %d, max threads %d, static smem %zu, local %zu, "
+                        "max dyn smem %d, requested dyn smem %zu, params %zu B)",
+                        cudaGetErrorString(e), fa.numRegs, fa.maxThreadsPerBlock, fa.sharedSizeBytes,
+                        fa.localSizeBytes, fa.maxDynamicSharedSizeBytes, smem, sizeof(SplitGemmParams));
+    }
+    ctx->launches++;
 
     if (rep) {
         rep->slices = s;

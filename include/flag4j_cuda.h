@@ -48,7 +48,8 @@ extern "C" {
 
 #define F4J_MODE_PLAIN 0 /* FP64 DMMA tensor-core GEMM (mma.sync f64)                   */
 #define F4J_MODE_SPLIT 1 /* FP64-accurate split GEMM: FP8 slices on tcgen05, exact FP32 */
-#define F4J_MODE_AUTO 2  /* SPLIT for finite inputs, PLAIN when a NaN/Inf is present    */
+#define F4J_MODE_AUTO 2  /* EXACT for tiny products (<= 2^24 flops); otherwise SPLIT for
+                            finite inputs and PLAIN when a NaN/Inf is present           */
 #define F4J_MODE_EXACT 3 /* Flag4j's own order: k-ascending, no FMA -> bit-identical     */
 
 typedef struct f4j_ctx f4j_ctx;
@@ -81,6 +82,11 @@ int64_t f4j_launch_count(f4j_ctx* ctx);
  * read the elapsed ms between two recorded slots (synchronises the end slot). */
 int f4j_timer_record(f4j_ctx* ctx, int slot);
 int f4j_timer_elapsed(f4j_ctx* ctx, int slot_begin, int slot_end, float* ms);
+/* Opt-in per-kernel timing: with profiling on, the main kernel of each product
+ * (slice GEMM, DMMA GEMM, SpMV, SpMM, ...) is bracketed by CUDA events; read
+ * returns the summed ms and the count since the last read (synchronises). */
+int f4j_set_profiling(f4j_ctx* ctx, int on);
+int f4j_profile_read(f4j_ctx* ctx, double* total_ms, int64_t* count);
 
 /* ---- device buffers ------------------------------------------------------ */
 int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out);

@@ -5,6 +5,7 @@ SPLIT (FP8 slices on tcgen05) satisfy |C - C_ref| <= 2 k u |A||B|
 (u = 2^-53, k = inner dimension), componentwise.
 """
 import ctypes
+import math
 
 import numpy as np
 import pytest
@@ -75,16 +76,47 @@ def test_exact_mode_reproduces_golden_vectors(f4j, golden):
         assert np.array_equal(C.data, cplx(v["exp"]).ravel()), c["line"]
 
 
+def split_normwise_tol(A, B, F):
+    """Documented bound of the split product with F fixed-point bits per element:
+    |C - C_true| <= 2^-F (2^e_i |b_j|_1 + 2^f_j |a_i|_1 + 8 k 2^(e_i + f_j)),
+    2^e_i > max|a_i.|, 2^f_j > max|b_.j| (real operands; complex via the
+    [Re | Im] concatenation)."""
+    if np.iscomplexobj(A):
+        Ac = np.hstack([A.real, A.imag])
+        Bc = np.vstack([np.hstack([B.real, B.imag]), np.hstack([-B.imag, B.real])])
+        t = split_normwise_tol(Ac, Bc, F)
+        n = B.shape[1]
+        return t[:, :n] + 1j * t[:, n:]
+    k = A.shape[1]
+    ra = np.abs(A).max(axis=1)
+    cb = np.abs(B).max(axis=0)
+    ea = np.where(ra > 0, np.floor(np.log2(np.where(ra > 0, ra, 1))) + 1, 0)
+    fb = np.where(cb > 0, np.floor(np.log2(np.where(cb > 0, cb, 1))) + 1, 0)
+    Ea, Fb = np.ldexp(1.0, ea.astype(int))[:, None], np.ldexp(1.0, fb.astype(int))[None, :]
+    return np.ldexp(Ea * np.abs(B).sum(axis=0)[None, :] + Fb * np.abs(A).sum(axis=1)[:, None]
+                    + 8.0 * k * Ea * Fb, -F)
+
+
 @pytest.mark.parametrize("mode", ["plain", "split", "auto"])
 def test_fast_modes_on_golden_vectors(f4j, golden, oracle, mode):
-    for c in golden["real_kernels"]:
-        A, B = np.array(c["vars"]["entriesA"]), np.array(c["vars"]["entriesB"])
-        C = f4j.Matrix(A).mult(f4j.Matrix(B), mode=mode).toNumpy()
-        check_bound(C, *ref_bound(oracle, A, B, False), A.shape[1], "%s line %d" % (mode, c["line"]))
-    for c in golden["complex_kernels"]:
-        A, B = cplx(c["vars"]["entriesA"]), cplx(c["vars"]["entriesB"])
-        C = f4j.CMatrix(A).mult(f4j.CMatrix(B), mode=mode).toNumpy()
-        check_bound(C, *ref_bound(oracle, A, B, True), A.shape[1], "%s line %d" % (mode, c["line"]))
+    for cp, key in ((False, "real_kernels"), (True, "complex_kernels")):
+        for c in golden[key]:
+            conv = cplx if cp else np.array
+            A, B = conv(c["vars"]["entriesA"]), conv(c["vars"]["entriesB"])
+            rep = {}
+            M = f4j.CMatrix if cp else f4j.Matrix
+            C = M(A).mult(M(B), mode=mode, report=rep).toNumpy()
+            ref, ab = ref_bound(oracle, A, B, cp)
+            if mode == "split":
+                # k = 3 with 20-bit spreads: the split keeps its normwise bound
+                tol = split_normwise_tol(A, B, rep["frac_bits"])
+                assert np.all(np.abs((C - ref).real) <= tol.real + 2 * A.shape[1] * U * ab.real), c["line"]
+                if cp:
+                    assert np.all(np.abs((C - ref).imag) <= tol.imag + 2 * A.shape[1] * U * ab.imag), c["line"]
+            else:
+                check_bound(C, ref, ab, A.shape[1], "%s line %d" % (mode, c["line"]))
+            if mode == "auto":
+                assert rep["mode_used"] == 3 and np.array_equal(C, ref)  # tiny: Flag4j's own order
 
 
 def test_api_golden_and_shape_errors(f4j, golden):
@@ -225,13 +257,16 @@ def test_split_with_wide_spread_picks_more_slices(f4j, oracle):
 
 
 def test_auto_mode_routes_nonfinite_to_dmma(f4j):
-    A = np.ones((16, 16))
+    A = np.ones((256, 256))
     A[3, 4] = np.nan
     A[5, 5] = np.inf
-    B = np.ones((16, 16))
+    B = np.ones((256, 256))
     C, rep = run_gemm(f4j, A, B, mode="auto")
     assert rep.mode_used == 0
-    assert np.isnan(C[3]).all() and not np.isnan(C[0]).any()
+    assert np.isnan(C[3]).all() and np.isinf(C[5]).all() and not np.isnan(C[0]).any()
+    # tiny products run Flag4j's own order under AUTO
+    _, rep2 = run_gemm(f4j, np.ones((16, 16)), np.ones((16, 16)), mode="auto")
+    assert rep2.mode_used == 3
 
 
 def test_gemm_check_agrees_with_oracle(f4j, oracle):
@@ -292,19 +327,23 @@ def test_dense_adjoint_finite_differences(f4j, mode):
     rng = np.random.default_rng(9)
     h = 1e-6
 
-    def loss(Am, Bm):
-        return float(np.sum(W * f4j.Matrix(Am).mult(f4j.Matrix(Bm), mode=mode).toNumpy()))
+    def prod(Am, Bm):
+        return f4j.Matrix(Am).mult(f4j.Matrix(Bm), mode=mode).toNumpy()
+
+    def central(Cp, Cm):
+        # (L(+h) - L(-h)) / 2h, difference taken before the (exact) sum
+        return math.fsum((W * (Cp - Cm)).ravel()) / (2 * h)
 
     for _ in range(32):
         i, j = rng.integers(0, m), rng.integers(0, k)
         Ap, Am_ = A.copy(), A.copy()
         Ap[i, j] += h
         Am_[i, j] -= h
-        fd = (loss(Ap, B) - loss(Am_, B)) / (2 * h)
+        fd = central(prod(Ap, B), prod(Am_, B))
         assert abs(fd - dA[i, j]) <= 1e-7 * max(1.0, abs(dA[i, j]))
         i, j = rng.integers(0, k), rng.integers(0, n)
         Bp, Bm_ = B.copy(), B.copy()
         Bp[i, j] += h
         Bm_[i, j] -= h
-        fd = (loss(A, Bp) - loss(A, Bm_)) / (2 * h)
+        fd = central(prod(A, Bp), prod(A, Bm_))
         assert abs(fd - dB[i, j]) <= 1e-7 * max(1.0, abs(dB[i, j]))

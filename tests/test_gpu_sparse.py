@@ -2,6 +2,7 @@
 restatement of Flag4j's loops (RealCsrDenseMatMult, CooMatrix.toCsr,
 CooDataSorter, RealCsrOps.transpose); SDDMM within 2 k u sum|a||b|."""
 import ctypes
+import math
 
 import numpy as np
 import pytest
@@ -162,21 +163,26 @@ def test_sparse_adjoint_finite_differences(f4j):
     rng = np.random.default_rng(3)
     h = 1e-6
 
-    def loss(vals, Xm):
-        return float(np.sum(W * f4j.CsrMatrix((rows, cols), vals, rp, ci).mult(f4j.Matrix(Xm)).toNumpy()))
+    def prod(vals, Xm):
+        return f4j.CsrMatrix((rows, cols), vals, rp, ci).mult(f4j.Matrix(Xm)).toNumpy()
 
-    for _ in range(16):
+    def central(Cp, Cm):
+        # (L(+h) - L(-h)) / 2h with the difference taken before the sum, which
+        # keeps the summation's rounding out of the quotient
+        return math.fsum((W * (Cp - Cm)).ravel()) / (2 * h)
+
+    for _ in range(32):
         q = rng.integers(0, len(v))
         vp, vm = v.copy(), v.copy()
         vp[q] += h
         vm[q] -= h
-        fd = (loss(vp, X) - loss(vm, X)) / (2 * h)
+        fd = central(prod(vp, X), prod(vm, X))
         assert abs(fd - dS[q]) <= 1e-7 * max(1.0, abs(dS[q]))
         i, j = rng.integers(0, cols), rng.integers(0, nc)
         Xp, Xm_ = X.copy(), X.copy()
         Xp[i, j] += h
         Xm_[i, j] -= h
-        fd = (loss(v, Xp) - loss(v, Xm_)) / (2 * h)
+        fd = central(prod(v, Xp), prod(v, Xm_))
         assert abs(fd - dX[i, j]) <= 1e-7 * max(1.0, abs(dX[i, j]))
 
 
