@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, the smoke check and the benchmark's
 CPU-baseline leg as the checker.  The product library never imports this.
 
-``build()`` compiles f4j_oracle.c with gcc -O2 -ffp-contract=off so every
+``build()`` compiles f4j_oracle.c with gcc -O3 -ffp-contract=off so every
 product and sum rounds separately, as the JVM does.
 """
 import ctypes
@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "f4j_oracle.c")
 LIB = os.path.join(HERE, "libf4j_oracle.so")
-CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread", "-std=c11"]
+CFLAGS = ["-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread", "-std=c11"]
 
 _lock = threading.Lock()
 _lib = None
