@@ -69,6 +69,7 @@ SIGNATURES = {
     "f4j_dgemm_adjoint": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _v, _v, _i, _rep]),
     "f4j_zgemm_adjoint": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _v, _v, _i, _rep]),
     "f4j_gemm_check": (_i, [_v, _i, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i64, _u64, _pd, _pd]),
+    "f4j_dgemm_split_noalloc": (_i, [_i64, _i64, _i64, _v, _i, _v, _i, _v, _v, ctypes.POINTER(ctypes.c_int32)]),
     "f4j_csr_wrap": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _i, _pv]),
     "f4j_csr_from_coo": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _pv]),
     "f4j_coo_sort": (_i, [_v, _i64, _v, _v, _v]),

@@ -22,6 +22,7 @@
 // so one real product of size m x 2n x 2k gives [Cr | Ci] (the four real
 // products of Complex128.mult, src/main/java/org/flag4j/numbers/Complex128.java:336-341).
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "f4j_internal.cuh"
@@ -661,5 +662,141 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
         rep->frac_bits = 4 + 5 * (s - 1);
         rep->exp_spread = spread;
     }
+    return F4J_OK;
+}
+
+// ------------------------------------------------------------------ no-allocation variant
+// Some callers cannot allocate device memory: code running inside a CUDA graph
+// being captured or replayed, engines that hand out a fixed memory pool and
+// forbid cudaMalloc after start-up, and JVM or other runtime hosts that only
+// pass in buffers they already own.  f4j_dgemm_split_noalloc serves them: it
+// runs the same split GEMM as f4j_dgemm(..., F4J_MODE_SPLIT, ...) but takes
+// its scratch (exponent statistics and the FP8 slice planes) from the
+// file-scope array below, so it calls no allocator at all.
+//
+// The array holds F4J_NOALLOC_SCRATCH_BYTES on every GPU that loads this
+// library, until the process exits.  It is shared by every call on a device and
+// keeps the last call's contents; each call clears what must start at zero.
+// Calls whose GPU work overlaps (e.g. on two streams) race on it.
+#define F4J_NOALLOC_SCRATCH_BYTES (32u << 20)
+static __device__ __align__(256) unsigned char g_f4j_noalloc_scratch[F4J_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[256];  // device address of the array, per device
+
+// Device address of the scratch array on the current device; the first call
+// on a device looks it up (cudaGetSymbolAddress) with that device current.
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    F4J_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return f4j_fail(F4J_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_f4j_noalloc_scratch);
+        if (e != cudaSuccess || !p) return f4j_cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return F4J_OK;
+}
+
+extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
+                                       int opB, double* C, void* stream, int32_t* slices_out) {
+    if (slices_out) *slices_out = 0;
+    if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null matrix pointer");
+    if (m < 0 || n < 0 || k < 0) return f4j_fail(F4J_ERR_ARG, "negative dimension");
+    if (opA == F4J_OP_C) opA = F4J_OP_T;
+    if (opB == F4J_OP_C) opB = F4J_OP_T;
+    if (opA < 0 || opA > F4J_OP_T || opB < 0 || opB > F4J_OP_T) return f4j_fail(F4J_ERR_ARG, "bad op");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (m == 0 || n == 0) return F4J_OK;
+    if (k == 0) {
+        F4J_CUDA(cudaMemsetAsync(C, 0, (size_t)m * n * 8, st));
+        return F4J_OK;
+    }
+    auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+    const int64_t M = m, N = n;
+    const int64_t Kp = f4j_cdiv(k, BKB) * BKB;
+    const size_t off_mxa = 0, off_esa = off_mxa + al(M * 8), off_cna = off_esa + al(M * 8);
+    const size_t off_mxb = off_cna + al(M * 4), off_esb = off_mxb + al(N * 8), off_cnb = off_esb + al(N * 8);
+    const size_t off_ea = off_cnb + al(N * 4), off_eb = off_ea + al(M * 4);
+    const size_t off_misc = off_eb + al(N * 4);
+    const size_t off_sl = off_misc + 1024;
+    // worst case over the slice counts this function may pick
+    const size_t need = off_sl + al((size_t)M * Kp * S_MAX) + al((size_t)N * Kp * S_MAX);
+    if (need > F4J_NOALLOC_SCRATCH_BYTES)
+        return f4j_fail(F4J_ERR_ARG,
+                        "f4j_dgemm_split_noalloc: m=%lld n=%lld k=%lld needs %zu bytes of scratch, more than the "
+                        "%u-byte static limit ((m+n)*roundup(k,128)*12 + small); use f4j_dgemm",
+                        (long long)m, (long long)n, (long long)k, need, F4J_NOALLOC_SCRATCH_BYTES);
+    void* base;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    char* w = (char*)base;
+    unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
+    long long* esa = (long long*)(w + off_esa);
+    int* cna = (int*)(w + off_cna);
+    unsigned long long* mxb = (unsigned long long*)(w + off_mxb);
+    long long* esb = (long long*)(w + off_esb);
+    int* cnb = (int*)(w + off_cnb);
+    int* ea = (int*)(w + off_ea);
+    int* eb = (int*)(w + off_eb);
+    int* misc = (int*)(w + off_misc);  // [0] non-finite, [1..2] spreads, [8] wait status
+    // statistics accumulate with atomics and the status word must read 0
+    F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, st));
+    F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, st));
+
+    const bool a_rows = (opA == F4J_OP_N), b_rows = (opB != F4J_OP_N);
+    if (a_rows) k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, st>>>(A, M, k, 0, mxa, esa, cna, misc);
+    else k_stats_cols<<<dim3((unsigned)f4j_cdiv(M, 256), (unsigned)f4j_cdiv(k, 256)), 256, 0, st>>>(A, k, M, 0, mxa,
+                                                                                                 esa, cna, misc);
+    if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(N, 8), 256, 0, st>>>(B, N, k, 0, mxb, esb, cnb, misc);
+    else k_stats_cols<<<dim3((unsigned)f4j_cdiv(N, 256), (unsigned)f4j_cdiv(k, 256)), 256, 0, st>>>(B, k, N, 0, mxb,
+                                                                                                 esb, cnb, misc);
+    k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
+    k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
+    F4J_CUDA(cudaGetLastError());
+    int hmisc[3];
+    F4J_CUDA(cudaMemcpyAsync(hmisc, misc, sizeof hmisc, cudaMemcpyDeviceToHost, st));
+    F4J_CUDA(cudaStreamSynchronize(st));
+    if (hmisc[0])
+        return f4j_fail(F4J_ERR_ARG, "f4j_dgemm_split_noalloc: NaN or Inf in an operand; use f4j_dgemm (AUTO)");
+    const double spread = (hmisc[1] > hmisc[2] ? hmisc[1] : hmisc[2]) / 256.0;
+    const int s = slices_for_spread(spread, k);
+    std::vector<Round> rounds;
+    int ubits = 0;
+    rc = build_rounds(s, Kp, k, rounds, ubits);
+    if (rc) return rc;
+    uint8_t* slA = (uint8_t*)(w + off_sl);
+    uint8_t* slB = slA + al((size_t)M * Kp * s);
+    k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
+        A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, 0, M, k, Kp, Kp, M, ea, s, slA);
+    k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(N, SP_TR)), 256, 0, st>>>(
+        B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 0, 1, N, k, Kp, Kp, N, eb, s, slB);
+    F4J_CUDA(cudaGetLastError());
+    CUtensorMap ta{}, tb{};
+    rc = make_slice_map(&ta, slA, Kp, M, s);
+    if (rc) return rc;
+    rc = make_slice_map(&tb, slB, Kp, N, s);
+    if (rc) return rc;
+    SplitGemmParams prm{};
+    prm.M = (int)M;
+    prm.N = (int)N;
+    prm.Kp = (int)Kp;
+    prm.nrounds = (int)rounds.size();
+    prm.cplx = 0;
+    prm.n_out = (int)N;
+    prm.ubits = ubits;
+    prm.ea = ea;
+    prm.eb = eb;
+    prm.C = C;
+    prm.status = misc + 8;
+    for (size_t i = 0; i < rounds.size(); i++) prm.rounds[i] = rounds[i];
+    const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
+    F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_split_gemm<<<dim3((unsigned)f4j_cdiv(N, BN), (unsigned)f4j_cdiv(M, BM)), GEMM_THREADS, smem, st>>>(ta, tb, prm);
+    F4J_CUDA(cudaGetLastError());
+    if (slices_out) *slices_out = s;
     return F4J_OK;
 }

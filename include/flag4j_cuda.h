@@ -135,6 +135,23 @@ int f4j_dgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, 
 int f4j_zgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, f4j_buf B,
                       f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode, f4j_report* report);
 
+/* No-allocation variant of the split GEMM (no counterpart in the reference).
+ * For callers that may not allocate device memory: work captured into or
+ * replayed from a CUDA graph, engines that own a fixed memory pool, and JVM or
+ * other hosts that only pass in buffers they already hold.  Same arithmetic as
+ * f4j_dgemm(..., F4J_MODE_SPLIT, ...) on real float64; A, B and C are the
+ * caller's device pointers, `stream` a cudaStream_t (NULL = default stream).
+ * Scratch comes from a static 32 MiB device array inside the library (held on
+ * every GPU that loads it until exit), so sizes with
+ *   (m + n) * roundup(k, 128) * 12 + 64 * (m + n) + 4096 > 32 MiB
+ * are rejected with F4J_ERR_ARG; NaN/Inf operands are rejected too.  The first
+ * call on a device looks up the array's address, so make that call before
+ * any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps race.  Calls no cudaMalloc/cudaFree.  `slices_out` (may be NULL)
+ * receives the slice count used. */
+int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
+                            int opB, double* C, void* stream, int32_t* slices_out);
+
 /* Sampled accuracy check of a computed C = op(A) op(B): evaluates `samples`
  * seeded entries in double-double (compensated Dot2) on the GPU and returns
  * max |C - C_true| and max |C - C_true| / sum|a||b| over the samples. */
