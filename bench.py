@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--case", default="full", choices=["full", "small"])
     p.add_argument("--skip-extras", action="store_true", help="headline GEMM only (for profiling)")
+    p.add_argument("--only-sparse", action="store_true", help="CSR products only (for profiling)")
     return p.parse_args()
 
 
@@ -159,15 +160,19 @@ class Eng:
                                            C.handle, samples, seed, ctypes.byref(ea), ctypes.byref(er)))
         return ea.value, er.value
 
-    def kernel_ms(self, fn, steps):
-        """Average CUDA-event time of the main product kernel inside fn()."""
+    def kernel_ms(self, fn, steps, with_prep=False):
+        """Average CUDA-event time per call of the main product kernel inside
+        fn() (and of the preparation kernels when with_prep)."""
         self.check(self.lib.f4j_set_profiling(self.ctx.handle, 1))
         for _ in range(steps):
             fn()
-        tot, cnt = ctypes.c_double(), ctypes.c_int64()
-        self.check(self.lib.f4j_profile_read(self.ctx.handle, ctypes.byref(tot), ctypes.byref(cnt)))
+        out = []
+        for tag in (0, 1):
+            tot, cnt = ctypes.c_double(), ctypes.c_int64()
+            self.check(self.lib.f4j_profile_read(self.ctx.handle, tag, ctypes.byref(tot), ctypes.byref(cnt)))
+            out.append(tot.value / steps)
         self.check(self.lib.f4j_set_profiling(self.ctx.handle, 0))
-        return tot.value / max(cnt.value, 1)
+        return tuple(out) if with_prep else out[0]
 
     def timed(self, fn, steps, warmup):
         """Average ms per call with CUDA events on the context stream."""
@@ -310,6 +315,42 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- sparse products
+def sparse_section(E, full, steps=20):
+    """CSR SpMV / SpMM (32 columns) at 2^20 rows, Poisson(16) row lengths."""
+    from flag4j_gb300 import synth
+    rows = (1 << 20) if full else (1 << 16)
+    rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
+    nnz = len(v)
+    S = E.f.CsrMatrix((rows, rows), v, rp, ci)
+    hS = S.handle(E.ctx)
+    x = E.dev(synth.normal(rows, 1, 5).ravel())
+    y = E.ctx.alloc(8 * rows)
+    X = E.dev(synth.normal(rows, 32, 6))
+    Y = E.ctx.alloc(8 * rows * 32)
+    t_spmv = E.timed(lambda: E.check(E.lib.f4j_spmv(E.ctx.handle, hS, x.handle, y.handle, None)), steps, 3)
+    t_spmm = E.timed(lambda: E.check(E.lib.f4j_spmm(E.ctx.handle, hS, X.handle, 32, Y.handle, None)), steps, 3)
+    b_spmv = 12.0 * nnz + 4.0 * (rows + 1) + 16.0 * rows
+    b_spmm = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 32 * rows
+    b_spmm_g = 12.0 * nnz + 8.0 * 32 * nnz + 8.0 * 32 * rows
+    hbm, hbm_src = measured_peaks()
+    res = {"rows": rows, "nnz": nnz, "spmm_ms": t_spmm, "spmm_gbs_compulsory": b_spmm / t_spmm / 1e6,
+           "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm / 1e6,
+           "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
+           "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
+           "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True}
+    del x, y, X, Y, S
+    return res
+
+
+def run_sparse_only(args):
+    """Profiling helper: the CSR products alone (prints their numbers, not the contract line)."""
+    from flag4j_gb300 import build
+    build.build()
+    E = Eng(dist_env()[2])
+    print(json.dumps(sparse_section(E, args.case == "full", steps=args.steps)))
+
+
 # ---------------------------------------------------------------- our arm
 def run_ours(args):
     ws, rank, local = dist_env()
@@ -411,33 +452,14 @@ def run_ours(args):
         fb = E.timed(step, 3, 1)
         out["adjoint"] = {"shape": [ma, ka, ma], "forward_ms": fwd, "fwd_bwd_ms": fb, "ratio": fb / fwd}
         del Aa, Ba, Wa, Ca, dA, dB
-        # ---- CSR SpMV / SpMM at 2^20 rows
-        rows = (1 << 20) if full else (1 << 16)
-        rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
-        nnz = len(v)
-        S = E.f.CsrMatrix((rows, rows), v, rp, ci)
-        hS = S.handle(E.ctx)
-        x = E.dev(synth.normal(rows, 1, 5).ravel())
-        y = E.ctx.alloc(8 * rows)
-        X = E.dev(synth.normal(rows, 32, 6))
-        Y = E.ctx.alloc(8 * rows * 32)
-        t_spmv = E.timed(lambda: E.check(E.lib.f4j_spmv(E.ctx.handle, hS, x.handle, y.handle, None)), 20, 3)
-        t_spmm = E.timed(lambda: E.check(E.lib.f4j_spmm(E.ctx.handle, hS, X.handle, 32, Y.handle, None)), 20, 3)
-        b_spmv = 12.0 * nnz + 4.0 * (rows + 1) + 16.0 * rows
-        b_spmm = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 32 * rows
-        b_spmm_g = 12.0 * nnz + 8.0 * 32 * nnz + 8.0 * 32 * rows
-        hbm, hbm_src = measured_peaks()
-        out["spmm"] = {"rows": rows, "nnz": nnz, "spmm_ms": t_spmm, "spmm_gbs_compulsory": b_spmm / t_spmm / 1e6,
-                       "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm / 1e6,
-                       "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
-                       "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
-                       "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True}
-        del x, y, X, Y, S
+        out["spmm"] = sparse_section(E, full)
 
     # ---- roofline of the dominant kernel (the tcgen05 slice GEMM), timed alone
     # with CUDA events around its launch on the context stream
     A, B = E.dev(A_h), E.dev(B_h)
-    kms = E.kernel_ms(lambda: E.gemm(A, B, C, n, n, n, L.MODE_SPLIT), max(3, args.steps // 2))
+    kms, prep_ms = E.kernel_ms(lambda: E.gemm(A, B, C, n, n, n, L.MODE_SPLIT), max(3, args.steps // 2), True)
+    out["split"]["prep_kernels_ms"] = prep_ms
+    out["split"]["gemm_kernel_ms"] = kms
     del A, B
     fp8_peak, fp8_src = fp8_peak_tflops() if not args.skip_extras else (2 * 1927.7, "2 x measured bf16")
     achieved = fp8_flops / (kms * 1e-3) / 1e12
@@ -497,6 +519,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_sparse:
+        run_sparse_only(args)
     else:
         run_ours(args)
 

@@ -52,7 +52,8 @@ SIGNATURES = {
     "f4j_timer_record": (_i, [_v, _i]),
     "f4j_timer_elapsed": (_i, [_v, _i, _i, _pf]),
     "f4j_set_profiling": (_i, [_v, _i]),
-    "f4j_profile_read": (_i, [_v, _pd, _pi64]),
+    "f4j_profile_read": (_i, [_v, _i, _pd, _pi64]),
+    "f4j_profile_reset": (_i, [_v]),
     "f4j_buf_alloc": (_i, [_v, _sz, _pv]),
     "f4j_buf_free": (_i, [_v, _v]),
     "f4j_buf_size": (_sz, [_v]),

@@ -87,7 +87,7 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
     for (int i = 0; i < 16; i++)
         if (ctx->ev_init[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->prof_init)
-        for (int i = 0; i < 512; i++) cudaEventDestroy(ctx->prof_ev[i]);
+        for (int i = 0; i < 1024; i++) cudaEventDestroy(ctx->prof_ev[i]);
     for (int i = 0; i < 4; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
     if (ctx->d_status) cudaFree(ctx->d_status);
@@ -143,13 +143,14 @@ extern "C" int f4j_timer_elapsed(f4j_ctx* ctx, int a, int b, float* ms) {
     return F4J_OK;
 }
 
-void f4j_prof_begin(f4j_ctx* ctx) {
-    if (!ctx->prof || ctx->prof_n >= 256) return;
+void f4j_prof_begin(f4j_ctx* ctx, int tag) {
+    if (!ctx->prof || ctx->prof_n >= 512) return;
+    ctx->prof_tag[ctx->prof_n] = tag;
     cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n], ctx->stream);
 }
 
 void f4j_prof_end(f4j_ctx* ctx) {
-    if (!ctx->prof || ctx->prof_n >= 256) return;
+    if (!ctx->prof || ctx->prof_n >= 512) return;
     cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n + 1], ctx->stream);
     ctx->prof_n++;
 }
@@ -157,7 +158,7 @@ void f4j_prof_end(f4j_ctx* ctx) {
 extern "C" int f4j_set_profiling(f4j_ctx* ctx, int on) {
     F4J_CHECK_CTX(ctx);
     if (on && !ctx->prof_init) {
-        for (int i = 0; i < 512; i++) F4J_CUDA(cudaEventCreate(&ctx->prof_ev[i]));
+        for (int i = 0; i < 1024; i++) F4J_CUDA(cudaEventCreate(&ctx->prof_ev[i]));
         ctx->prof_init = true;
     }
     ctx->prof = on != 0;
@@ -165,18 +166,27 @@ extern "C" int f4j_set_profiling(f4j_ctx* ctx, int on) {
     return F4J_OK;
 }
 
-extern "C" int f4j_profile_read(f4j_ctx* ctx, double* total_ms, int64_t* count) {
+extern "C" int f4j_profile_read(f4j_ctx* ctx, int tag, double* total_ms, int64_t* count) {
     F4J_CHECK_CTX(ctx);
     if (!total_ms || !count) return f4j_fail(F4J_ERR_ARG, "null output");
     double t = 0;
+    int64_t c = 0;
     for (int i = 0; i < ctx->prof_n; i++) {
+        if (tag >= 0 && ctx->prof_tag[i] != tag) continue;
         float ms = 0;
         F4J_CUDA(cudaEventSynchronize(ctx->prof_ev[2 * i + 1]));
         F4J_CUDA(cudaEventElapsedTime(&ms, ctx->prof_ev[2 * i], ctx->prof_ev[2 * i + 1]));
         t += ms;
+        c++;
     }
     *total_ms = t;
-    *count = ctx->prof_n;
+    *count = c;
+    return F4J_OK;
+}
+
+extern "C" int f4j_profile_reset(f4j_ctx* ctx) {
+    F4J_CHECK_CTX(ctx);
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->prof_n = 0;
     return F4J_OK;
 }

@@ -39,16 +39,20 @@ struct f4j_ctx {
     cudaEvent_t ev[16];
     bool ev_init[16];
     int64_t launches;
-    // Opt-in profiling: CUDA events around each main product kernel.
+    // Opt-in profiling: CUDA events around product kernels, tagged
+    // F4J_PROF_MAIN (the product kernel) or F4J_PROF_PREP (statistics,
+    // slicing, structure preparation).
     bool prof;
     int prof_n;
-    cudaEvent_t prof_ev[2 * 256];
+    cudaEvent_t prof_ev[2 * 512];
+    int prof_tag[512];
     bool prof_init;
 };
 
-// Bracket the main kernel of a product with profiling events (no-ops unless
-// profiling is on).
-void f4j_prof_begin(f4j_ctx* ctx);
+enum { F4J_PROF_MAIN = 0, F4J_PROF_PREP = 1 };
+
+// Bracket a kernel with profiling events (no-ops unless profiling is on).
+void f4j_prof_begin(f4j_ctx* ctx, int tag = F4J_PROF_MAIN);
 void f4j_prof_end(f4j_ctx* ctx);
 
 // ---------------------------------------------------------------- errors

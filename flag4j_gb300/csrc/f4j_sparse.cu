@@ -16,39 +16,50 @@
 namespace {
 
 // ------------------------------------------------------------------ SpMV
-// Thread per row (bit-exact sequential sum); each warp stages its rows'
-// nonzeros through shared memory in coalesced chunks.
-constexpr int SPMV_WARPS = 8, SPMV_CHUNK = 128;
+// Each warp owns 32 consecutive rows.  It walks their nonzeros in chunks of
+// SPMV_CHUNK: lanes gather x[col] and form the rounded products v * x[col]
+// cooperatively (coalesced index/value loads, SPMV_CHUNK/32 independent
+// gathers in flight per lane) into shared memory; then each lane adds its own
+// row's products in storage order.  Products and sums round exactly as
+// RealCsrDenseMatMult.standardVector does, so y is bit-identical.
+constexpr int SPMV_WARPS = 8, SPMV_CHUNK = 256;
 
 __global__ void __launch_bounds__(SPMV_WARPS * 32)
     k_spmv(int64_t rows, const int* __restrict__ rowptr, const int* __restrict__ colidx,
            const double* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
-    __shared__ int scol[SPMV_WARPS][SPMV_CHUNK];
-    __shared__ double sval[SPMV_WARPS][SPMV_CHUNK];
+    __shared__ double sprod[SPMV_WARPS][SPMV_CHUNK];
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int64_t wrow0 = ((int64_t)blockIdx.x * SPMV_WARPS + warp) * 32;
     if (wrow0 >= rows) return;
     const int64_t row = wrow0 + lane;
     const int64_t wrow1 = wrow0 + 32 < rows ? wrow0 + 32 : rows;
-    const int p0 = rowptr[wrow0], p1 = rowptr[wrow1];
+    const int p0 = __ldg(&rowptr[wrow0]), p1 = __ldg(&rowptr[wrow1]);
     int q = 0, qend = 0;
     if (row < rows) {
-        q = rowptr[row];
-        qend = rowptr[row + 1];
+        q = __ldg(&rowptr[row]);
+        qend = __ldg(&rowptr[row + 1]);
     }
     double acc = 0.0;
     for (int c0 = p0; c0 < p1; c0 += SPMV_CHUNK) {
         const int cn = (p1 - c0) < SPMV_CHUNK ? (p1 - c0) : SPMV_CHUNK;
-        for (int e = lane; e < cn; e += 32) {
-            scol[warp][e] = colidx[c0 + e];
-            sval[warp][e] = vals[c0 + e];
+        if (cn == SPMV_CHUNK) {
+            int c[SPMV_CHUNK / 32];
+            double v[SPMV_CHUNK / 32], xv[SPMV_CHUNK / 32];
+#pragma unroll
+            for (int u = 0; u < SPMV_CHUNK / 32; u++) {
+                c[u] = __ldg(&colidx[c0 + lane + 32 * u]);
+                v[u] = __ldg(&vals[c0 + lane + 32 * u]);
+            }
+#pragma unroll
+            for (int u = 0; u < SPMV_CHUNK / 32; u++) xv[u] = __ldg(&x[c[u]]);
+#pragma unroll
+            for (int u = 0; u < SPMV_CHUNK / 32; u++) sprod[warp][lane + 32 * u] = __dmul_rn(v[u], xv[u]);
+        } else {
+            for (int e = lane; e < cn; e += 32) sprod[warp][e] = __dmul_rn(__ldg(&vals[c0 + e]), __ldg(&x[__ldg(&colidx[c0 + e])]));
         }
         __syncwarp();
         const int stop = qend < c0 + cn ? qend : c0 + cn;
-        for (; q < stop; q++) {
-            const int e = q - c0;
-            acc = __dadd_rn(acc, __dmul_rn(sval[warp][e], __ldg(&x[scol[warp][e]])));
-        }
+        for (; q < stop; q++) acc = __dadd_rn(acc, sprod[warp][q - c0]);
         __syncwarp();
     }
     if (row < rows) y[row] = acc;
@@ -73,29 +84,30 @@ __global__ void __launch_bounds__(256)
     for (int64_t cbase = (int64_t)lane * W; cbase < ncols; cbase += (int64_t)G * W) {
         double a0 = 0.0, a1 = 0.0;
         int q = q0;
-        for (; q + 4 <= q1; q += 4) {
-            int c[4];
-            double v[4];
+        constexpr int UN = 8;  // nonzeros whose X rows are in flight together
+        for (; q + UN <= q1; q += UN) {
+            int c[UN];
+            double v[UN];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < UN; u++) {
                 c[u] = __ldg(&colidx[q + u]);
                 v[u] = PERM ? __ldg(&vals[__ldg(&perm[q + u])]) : __ldg(&vals[q + u]);
             }
             if (VEC2) {
-                double2 xv[4];
+                double2 xv[UN];
 #pragma unroll
-                for (int u = 0; u < 4; u++) xv[u] = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c[u] * ncols + cbase));
+                for (int u = 0; u < UN; u++) xv[u] = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c[u] * ncols + cbase));
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
+                for (int u = 0; u < UN; u++) {
                     a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u].x));
                     a1 = __dadd_rn(a1, __dmul_rn(v[u], xv[u].y));
                 }
             } else {
-                double xv[4];
+                double xv[UN];
 #pragma unroll
-                for (int u = 0; u < 4; u++) xv[u] = __ldg(X + (int64_t)c[u] * ncols + cbase);
+                for (int u = 0; u < UN; u++) xv[u] = __ldg(X + (int64_t)c[u] * ncols + cbase);
 #pragma unroll
-                for (int u = 0; u < 4; u++) a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u]));
+                for (int u = 0; u < UN; u++) a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u]));
             }
         }
         for (; q < q1; q++) {

@@ -558,6 +558,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     int* misc = (int*)(w + off_misc);  // [0] non-finite seen, [1] spread A x256, [2] spread B x256
 
     const bool a_rows = (opA == F4J_OP_N);  // targets of A (rows of op(A)) are stored rows
+    f4j_prof_begin(ctx, F4J_PROF_PREP);
     if (a_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
     } else {
@@ -578,6 +579,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
+    f4j_prof_end(ctx);
     int hmisc[3];
     F4J_CUDA(cudaMemcpyAsync(hmisc, misc, sizeof hmisc, cudaMemcpyDeviceToHost, ctx->stream));
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -601,6 +603,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     uint8_t* slA = (uint8_t*)ws0;
     uint8_t* slB = slA + al(plane_a * s);
 
+    f4j_prof_begin(ctx, F4J_PROF_PREP);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
         k_split<<<g, 256, 0, ctx->stream>>>(A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, cplx,
@@ -613,6 +616,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
                                             opB == F4J_OP_C, 1, n, k, Kh, Kp, N, eb, s, slB);
         F4J_LAUNCHED(ctx);
     }
+    f4j_prof_end(ctx);
 
     CUtensorMap ta{}, tb{};
     rc = make_slice_map(&ta, slA, Kp, M, s);

@@ -82,11 +82,14 @@ int64_t f4j_launch_count(f4j_ctx* ctx);
  * read the elapsed ms between two recorded slots (synchronises the end slot). */
 int f4j_timer_record(f4j_ctx* ctx, int slot);
 int f4j_timer_elapsed(f4j_ctx* ctx, int slot_begin, int slot_end, float* ms);
-/* Opt-in per-kernel timing: with profiling on, the main kernel of each product
- * (slice GEMM, DMMA GEMM, SpMV, SpMM, ...) is bracketed by CUDA events; read
- * returns the summed ms and the count since the last read (synchronises). */
+/* Opt-in per-kernel timing: with profiling on, kernels are bracketed by CUDA
+ * events tagged 0 (the product kernel: slice GEMM, DMMA GEMM, SpMV, SpMM, ...)
+ * or 1 (preparation: exponent statistics, slicing, structure).  read returns
+ * the summed ms and count for one tag (-1: all) since the last reset
+ * (synchronises); set_profiling and reset clear the record. */
 int f4j_set_profiling(f4j_ctx* ctx, int on);
-int f4j_profile_read(f4j_ctx* ctx, double* total_ms, int64_t* count);
+int f4j_profile_read(f4j_ctx* ctx, int tag, double* total_ms, int64_t* count);
+int f4j_profile_reset(f4j_ctx* ctx);
 
 /* ---- device buffers ------------------------------------------------------ */
 int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out);
