@@ -148,10 +148,12 @@ class Eng:
     def dev(self, arr):
         return self.ctx.from_numpy(arr)
 
-    def gemm(self, A, B, C, m, n, k, mode, cplx=False, opA=0, opB=0):
-        rep = self.L.f4j_report()
+    def gemm(self, A, B, C, m, n, k, mode, cplx=False, opA=0, opB=0, report=False):
+        """One product; with report=True the call also fills (and waits for) the report."""
+        rep = self.L.f4j_report() if report else None
         fn = self.lib.f4j_zgemm if cplx else self.lib.f4j_dgemm
-        self.check(fn(self.ctx.handle, m, n, k, A.handle, opA, B.handle, opB, C.handle, mode, ctypes.byref(rep)))
+        self.check(fn(self.ctx.handle, m, n, k, A.handle, opA, B.handle, opB, C.handle, mode,
+                      ctypes.byref(rep) if report else None))
         return rep
 
     def check_err(self, A, B, C, m, n, k, cplx=False, samples=4096, seed=1234):
@@ -368,7 +370,7 @@ def run_ours(args):
     B_h = synth.scaled(n, n, 8, 2, "col")
     A, B = E.dev(A_h), E.dev(B_h)
     C = E.ctx.alloc(8 * n * n)
-    rep = E.gemm(A, B, C, n, n, n, L.MODE_SPLIT)
+    rep = E.gemm(A, B, C, n, n, n, L.MODE_SPLIT, report=True)
     E.ctx.sync()
     clk = Clocks(local)
     dist.barrier()
@@ -414,7 +416,7 @@ def run_ours(args):
         errs = {}
         for phi in (0, 8, 32):
             Ap, Bp = E.dev(synth.scaled(n, n, phi, 10 + phi, "row")), E.dev(synth.scaled(n, n, phi, 20 + phi, "col"))
-            r = E.gemm(Ap, Bp, C, n, n, n, L.MODE_SPLIT)
+            r = E.gemm(Ap, Bp, C, n, n, n, L.MODE_SPLIT, report=True)
             se = E.check_err(Ap, Bp, C, n, n, n)
             E.gemm(Ap, Bp, C, n, n, n, L.MODE_PLAIN)
             pe = E.check_err(Ap, Bp, C, n, n, n)
@@ -428,7 +430,7 @@ def run_ours(args):
         Az = synth.scaled(nz, nz, 8, 3, "row", cplx=True)
         Bz = synth.scaled(nz, nz, 8, 4, "col", cplx=True)
         dAz, dBz, dCz = E.dev(Az), E.dev(Bz), E.ctx.alloc(16 * nz * nz)
-        zr = E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_SPLIT, cplx=True)
+        zr = E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_SPLIT, cplx=True, report=True)
         zms = E.timed(lambda: E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_SPLIT, cplx=True), 3, 1)
         zs = E.check_err(dAz, dBz, dCz, nz, nz, nz, cplx=True)
         zpms = E.timed(lambda: E.gemm(dAz, dBz, dCz, nz, nz, nz, L.MODE_PLAIN, cplx=True), 1, 1)

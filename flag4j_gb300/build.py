@@ -57,7 +57,7 @@ def build(force=False, verbose=False):
         for _, log in results:
             sys.stderr.write(log)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *[o for o, _ in results]]
+    cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", tmp, *[o for o, _ in results]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

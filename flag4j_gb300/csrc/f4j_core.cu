@@ -364,14 +364,14 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     } else if (mode == F4J_MODE_PLAIN) {
         rc = f4j_gemm_dmma(ctx, cplx, m, n, k, A, opA, B, opB, C);
     } else {
-        bool nonfinite = false;
-        rc = f4j_gemm_split(ctx, cplx, m, n, k, A, opA, B, opB, C, 0, rep, &nonfinite);
+        // NaN/Inf cannot be sliced: the split kernels stand down on the device
+        // and the gated DMMA launch (a no-op otherwise) propagates them like
+        // the reference.  Nothing here waits for the GPU.
+        const int* gate = nullptr;
+        rc = f4j_gemm_split(ctx, cplx, m, n, k, A, opA, B, opB, C, 0, rep, &gate);
         used = F4J_MODE_SPLIT;
-        if (rc == F4J_OK && nonfinite) {
-            // NaN/Inf cannot be sliced; the DMMA path propagates them like the reference.
-            used = F4J_MODE_PLAIN;
-            rc = f4j_gemm_dmma(ctx, cplx, m, n, k, A, opA, B, opB, C);
-        }
+        if (rc == F4J_OK) rc = f4j_gemm_dmma(ctx, cplx, m, n, k, A, opA, B, opB, C, gate);
+        if (rc == F4J_OK && rep && rep->slices == 0) used = F4J_MODE_PLAIN;
     }
     if (rep) {
         rep->mode_used = used;

@@ -125,6 +125,8 @@ struct DmmaParams {
     int opA, opB;
     int use_tma;
     int* status;
+    const int* gate;  // compute only when null or *gate != 0
+    int tiles_n, ntiles;
 };
 
 __device__ __forceinline__ void dmma_16x8x4(double (&d)[4], double a0, double a1, double b0) {
@@ -175,8 +177,8 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
     __shared__ __align__(8) uint64_t full[DM_ST], empty[DM_ST];
     __shared__ int abort_flag;
 
+    if (p.gate && *(volatile const int*)p.gate == 0) return;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int64_t m0 = (int64_t)blockIdx.y * DM_BM, n0 = (int64_t)blockIdx.x * DM_BN;
     const int nk = (int)((p.k + DM_BK - 1) / DM_BK);
 
     if (threadIdx.x == 0) {
@@ -190,11 +192,15 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
     __syncthreads();
 
     if (warp == 0) {
-        // ---------------- producer
-        for (int kt = 0; kt < nk; kt++) {
-            const int s = kt % DM_ST;
-            const uint32_t ph = (kt / DM_ST) & 1;
-            if (kt >= DM_ST) {
+        // ---------------- producer (persistent over tiles; the stage counter
+        // `it` runs on across tiles so barrier phases stay in step)
+        int it = 0;
+        for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+        const int64_t m0 = (int64_t)(tile / p.tiles_n) * DM_BM, n0 = (int64_t)(tile % p.tiles_n) * DM_BN;
+        for (int kt = 0; kt < nk; kt++, it++) {
+            const int s = it % DM_ST;
+            const uint32_t ph = (it / DM_ST) & 1;
+            if (it >= DM_ST) {
                 bool ok = true;
                 if (lane == 0) ok = mbar_wait(&empty[s], ph ^ 1, p.status, 1);
                 ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -248,10 +254,12 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
                 if (lane == 0) mbar_arrive(&full[s]);
             }
         }
+        if (*(volatile int*)&abort_flag) break;
+        }  // tile loop
         // Drain: wait (bounded) for the last copies in flight before exiting.
         if (lane == 0 && p.use_tma) {
-            for (int kt = (nk > DM_ST ? nk - DM_ST : 0); kt < nk; kt++)
-                mbar_wait(&full[kt % DM_ST], (kt / DM_ST) & 1, nullptr, 0);
+            for (int q = (it > DM_ST ? it - DM_ST : 0); q < it; q++)
+                mbar_wait(&full[q % DM_ST], (q / DM_ST) & 1, nullptr, 0);
         }
         return;
     }
@@ -260,6 +268,9 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
     const int cw = warp - 1;
     const int wm = (cw / 2) * 32, wn = (cw % 2) * 32;
     const int g = lane >> 2, t = lane & 3;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    const int64_t m0 = (int64_t)(tile / p.tiles_n) * DM_BM, n0 = (int64_t)(tile % p.tiles_n) * DM_BN;
     double accr[2][4][4], acci[CPLX ? 2 : 1][4][4];
 #pragma unroll
     for (int i = 0; i < 2; i++)
@@ -271,9 +282,9 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
                 if (CPLX) acci[i][j][q] = 0.0;
             }
 
-    for (int kt = 0; kt < nk; kt++) {
-        const int s = kt % DM_ST;
-        const uint32_t ph = (kt / DM_ST) & 1;
+    for (int kt = 0; kt < nk; kt++, it++) {
+        const int s = it % DM_ST;
+        const uint32_t ph = (it / DM_ST) & 1;
         bool ok = true;
         if (lane == 0) ok = mbar_wait(&full[s], ph, p.status, 2);
         ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -327,6 +338,7 @@ __global__ void __launch_bounds__(DM_THREADS, 1)
                     }
                 }
             }
+    }  // tile loop
 }
 
 // ------------------------------------------------------------------ check
@@ -448,7 +460,7 @@ static int make_map_2d(CUtensorMap* map, const void* base, uint64_t inner, uint6
 }
 
 int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
-                  const double* B, int opB, double* C) {
+                  const double* B, int opB, double* C, const int* gate) {
     const int W = cplx ? 2 : 1;
     DmmaParams p{};
     p.m = m; p.n = n; p.k = k; p.A = A; p.B = B; p.C = C;
@@ -456,6 +468,11 @@ int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     p.lda = (opA == F4J_OP_N) ? k : m;
     p.ldb = (opB == F4J_OP_N) ? n : k;
     p.status = ctx->d_status + F4J_ST_TIMEOUT;
+    p.gate = gate;
+    p.tiles_n = (int)f4j_cdiv(n, DM_BN);
+    const int64_t ntiles = f4j_cdiv(n, DM_BN) * f4j_cdiv(m, DM_BM);
+    if (ntiles > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "DMMA GEMM too large");
+    p.ntiles = (int)ntiles;
     // TMA needs 16-byte aligned bases and row strides.
     p.use_tma = f4j_aligned16(A) && f4j_aligned16(B) && ((p.lda * 8 * W) % 16 == 0) &&
                 ((p.ldb * 8 * W) % 16 == 0) && f4j_encode_fn() != nullptr;
@@ -469,9 +486,12 @@ int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
         else rc = make_map_2d(&tb, B, W * k, n, W * DM_BK, DM_BN);
         if (rc) return rc;
     }
-    dim3 grid((unsigned)f4j_cdiv(n, DM_BN), (unsigned)f4j_cdiv(m, DM_BM));
-    if (grid.y > 65535) return f4j_fail(F4J_ERR_ARG, "m too large for the DMMA kernel grid");
     size_t smem = (size_t)DM_ST * (cplx ? DmTile<true>::STAGE_BYTES : DmTile<false>::STAGE_BYTES);
+    // persistent: as many CTAs as fit at once (shared memory bound), each
+    // walking tiles grid-stride
+    const int per_sm = (int)((200 * 1024) / (smem + 2048)) > 0 ? (int)((200 * 1024) / (smem + 2048)) : 1;
+    const int64_t cap = (int64_t)ctx->sm_count * per_sm;
+    const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
     if (cplx) {
         F4J_CUDA(cudaFuncSetAttribute(k_gemm_dmma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         f4j_prof_begin(ctx);

@@ -107,10 +107,12 @@ static inline bool f4j_aligned16(const void* p) { return (reinterpret_cast<uintp
 // Internal GEMM entry points shared by the dense front ends.
 int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                   int opA, const double* B, int opB, double* C, int mode, f4j_report* rep);
+// `gate` (device int, may be null): the DMMA kernel computes only when *gate
+// is non-zero -- the split path's NaN/Inf fallback, decided on the device.
 int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
-                  int opA, const double* B, int opB, double* C);
+                  int opA, const double* B, int opB, double* C, const int* gate = nullptr);
 int f4j_gemm_exact(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                    int opA, const double* B, int opB, double* C);
 int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                    int opA, const double* B, int opB, double* C, int slices_req,
-                   f4j_report* rep, bool* nonfinite);
+                   f4j_report* rep, const int** gate);

@@ -46,17 +46,27 @@ struct Round {
     int32_t kb0, kb1;  // K blocks [kb0, kb1)
 };
 
+// Decided on the device from the exponent statistics (k_plan), so a split
+// GEMM never waits for the host between its kernels.
+struct SplitPlan {
+    int s;          // slices per operand
+    int nrounds;
+    int ubits;      // fixed-point unit exponent: value = acc * 2^(ubits + ea + eb)
+    int nonfinite;  // a NaN/Inf was seen: slicing and the slice GEMM stand down
+    float spread;   // measured exponent spread (bits)
+    int pad[3];
+    Round rounds[MAX_ROUNDS];
+};
+
 struct SplitGemmParams {
     int M, N, Kp;           // cat sizes; Kp multiple of 128
-    int nrounds;
     int cplx;               // 1: C interleaved complex, N = 2n
     int n_out;              // n (complex output columns) or N
-    int ubits;              // fixed-point unit exponent: value = acc * 2^(ubits + ea + eb)
     const int* ea;          // [M]
     const int* eb;          // [N]
     double* C;
     int* status;
-    Round rounds[MAX_ROUNDS];
+    const SplitPlan* plan;
 };
 
 // ------------------------------------------------------------------ stats
@@ -151,6 +161,75 @@ __global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long l
     if ((threadIdx.x & 31) == 0 && sp) atomicMax(spread_x256, sp);
 }
 
+// ------------------------------------------------------------------ plan
+// Slice count from the measured exponent spread sigma (bits between a row's
+// largest and its mean element exponent) and the inner dimension k.  The
+// truncation error of an element is 2^-F of its row's 2^e; it must stay below
+// the plain FP64 product's error, which grows with k while the truncation
+// error grows only with sqrt(k):  F >= max(48 + sigma, 54 + sigma - log2 k).
+__host__ __device__ inline int slices_for(double spread, int64_t k) {
+    const double sg = spread > 0 ? spread : 0.0;
+    int lk = 0;
+    while (lk < 62 && (2ll << lk) <= k) lk++;  // floor(log2 k)
+    const double need = fmax(48.0 + sg, 54.0 + sg - (double)lk);
+    int s = 1 + (int)ceil((need - 4.0) / 5.0);
+    return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
+}
+
+// Round table: products A_i B_j with i + j = t (weight level t) accumulate in
+// one TMEM buffer as long as pairs * kchunk * 16 * 16 <= 2^24, which keeps the
+// FP32 accumulator an exact integer; larger levels / K are split into rounds.
+// The fixed-point unit keeps the worst-case accumulator below 2^62.
+__host__ __device__ inline int plan_rounds(int s, int64_t Kp, int64_t klen_cat, Round* out, int* ubits) {
+    const int64_t nkb = Kp / BKB;
+    int64_t kchunk_blocks = nkb;
+    while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
+    const int64_t kchunk = kchunk_blocks * BKB;
+    int64_t pairs_per_round = (1ll << 24) / (kchunk * 256);
+    if (pairs_per_round < 1) pairs_per_round = 1;
+    int kbits = 0;
+    while (kbits < 62 && (1ll << kbits) < (klen_cat > 0 ? klen_cat : 1)) kbits++;  // ceil(log2 k)
+    int D = kbits + 9 + 5 * (s - 1) - 62;
+    if (D < 0) D = 0;
+    *ubits = -(8 + 5 * (s - 1)) + D;
+    int n = 0;
+    for (int t = 2; t <= s + 1; t++) {
+        const int ilo = t - s > 1 ? t - s : 1, ihi = t - 1 < s ? t - 1 : s;  // inclusive
+        const int shift = 5 * (s + 1 - t) - D;
+        for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
+            for (int i = ilo; i <= ihi; i += (int)pairs_per_round) {
+                if (n >= MAX_ROUNDS) return -1;
+                Round rd;
+                rd.level = (uint8_t)t;
+                rd.i0 = (uint8_t)i;
+                rd.i1 = (uint8_t)((i + pairs_per_round - 1 < ihi ? i + pairs_per_round - 1 : ihi) + 1);
+                rd.shift = (int8_t)shift;
+                rd.kb0 = (int32_t)kb;
+                rd.kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
+                out[n++] = rd;
+            }
+        }
+    }
+    return n;
+}
+
+// One thread: slice count, round table and unit from the statistics.
+// misc: [0] non-finite flag, [1] spread of A x256, [2] spread of B x256.
+__global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
+                       SplitPlan* __restrict__ plan) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
+    int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
+    int ubits = 0;
+    int n = plan_rounds(s, Kp, klen_cat, plan->rounds, &ubits);
+    plan->s = s;
+    plan->nrounds = n < 0 ? 0 : n;
+    plan->ubits = ubits;
+    plan->spread = (float)spread;
+    // a plan that does not fit is treated like a non-finite input (plain path)
+    plan->nonfinite = (misc[0] != 0 || n < 0) ? 1 : 0;
+}
+
 // ------------------------------------------------------------------ split
 __device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
     int v = d < 0 ? -d : d;
@@ -193,10 +272,12 @@ constexpr int SP_TR = 32, SP_TQ = 64;  // tile: 32 target rows x 64 k-indices
 __global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int64_t srows, int64_t scols,
                                                int transposed, int cplx, int conj, int role,
                                                int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
-                                               int64_t rows_out, const int* __restrict__ e_t, int s,
-                                               uint8_t* __restrict__ out) {
+                                               int64_t rows_out, const int* __restrict__ e_t,
+                                               const SplitPlan* __restrict__ plan, uint8_t* __restrict__ out) {
     __shared__ double sre[SP_TR][SP_TQ + 1];
     __shared__ double sim[SP_TR][SP_TQ + 1];
+    if (plan->nonfinite) return;
+    const int s = plan->s;
     const int64_t r0 = (int64_t)blockIdx.y * SP_TR, q0 = (int64_t)blockIdx.x * SP_TQ;
     // ---- stage the tile (zeros outside the matrix)
     for (int e = threadIdx.x; e < SP_TR * SP_TQ; e += 256) {
@@ -285,8 +366,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     __shared__ uint32_t tmem_base_slot;
     __shared__ int abort_flag;
 
+    const SplitPlan* __restrict__ plan = p.plan;
+    if (plan->nonfinite) return;  // the gated plain path computes this product
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int nrounds = plan->nrounds;
+    // persistent: CTA b takes tiles b, b + grid, ...; tiles run along N within
+    // a row of tiles so concurrently active CTAs share A panels in L2
+    const int tiles_n = (p.N + BN - 1) / BN, tiles_m = (p.M + BM - 1) / BM;
+    const int ntiles = tiles_n * tiles_m;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; i++) {
@@ -318,20 +405,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // ---------------- TMA producer
         if (lane == 0) {
             int it = 0;
-            for (int r = 0; r < p.nrounds && !abort_flag; r++) {
-                const Round rd = p.rounds[r];
-                for (int i = rd.i0; i < rd.i1 && !abort_flag; i++) {
-                    const int j = rd.level - i;
-                    for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
-                        const int s = it % STAGES;
-                        const uint32_t ph = (it / STAGES) & 1;
-                        if (it >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.status, 11)) {
-                            abort_flag = 1;
-                            break;
+            for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
+                const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+                for (int r = 0; r < nrounds && !*(volatile int*)&abort_flag; r++) {
+                    const Round rd = plan->rounds[r];
+                    for (int i = rd.i0; i < rd.i1 && !*(volatile int*)&abort_flag; i++) {
+                        const int j = rd.level - i;
+                        for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
+                            const int s = it % STAGES;
+                            const uint32_t ph = (it / STAGES) & 1;
+                            if (it >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.status, 11)) {
+                                abort_flag = 1;
+                                break;
+                            }
+                            mbar_arrive_expect_tx(&full[s], 2 * TILE_BYTES);
+                            tma_load_3d(sA + s * TILE_BYTES, &tmA, &full[s], kb * BKB, m0, i - 1);
+                            tma_load_3d(sB + s * TILE_BYTES, &tmB, &full[s], kb * BKB, n0, j - 1);
                         }
-                        mbar_arrive_expect_tx(&full[s], 2 * TILE_BYTES);
-                        tma_load_3d(sA + s * TILE_BYTES, &tmA, &full[s], kb * BKB, m0, i - 1);
-                        tma_load_3d(sB + s * TILE_BYTES, &tmB, &full[s], kb * BKB, n0, j - 1);
                     }
                 }
             }
@@ -343,38 +433,40 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
             constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
-            int it = 0;
-            for (int r = 0; r < p.nrounds && !abort_flag; r++) {
-                const Round rd = p.rounds[r];
-                const int buf = r % NBUF;
-                if (r >= NBUF && !mbar_wait(&accempty[buf], ((r / NBUF) & 1) ^ 1, p.status, 12)) {
-                    abort_flag = 1;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t d_tmem = tmem + buf * BN;
-                bool first = true;
-                for (int i = rd.i0; i < rd.i1 && !abort_flag; i++) {
-                    for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
-                        const int s = it % STAGES;
-                        if (!mbar_wait(&full[s], (it / STAGES) & 1, p.status, 13)) {
-                            abort_flag = 1;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint64_t da = umma_desc_sw128(sA + s * TILE_BYTES);
-                        const uint64_t db = umma_desc_sw128(sB + s * TILE_BYTES);
-#pragma unroll
-                        for (int kk = 0; kk < BKB / 32; kk++) {
-                            // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
-                            umma_f8(d_tmem, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), idesc,
-                                    first ? 0u : 1u);
-                            first = false;
-                        }
-                        umma_commit(&empty[s]);
+            int it = 0, rg = 0;  // stage and round counters carried across tiles
+            for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
+                for (int r = 0; r < nrounds && !*(volatile int*)&abort_flag; r++, rg++) {
+                    const Round rd = plan->rounds[r];
+                    const int buf = rg % NBUF;
+                    if (rg >= NBUF && !mbar_wait(&accempty[buf], ((rg / NBUF) & 1) ^ 1, p.status, 12)) {
+                        abort_flag = 1;
+                        break;
                     }
+                    tc_fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+                    bool first = true;
+                    for (int i = rd.i0; i < rd.i1 && !*(volatile int*)&abort_flag; i++) {
+                        for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
+                            const int s = it % STAGES;
+                            if (!mbar_wait(&full[s], (it / STAGES) & 1, p.status, 13)) {
+                                abort_flag = 1;
+                                break;
+                            }
+                            tc_fence_after();
+                            const uint64_t da = umma_desc_sw128(sA + s * TILE_BYTES);
+                            const uint64_t db = umma_desc_sw128(sB + s * TILE_BYTES);
+#pragma unroll
+                            for (int kk = 0; kk < BKB / 32; kk++) {
+                                // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
+                                umma_f8(d_tmem, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), idesc,
+                                        first ? 0u : 1u);
+                                first = false;
+                            }
+                            umma_commit(&empty[s]);
+                        }
+                    }
+                    umma_commit(&accfull[buf]);
                 }
-                umma_commit(&accfull[buf]);
             }
             umma_commit(&mma_done);
             mbar_wait(&mma_done, 0, p.status, 14);
@@ -383,15 +475,19 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // ---------------- epilogue warps 2..9
         const int q = warp % 4;          // TMEM lane quarter this warp may access
         const int h = (warp - 2) / 4;    // column half of the tile
+        const int ubits = plan->ubits;
+        int rg = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
         const int row = m0 + 32 * q + lane;
         long long acc[64];
 #pragma unroll
         for (int c = 0; c < 64; c++) acc[c] = 0;
         bool ok = true;
-        for (int r = 0; r < p.nrounds; r++) {
-            const int buf = r % NBUF;
+        for (int r = 0; r < nrounds; r++, rg++) {
+            const int buf = rg % NBUF;
             bool w = true;
-            if (lane == 0) w = mbar_wait(&accfull[buf], (r / NBUF) & 1, p.status, 15);
+            if (lane == 0) w = mbar_wait(&accfull[buf], (rg / NBUF) & 1, p.status, 15);
             w = __shfl_sync(0xffffffffu, w, 0);
             if (!w || *(volatile int*)&abort_flag) {
                 ok = false;
@@ -399,7 +495,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            const int sh = p.rounds[r].shift;
+            const int sh = plan->rounds[r].shift;
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 uint32_t v[32];
@@ -417,14 +513,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(&accempty[buf]);
         }
-        if (ok && row < p.M) {
+        if (!ok) break;
+        if (row < p.M) {
             const int ea = p.ea[row];
 #pragma unroll
             for (int c = 0; c < 64; c += 2) {
                 const int col = n0 + h * 64 + c;
                 double v0 = 0, v1 = 0;
-                if (col < p.N) v0 = scale_pow2((double)acc[c], p.ubits + ea + p.eb[col]);
-                if (col + 1 < p.N) v1 = scale_pow2((double)acc[c + 1], p.ubits + ea + p.eb[col + 1]);
+                if (col < p.N) v0 = scale_pow2((double)acc[c], ubits + ea + p.eb[col]);
+                if (col + 1 < p.N) v1 = scale_pow2((double)acc[c + 1], ubits + ea + p.eb[col + 1]);
                 if (!p.cplx) {
                     double* dst = p.C + (int64_t)row * p.N + col;
                     if (col + 1 < p.N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
@@ -444,6 +541,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 }
             }
         }
+        }  // tile loop
     }
     tc_fence_before();
     __syncthreads();
@@ -470,83 +568,43 @@ static int make_slice_map(CUtensorMap* map, const void* base, uint64_t Kp, uint6
     return F4J_OK;
 }
 
-// Slice count from the measured exponent spread sigma (bits between a row's
-// largest and its mean element exponent) and the inner dimension k.  The
-// truncation error of an element is 2^-F of its row's 2^e; it must stay below
-// the plain FP64 product's error, which grows with k while the truncation
-// error grows only with sqrt(k):  F >= max(48 + sigma, 54 + sigma - log2 k).
-static int slices_for_spread(double spread, int64_t k) {
+// Slice-count override from the environment (F4J_SPLIT_SLICES), 0 = from spread.
+static int env_slices() {
     const char* env = getenv("F4J_SPLIT_SLICES");
-    if (env && atoi(env) > 0) {
-        int s = atoi(env);
-        return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
-    }
-    const double sg = spread > 0 ? spread : 0.0;
-    const double lk = floor(log2((double)(k > 1 ? k : 1)));
-    const double need = fmax(48.0 + sg, 54.0 + sg - lk);
-    int s = 1 + (int)ceil((need - 4.0) / 5.0);
-    return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
+    return (env && atoi(env) > 0) ? atoi(env) : 0;
 }
 
-// Build the round table: rounds of one level whose FP32 sums stay exact.
-static int build_rounds(int s, int64_t Kp, int64_t klen_cat, std::vector<Round>& out, int& ubits) {
-    out.clear();
-    const int64_t nkb = Kp / BKB;
-    // exact budget: pairs * kchunk * 256 <= 2^24
-    int64_t kchunk_blocks = nkb;
-    while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
-    const int64_t kchunk = kchunk_blocks * BKB;
-    int64_t pairs_per_round = (1ll << 24) / (kchunk * 256);
-    if (pairs_per_round < 1) pairs_per_round = 1;
-    // fixed-point unit: finest level weight is 2^-(8 + 5(s-1)); drop D bits so
-    // the worst-case accumulator magnitude stays below 2^62.
-    double kbits = log2((double)(klen_cat > 0 ? klen_cat : 1));
-    int D = (int)ceil(kbits + 8.0 + 5.0 * (s - 1) + 0.2 - 62.0);
-    if (D < 0) D = 0;
-    ubits = -(8 + 5 * (s - 1)) + D;
-    for (int t = 2; t <= s + 1; t++) {
-        const int ilo = t - s > 1 ? t - s : 1, ihi = t - 1 < s ? t - 1 : s;  // inclusive
-        const int shift = 5 * (s + 1 - t) - D;
-        if (shift > 62 || shift < -62) return f4j_fail(F4J_ERR_UNSUPPORTED, "slice weight out of range");
-        for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
-            for (int i = ilo; i <= ihi; i += (int)pairs_per_round) {
-                Round rd;
-                rd.level = (uint8_t)t;
-                rd.i0 = (uint8_t)i;
-                rd.i1 = (uint8_t)((i + pairs_per_round - 1 < ihi ? i + pairs_per_round - 1 : ihi) + 1);
-                rd.shift = (int8_t)shift;
-                rd.kb0 = (int32_t)kb;
-                rd.kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
-                out.push_back(rd);
-            }
-        }
-    }
-    if ((int)out.size() > MAX_ROUNDS) return f4j_fail(F4J_ERR_UNSUPPORTED, "too many split rounds (%d)", (int)out.size());
-    return F4J_OK;
-}
+static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 
+// Asynchronous split GEMM: statistics -> device plan -> slicing -> slice GEMM,
+// all queued on the context stream with no host synchronisation.  *gate
+// receives the device flag that is non-zero when the plan stood down (NaN/Inf
+// input); the caller then runs the gated plain kernel.  With a report the
+// call waits for the plan to fill in slices / spread.
 int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
-                   const double* B, int opB, double* C, int slices_req, f4j_report* rep, bool* nonfinite) {
-    *nonfinite = false;
+                   const double* B, int opB, double* C, int slices_req, f4j_report* rep, const int** gate) {
+    *gate = nullptr;
     const int64_t M = m, N = cplx ? 2 * n : n;
     const int64_t Kh = f4j_cdiv(k, BKB) * BKB;  // K of one real part, padded to whole stages
     const int64_t Kp = cplx ? 2 * Kh : Kh;      // cat K: [re | im], zero padded in between
     const int64_t klen_cat = cplx ? 2 * k : k;
     if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "split GEMM too large");
 
-    // ---- small workspace (slot 1): statistics and exponents
-    auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
-    const size_t off_mxa = 0, off_esa = off_mxa + al(M * 8), off_cna = off_esa + al(M * 8);
-    const size_t off_mxb = off_cna + al(M * 4), off_esb = off_mxb + al(n * 8), off_cnb = off_esb + al(n * 8);
-    const size_t off_ea = off_cnb + al(n * 4), off_eb = off_ea + al(M * 4);
-    const size_t off_misc = off_eb + al(N * 4);
-    const size_t small_bytes = off_misc + 1024;
-    void* ws1;
+    // ---- small workspace (slot 1): statistics, exponents, plan
+    const size_t off_mxa = 0, off_esa = off_mxa + al1k(M * 8), off_cna = off_esa + al1k(M * 8);
+    const size_t off_mxb = off_cna + al1k(M * 4), off_esb = off_mxb + al1k(n * 8), off_cnb = off_esb + al1k(n * 8);
+    const size_t off_ea = off_cnb + al1k(n * 4), off_eb = off_ea + al1k(M * 4);
+    const size_t off_misc = off_eb + al1k(N * 4);
+    const size_t off_plan = off_misc + 1024;
+    const size_t small_bytes = off_plan + al1k(sizeof(SplitPlan));
+    // ---- bulk workspace (slot 0): S_MAX slice planes per operand
+    const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
+    void *ws1, *ws0;
     int rc = f4j_workspace(ctx, 1, small_bytes, &ws1);
     if (rc) return rc;
+    rc = f4j_workspace(ctx, 0, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX), &ws0);
+    if (rc) return rc;
     char* w = (char*)ws1;
-    F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, ctx->stream));
-    F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, ctx->stream));
     unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
     long long* esa = (long long*)(w + off_esa);
     int* cna = (int*)(w + off_cna);
@@ -556,8 +614,15 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     int* ea = (int*)(w + off_ea);
     int* eb = (int*)(w + off_eb);
     int* misc = (int*)(w + off_misc);  // [0] non-finite seen, [1] spread A x256, [2] spread B x256
+    SplitPlan* plan = (SplitPlan*)(w + off_plan);
+    uint8_t* slA = (uint8_t*)ws0;
+    uint8_t* slB = slA + al1k(plane_a * S_MAX);
+
+    F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, ctx->stream));
+    F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, ctx->stream));
 
     const bool a_rows = (opA == F4J_OP_N);  // targets of A (rows of op(A)) are stored rows
+    const bool b_rows = (opB != F4J_OP_N);  // targets of B (columns of op(B)) are stored rows
     f4j_prof_begin(ctx, F4J_PROF_PREP);
     if (a_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
@@ -566,7 +631,6 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
         k_stats_cols<<<g, 256, 0, ctx->stream>>>(A, k, M, cplx, mxa, esa, cna, misc);
     }
     F4J_LAUNCHED(ctx);
-    const bool b_rows = (opB != F4J_OP_N);  // targets of B (columns of op(B)) are stored rows
     if (b_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, ctx->stream>>>(B, n, k, cplx, mxb, esb, cnb, misc);
     } else {
@@ -579,76 +643,48 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
-    f4j_prof_end(ctx);
-    int hmisc[3];
-    F4J_CUDA(cudaMemcpyAsync(hmisc, misc, sizeof hmisc, cudaMemcpyDeviceToHost, ctx->stream));
-    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (hmisc[0]) {
-        *nonfinite = true;
-        return F4J_OK;
-    }
-    const double spread = (hmisc[1] > hmisc[2] ? hmisc[1] : hmisc[2]) / 256.0;
-    const int s = slices_req > 0 ? (slices_req > S_MAX ? S_MAX : slices_req) : slices_for_spread(spread, k);
-
-    std::vector<Round> rounds;
-    int ubits = 0;
-    rc = build_rounds(s, Kp, klen_cat, rounds, ubits);
-    if (rc) return rc;
-
-    // ---- bulk workspace (slot 0): slice planes
-    const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
-    void* ws0;
-    rc = f4j_workspace(ctx, 0, al(plane_a * s) + al(plane_b * s), &ws0);
-    if (rc) return rc;
-    uint8_t* slA = (uint8_t*)ws0;
-    uint8_t* slB = slA + al(plane_a * s);
-
-    f4j_prof_begin(ctx, F4J_PROF_PREP);
+    k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(), plan);
+    F4J_LAUNCHED(ctx);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
         k_split<<<g, 256, 0, ctx->stream>>>(A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, cplx,
-                                            opA == F4J_OP_C, 0, M, k, Kh, Kp, M, ea, s, slA);
+                                            opA == F4J_OP_C, 0, M, k, Kh, Kp, M, ea, plan, slA);
         F4J_LAUNCHED(ctx);
     }
     {   // B: targets = columns of op(B); stored k x n (N, transposed read) or n x k (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(n, SP_TR));
         k_split<<<g, 256, 0, ctx->stream>>>(B, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, cplx,
-                                            opB == F4J_OP_C, 1, n, k, Kh, Kp, N, eb, s, slB);
+                                            opB == F4J_OP_C, 1, n, k, Kh, Kp, N, eb, plan, slB);
         F4J_LAUNCHED(ctx);
     }
     f4j_prof_end(ctx);
 
     CUtensorMap ta{}, tb{};
-    rc = make_slice_map(&ta, slA, Kp, M, s);
+    rc = make_slice_map(&ta, slA, Kp, M, S_MAX);
     if (rc) return rc;
-    rc = make_slice_map(&tb, slB, Kp, N, s);
+    rc = make_slice_map(&tb, slB, Kp, N, S_MAX);
     if (rc) return rc;
 
-    SplitGemmParams* prm = new SplitGemmParams();
-    prm->M = (int)M;
-    prm->N = (int)N;
-    prm->Kp = (int)Kp;
-    prm->nrounds = (int)rounds.size();
-    prm->cplx = cplx ? 1 : 0;
-    prm->n_out = (int)n;
-    prm->ubits = ubits;
-    prm->ea = ea;
-    prm->eb = eb;
-    prm->C = C;
-    prm->status = ctx->d_status + F4J_ST_TIMEOUT;
-    for (size_t i = 0; i < rounds.size(); i++) prm->rounds[i] = rounds[i];
+    SplitGemmParams prm{};
+    prm.M = (int)M;
+    prm.N = (int)N;
+    prm.Kp = (int)Kp;
+    prm.cplx = cplx ? 1 : 0;
+    prm.n_out = (int)n;
+    prm.ea = ea;
+    prm.eb = eb;
+    prm.C = C;
+    prm.status = ctx->d_status + F4J_ST_TIMEOUT;
+    prm.plan = plan;
 
     const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) {
-        delete prm;
-        return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
-    }
-    dim3 grid((unsigned)f4j_cdiv(N, BN), (unsigned)f4j_cdiv(M, BM));
+    if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
+    const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
+    const unsigned grid = (unsigned)(ntiles < ctx->sm_count ? ntiles : ctx->sm_count);
     f4j_prof_begin(ctx);
-    k_split_gemm<<<grid, GEMM_THREADS, smem, ctx->stream>>>(ta, tb, *prm);
+    k_split_gemm<<<grid, GEMM_THREADS, smem, ctx->stream>>>(ta, tb, prm);
     f4j_prof_end(ctx);
-    delete prm;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         cudaFuncAttributes fa{};
@@ -660,11 +696,18 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
                         fa.localSizeBytes, fa.maxDynamicSharedSizeBytes, smem, sizeof(SplitGemmParams));
     }
     ctx->launches++;
+    *gate = &plan->nonfinite;
 
     if (rep) {
-        rep->slices = s;
-        rep->frac_bits = 4 + 5 * (s - 1);
+        int hp[5];
+        F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        float spread;
+        memcpy(&spread, &hp[4], 4);
+        rep->slices = hp[0];
+        rep->frac_bits = 4 + 5 * (hp[0] - 1);
         rep->exp_spread = spread;
+        if (hp[3]) rep->slices = 0;
     }
     return F4J_OK;
 }
@@ -719,16 +762,16 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
         F4J_CUDA(cudaMemsetAsync(C, 0, (size_t)m * n * 8, st));
         return F4J_OK;
     }
-    auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
     const int64_t M = m, N = n;
     const int64_t Kp = f4j_cdiv(k, BKB) * BKB;
-    const size_t off_mxa = 0, off_esa = off_mxa + al(M * 8), off_cna = off_esa + al(M * 8);
-    const size_t off_mxb = off_cna + al(M * 4), off_esb = off_mxb + al(N * 8), off_cnb = off_esb + al(N * 8);
-    const size_t off_ea = off_cnb + al(N * 4), off_eb = off_ea + al(M * 4);
-    const size_t off_misc = off_eb + al(N * 4);
-    const size_t off_sl = off_misc + 1024;
+    const size_t off_mxa = 0, off_esa = off_mxa + al1k(M * 8), off_cna = off_esa + al1k(M * 8);
+    const size_t off_mxb = off_cna + al1k(M * 4), off_esb = off_mxb + al1k(N * 8), off_cnb = off_esb + al1k(N * 8);
+    const size_t off_ea = off_cnb + al1k(N * 4), off_eb = off_ea + al1k(M * 4);
+    const size_t off_misc = off_eb + al1k(N * 4);
+    const size_t off_plan = off_misc + 1024;
+    const size_t off_sl = off_plan + al1k(sizeof(SplitPlan));
     // worst case over the slice counts this function may pick
-    const size_t need = off_sl + al((size_t)M * Kp * S_MAX) + al((size_t)N * Kp * S_MAX);
+    const size_t need = off_sl + al1k((size_t)M * Kp * S_MAX) + al1k((size_t)N * Kp * S_MAX);
     if (need > F4J_NOALLOC_SCRATCH_BYTES)
         return f4j_fail(F4J_ERR_ARG,
                         "f4j_dgemm_split_noalloc: m=%lld n=%lld k=%lld needs %zu bytes of scratch, more than the "
@@ -737,6 +780,9 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     void* base;
     int rc = noalloc_scratch(&base);
     if (rc) return rc;
+    int dev = 0, sms = 0;
+    F4J_CUDA(cudaGetDevice(&dev));
+    F4J_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     char* w = (char*)base;
     unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
     long long* esa = (long long*)(w + off_esa);
@@ -747,6 +793,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     int* ea = (int*)(w + off_ea);
     int* eb = (int*)(w + off_eb);
     int* misc = (int*)(w + off_misc);  // [0] non-finite, [1..2] spreads, [8] wait status
+    SplitPlan* plan = (SplitPlan*)(w + off_plan);
     // statistics accumulate with atomics and the status word must read 0
     F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, st));
     F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, st));
@@ -760,47 +807,43 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
                                                                                                  esb, cnb, misc);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
+    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), plan);
     F4J_CUDA(cudaGetLastError());
-    int hmisc[3];
-    F4J_CUDA(cudaMemcpyAsync(hmisc, misc, sizeof hmisc, cudaMemcpyDeviceToHost, st));
+    // NaN/Inf operands are rejected, so wait for the plan's verdict
+    int hp[4];
+    F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, st));
     F4J_CUDA(cudaStreamSynchronize(st));
-    if (hmisc[0])
+    if (hp[3])
         return f4j_fail(F4J_ERR_ARG, "f4j_dgemm_split_noalloc: NaN or Inf in an operand; use f4j_dgemm (AUTO)");
-    const double spread = (hmisc[1] > hmisc[2] ? hmisc[1] : hmisc[2]) / 256.0;
-    const int s = slices_for_spread(spread, k);
-    std::vector<Round> rounds;
-    int ubits = 0;
-    rc = build_rounds(s, Kp, k, rounds, ubits);
-    if (rc) return rc;
     uint8_t* slA = (uint8_t*)(w + off_sl);
-    uint8_t* slB = slA + al((size_t)M * Kp * s);
+    uint8_t* slB = slA + al1k((size_t)M * Kp * S_MAX);
     k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
-        A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, 0, M, k, Kp, Kp, M, ea, s, slA);
+        A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, 0, M, k, Kp, Kp, M, ea, plan, slA);
     k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(N, SP_TR)), 256, 0, st>>>(
-        B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 0, 1, N, k, Kp, Kp, N, eb, s, slB);
+        B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 0, 1, N, k, Kp, Kp, N, eb, plan, slB);
     F4J_CUDA(cudaGetLastError());
     CUtensorMap ta{}, tb{};
-    rc = make_slice_map(&ta, slA, Kp, M, s);
+    rc = make_slice_map(&ta, slA, Kp, M, S_MAX);
     if (rc) return rc;
-    rc = make_slice_map(&tb, slB, Kp, N, s);
+    rc = make_slice_map(&tb, slB, Kp, N, S_MAX);
     if (rc) return rc;
     SplitGemmParams prm{};
     prm.M = (int)M;
     prm.N = (int)N;
     prm.Kp = (int)Kp;
-    prm.nrounds = (int)rounds.size();
     prm.cplx = 0;
     prm.n_out = (int)N;
-    prm.ubits = ubits;
     prm.ea = ea;
     prm.eb = eb;
     prm.C = C;
     prm.status = misc + 8;
-    for (size_t i = 0; i < rounds.size(); i++) prm.rounds[i] = rounds[i];
+    prm.plan = plan;
     const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_split_gemm<<<dim3((unsigned)f4j_cdiv(N, BN), (unsigned)f4j_cdiv(M, BM)), GEMM_THREADS, smem, st>>>(ta, tb, prm);
+    const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
+    const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
+    k_split_gemm<<<grid, GEMM_THREADS, smem, st>>>(ta, tb, prm);
     F4J_CUDA(cudaGetLastError());
-    if (slices_out) *slices_out = s;
+    if (slices_out) *slices_out = hp[0];
     return F4J_OK;
 }
