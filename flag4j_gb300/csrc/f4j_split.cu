@@ -32,12 +32,12 @@ namespace {
 
 constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits keeps Y < 2^62 in int64
 constexpr int BM = 128, BN = 128;  // output tile
-constexpr int BKB = 128;           // K bytes per stage (one 128B swizzle row)
-constexpr int STAGES = 6;
+constexpr int BKB = 128;           // K bytes per tile load (one 128B swizzle row)
+constexpr int RING = 12;           // shared-memory ring of operand tiles (A or B slice tiles)
 constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns
-constexpr int TILE_BYTES = BM * BKB;  // 16 KB (A) and 16 KB (B) per stage
+constexpr int TILE_BYTES = BM * BKB;  // 16 KB per operand tile
 constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
-constexpr int MAX_ROUNDS = 256;
+constexpr int MAX_ROUNDS = 512, MAX_GROUPS = 320, MAX_LOADS = 4096, MAX_OPS = 2048;
 
 struct Round {
     uint8_t level;   // t = i + j
@@ -46,16 +46,40 @@ struct Round {
     int32_t kb0, kb1;  // K blocks [kb0, kb1)
 };
 
+// A group runs one or two rounds of adjacent levels together: per K block
+// it loads each needed slice tile once and issues the rounds' MMAs in
+// zig-zag order (A_i B_{t+1-i}, A_i B_{t-i}, A_{i+1} B_{t-i}, ...), so a tile
+// feeds up to two MMAs before its ring slot is released.
+struct Load {
+    uint8_t which;  // 0: A slice tile, 1: B slice tile
+    uint8_t slice;  // 0-based slice plane
+};
+struct Op {
+    uint8_t la, lb;  // indices of the A and B tiles in the group's load list
+    uint8_t buf;     // 0: the group's first round, 1: its second
+    uint8_t rel;     // bit 0: last use of A tile, bit 1: last use of B tile
+};
+struct Group {
+    int16_t r0, nr;        // rounds [r0, r0 + nr)
+    int16_t load0, nload;  // load list (per K block)
+    int16_t op0, nop;      // MMA list (per K block)
+    int32_t kb0, kb1;      // K blocks
+};
+
 // Decided on the device from the exponent statistics (k_plan), so a split
 // GEMM never waits for the host between its kernels.
 struct SplitPlan {
     int s;          // slices per operand
     int nrounds;
     int ubits;      // fixed-point unit exponent: value = acc * 2^(ubits + ea + eb)
-    int nonfinite;  // a NaN/Inf was seen: slicing and the slice GEMM stand down
+    int nonfinite;  // a NaN/Inf was seen (or no plan fits): the split stands down
     float spread;   // measured exponent spread (bits)
-    int pad[3];
+    int ngroups;
+    int pad[2];
     Round rounds[MAX_ROUNDS];
+    Group groups[MAX_GROUPS];
+    Load loads[MAX_LOADS];
+    Op ops[MAX_OPS];
 };
 
 struct SplitGemmParams {
@@ -180,51 +204,110 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
 // one TMEM buffer as long as pairs * kchunk * 16 * 16 <= 2^24, which keeps the
 // FP32 accumulator an exact integer; larger levels / K are split into rounds.
 // The fixed-point unit keeps the worst-case accumulator below 2^62.
-__host__ __device__ inline int plan_rounds(int s, int64_t Kp, int64_t klen_cat, Round* out, int* ubits) {
+// Rounds are emitted group by group: for each K chunk, each level pair
+// (t, t+1) and each chunk of A-slice indices i, one group holding the round of
+// level t and the round of level t+1 restricted to those i.  Returns the
+// number of rounds, or -1 if a table would overflow.
+__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P) {
     const int64_t nkb = Kp / BKB;
     int64_t kchunk_blocks = nkb;
     while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
     const int64_t kchunk = kchunk_blocks * BKB;
-    int64_t pairs_per_round = (1ll << 24) / (kchunk * 256);
-    if (pairs_per_round < 1) pairs_per_round = 1;
+    int64_t PP = (1ll << 24) / (kchunk * 256);  // pairs per round
+    if (PP < 1) PP = 1;
     int kbits = 0;
     while (kbits < 62 && (1ll << kbits) < (klen_cat > 0 ? klen_cat : 1)) kbits++;  // ceil(log2 k)
     int D = kbits + 9 + 5 * (s - 1) - 62;
     if (D < 0) D = 0;
-    *ubits = -(8 + 5 * (s - 1)) + D;
-    int n = 0;
-    for (int t = 2; t <= s + 1; t++) {
-        const int ilo = t - s > 1 ? t - s : 1, ihi = t - 1 < s ? t - 1 : s;  // inclusive
-        const int shift = 5 * (s + 1 - t) - D;
-        for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
-            for (int i = ilo; i <= ihi; i += (int)pairs_per_round) {
-                if (n >= MAX_ROUNDS) return -1;
-                Round rd;
-                rd.level = (uint8_t)t;
-                rd.i0 = (uint8_t)i;
-                rd.i1 = (uint8_t)((i + pairs_per_round - 1 < ihi ? i + pairs_per_round - 1 : ihi) + 1);
-                rd.shift = (int8_t)shift;
-                rd.kb0 = (int32_t)kb;
-                rd.kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
-                out[n++] = rd;
+    P->ubits = -(8 + 5 * (s - 1)) + D;
+    int nr = 0, ng = 0, nl = 0, no = 0;
+    for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
+        const int32_t kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
+        for (int t = 2; t <= s + 1; t += 2) {
+            for (int c0 = 1; c0 <= s; c0 += (int)PP) {
+                const int c1 = c0 + (int)PP - 1 < s ? c0 + (int)PP - 1 : s;
+                if (ng >= MAX_GROUPS || nr + 2 > MAX_ROUNDS) return -1;
+                Group g;
+                g.r0 = (int16_t)nr;
+                g.nr = 0;
+                g.load0 = (int16_t)nl;
+                g.op0 = (int16_t)no;
+                g.kb0 = (int32_t)kb;
+                g.kb1 = kb1;
+                int lo[2] = {0, 0}, hi[2] = {-1, -1}, pos[2] = {0, 0};
+                for (int u = 0; u < 2; u++) {
+                    const int tt = t + u;
+                    if (tt > s + 1) continue;
+                    int ilo = tt - s > 1 ? tt - s : 1, ihi = tt - 1 < s ? tt - 1 : s;
+                    if (ilo < c0) ilo = c0;
+                    if (ihi > c1) ihi = c1;
+                    if (ilo > ihi) continue;
+                    lo[u] = ilo;
+                    hi[u] = ihi;
+                    pos[u] = g.nr++;
+                    Round rd;
+                    rd.level = (uint8_t)tt;
+                    rd.i0 = (uint8_t)ilo;
+                    rd.i1 = (uint8_t)(ihi + 1);
+                    rd.shift = (int8_t)(5 * (s + 1 - tt) - D);
+                    rd.kb0 = (int32_t)kb;
+                    rd.kb1 = kb1;
+                    P->rounds[nr++] = rd;
+                }
+                if (g.nr == 0) continue;
+                // zig-zag: for each i, the level t+1 product then the level t product
+                int la[S_MAX + 2], lb[S_MAX + 2];
+                for (int q = 0; q < S_MAX + 2; q++) la[q] = lb[q] = -1;
+                for (int i = c0; i <= c1; i++) {
+                    for (int u = 1; u >= 0; u--) {
+                        if (i < lo[u] || i > hi[u]) continue;
+                        const int j = t + u - i;
+                        if (nl + 2 > MAX_LOADS || no + 1 > MAX_OPS) return -1;
+                        if (la[i] < 0) {
+                            P->loads[nl].which = 0;
+                            P->loads[nl].slice = (uint8_t)(i - 1);
+                            la[i] = nl++ - g.load0;
+                        }
+                        if (lb[j] < 0) {
+                            P->loads[nl].which = 1;
+                            P->loads[nl].slice = (uint8_t)(j - 1);
+                            lb[j] = nl++ - g.load0;
+                        }
+                        Op op;
+                        op.la = (uint8_t)la[i];
+                        op.lb = (uint8_t)lb[j];
+                        op.buf = (uint8_t)pos[u];
+                        op.rel = 0;
+                        P->ops[no++] = op;
+                    }
+                }
+                g.nload = (int16_t)(nl - g.load0);
+                g.nop = (int16_t)(no - g.op0);
+                // release each tile's ring slot after its last use
+                bool seen[2 * S_MAX + 4];
+                for (int q = 0; q < 2 * S_MAX + 4; q++) seen[q] = false;
+                for (int o = no - 1; o >= g.op0; o--) {
+                    if (!seen[P->ops[o].la]) { seen[P->ops[o].la] = true; P->ops[o].rel |= 1; }
+                    if (!seen[P->ops[o].lb]) { seen[P->ops[o].lb] = true; P->ops[o].rel |= 2; }
+                }
+                P->groups[ng++] = g;
             }
         }
     }
-    return n;
+    P->ngroups = ng;
+    return nr;
 }
 
-// One thread: slice count, round table and unit from the statistics.
-// misc: [0] non-finite flag, [1] spread of A x256, [2] spread of B x256.
+// One thread: slice count and the group / round / MMA program from the
+// statistics.  misc: [0] non-finite flag, [1] spread of A x256, [2] of B.
 __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
                        SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
     int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
-    int ubits = 0;
-    int n = plan_rounds(s, Kp, klen_cat, plan->rounds, &ubits);
+    int n = plan_build(s, Kp, klen_cat, plan);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
-    plan->ubits = ubits;
     plan->spread = (float)spread;
     // a plan that does not fit is treated like a non-finite input (plain path)
     plan->nonfinite = (misc[0] != 0 || n < 0) ? 1 : 0;
@@ -360,9 +443,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // 1024-byte alignment for the 128B-swizzled TMA tiles
     unsigned char* smem = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char* sA = smem;
-    unsigned char* sB = smem + STAGES * TILE_BYTES;
-    __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accfull[NBUF], accempty[NBUF], mma_done;
+    unsigned char* sT = smem;  // RING operand tiles of 16 KB
+    __shared__ __align__(8) uint64_t full[RING], empty[RING], accfull[NBUF], accempty[NBUF], mma_done;
     __shared__ uint32_t tmem_base_slot;
     __shared__ int abort_flag;
 
@@ -375,8 +457,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int tiles_n = (p.N + BN - 1) / BN, tiles_m = (p.M + BM - 1) / BM;
     const int ntiles = tiles_n * tiles_m;
 
+    const int ngroups = plan->ngroups;
     if (threadIdx.x == 0) {
-        for (int i = 0; i < STAGES; i++) {
+        for (int i = 0; i < RING; i++) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -404,57 +487,71 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (warp == 0) {
         // ---------------- TMA producer
         if (lane == 0) {
-            int it = 0;
+            int ls = 0;  // tile loads issued (ring position), carried across tiles
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
-                for (int r = 0; r < nrounds && !*(volatile int*)&abort_flag; r++) {
-                    const Round rd = plan->rounds[r];
-                    for (int i = rd.i0; i < rd.i1 && !*(volatile int*)&abort_flag; i++) {
-                        const int j = rd.level - i;
-                        for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
-                            const int s = it % STAGES;
-                            const uint32_t ph = (it / STAGES) & 1;
-                            if (it >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.status, 11)) {
+                for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
+                    const Group G = plan->groups[g];
+                    for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
+                        for (int l = 0; l < G.nload; l++, ls++) {
+                            const Load L = plan->loads[G.load0 + l];
+                            const int s = ls % RING;
+                            if (ls >= RING && !mbar_wait(&empty[s], ((ls / RING) & 1) ^ 1, p.status, 11)) {
                                 abort_flag = 1;
                                 break;
                             }
-                            mbar_arrive_expect_tx(&full[s], 2 * TILE_BYTES);
-                            tma_load_3d(sA + s * TILE_BYTES, &tmA, &full[s], kb * BKB, m0, i - 1);
-                            tma_load_3d(sB + s * TILE_BYTES, &tmB, &full[s], kb * BKB, n0, j - 1);
+                            mbar_arrive_expect_tx(&full[s], TILE_BYTES);
+                            tma_load_3d(sT + s * TILE_BYTES, L.which ? &tmB : &tmA, &full[s], kb * BKB,
+                                        L.which ? n0 : m0, L.slice);
                         }
                     }
                 }
             }
             // drain the copies still in flight (bounded)
-            int first = it > STAGES ? it - STAGES : 0;
-            for (int q = first; q < it; q++) mbar_wait(&full[q % STAGES], (q / STAGES) & 1, nullptr, 0);
+            int first = ls > RING ? ls - RING : 0;
+            for (int q = first; q < ls; q++) mbar_wait(&full[q % RING], (q / RING) & 1, nullptr, 0);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
             constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
-            int it = 0, rg = 0;  // stage and round counters carried across tiles
+            int ls = 0, rg = 0;  // ring and round counters carried across tiles
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
-                for (int r = 0; r < nrounds && !*(volatile int*)&abort_flag; r++, rg++) {
-                    const Round rd = plan->rounds[r];
-                    const int buf = rg % NBUF;
-                    if (rg >= NBUF && !mbar_wait(&accempty[buf], ((rg / NBUF) & 1) ^ 1, p.status, 12)) {
-                        abort_flag = 1;
-                        break;
+                for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
+                    const Group G = plan->groups[g];
+                    // the group's TMEM buffers must have been drained by the epilogue
+                    for (int u = 0; u < G.nr; u++) {
+                        const int rr = rg + u;
+                        if (rr >= NBUF && !mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12)) {
+                            abort_flag = 1;
+                            break;
+                        }
                     }
                     tc_fence_after();
-                    const uint32_t d_tmem = tmem + buf * BN;
-                    bool first = true;
-                    for (int i = rd.i0; i < rd.i1 && !*(volatile int*)&abort_flag; i++) {
-                        for (int kb = rd.kb0; kb < rd.kb1; kb++, it++) {
-                            const int s = it % STAGES;
-                            if (!mbar_wait(&full[s], (it / STAGES) & 1, p.status, 13)) {
+                    bool first0 = true, first1 = true;
+                    for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
+                        int nw = 0;  // loads of this K block already waited for
+                        for (int o = 0; o < G.nop; o++) {
+                            const Op O = plan->ops[G.op0 + o];
+                            const int need = O.la > O.lb ? O.la : O.lb;
+                            bool ok = true;
+                            for (; nw <= need; nw++) {
+                                const int q = ls + nw;
+                                if (!mbar_wait(&full[q % RING], (q / RING) & 1, p.status, 13)) {
+                                    ok = false;
+                                    break;
+                                }
+                            }
+                            if (!ok) {
                                 abort_flag = 1;
                                 break;
                             }
                             tc_fence_after();
-                            const uint64_t da = umma_desc_sw128(sA + s * TILE_BYTES);
-                            const uint64_t db = umma_desc_sw128(sB + s * TILE_BYTES);
+                            const int sa = (ls + O.la) % RING, sb = (ls + O.lb) % RING;
+                            const uint64_t da = umma_desc_sw128(sT + sa * TILE_BYTES);
+                            const uint64_t db = umma_desc_sw128(sT + sb * TILE_BYTES);
+                            const uint32_t d_tmem = tmem + ((rg + O.buf) % NBUF) * BN;
+                            bool& first = O.buf ? first1 : first0;
 #pragma unroll
                             for (int kk = 0; kk < BKB / 32; kk++) {
                                 // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
@@ -462,10 +559,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                                         first ? 0u : 1u);
                                 first = false;
                             }
-                            umma_commit(&empty[s]);
+                            if (O.rel & 1) umma_commit(&empty[sa]);
+                            if (O.rel & 2) umma_commit(&empty[sb]);
                         }
+                        ls += G.nload;
                     }
-                    umma_commit(&accfull[buf]);
+                    for (int u = 0; u < G.nr; u++) umma_commit(&accfull[(rg + u) % NBUF]);
+                    rg += G.nr;
                 }
             }
             umma_commit(&mma_done);
@@ -677,7 +777,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     prm.status = ctx->d_status + F4J_ST_TIMEOUT;
     prm.plan = plan;
 
-    const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024;
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
@@ -838,7 +938,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.C = C;
     prm.status = misc + 8;
     prm.plan = plan;
-    const size_t smem = (size_t)STAGES * 2 * TILE_BYTES + 1024;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024;
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
