@@ -38,6 +38,10 @@ constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns
 constexpr int TILE_BYTES = BM * BKB;  // 16 KB per operand tile
 constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
 constexpr int MAX_ROUNDS = 512, MAX_GROUPS = 320, MAX_LOADS = 4096, MAX_OPS = 2048;
+// Program tables staged in shared memory when they fit (the usual case), so
+// the MMA-issuing thread never waits on a global load between MMAs.
+constexpr int PG_MAX = 128, PO_MAX = 1024, PL_MAX = 2048, PR_MAX = 512;
+constexpr int PROG_BYTES = PG_MAX * 20 + PO_MAX * 4 + PL_MAX * 2 + PR_MAX;
 
 struct Round {
     uint8_t level;   // t = i + j
@@ -479,6 +483,30 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
     }
+    // stage the group / load / MMA program and the round shifts
+    const Group* gp = plan->groups;
+    const Op* opp = plan->ops;
+    const Load* ldp = plan->loads;
+    Group* sg = reinterpret_cast<Group*>(smem + RING * TILE_BYTES);
+    Op* so = reinterpret_cast<Op*>(sg + PG_MAX);
+    Load* sl = reinterpret_cast<Load*>(so + PO_MAX);
+    int8_t* ssh = reinterpret_cast<int8_t*>(sl + PL_MAX);
+    int nops_total = 0, nloads_total = 0;
+    if (ngroups > 0) {
+        const Group last = plan->groups[ngroups - 1];
+        nops_total = last.op0 + last.nop;
+        nloads_total = last.load0 + last.nload;
+    }
+    const bool in_smem = ngroups <= PG_MAX && nops_total <= PO_MAX && nloads_total <= PL_MAX && nrounds <= PR_MAX;
+    if (in_smem) {
+        for (int i = threadIdx.x; i < ngroups; i += blockDim.x) sg[i] = plan->groups[i];
+        for (int i = threadIdx.x; i < nops_total; i += blockDim.x) so[i] = plan->ops[i];
+        for (int i = threadIdx.x; i < nloads_total; i += blockDim.x) sl[i] = plan->loads[i];
+        for (int i = threadIdx.x; i < nrounds; i += blockDim.x) ssh[i] = plan->rounds[i].shift;
+        gp = sg;
+        opp = so;
+        ldp = sl;
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -491,10 +519,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
                 for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
-                    const Group G = plan->groups[g];
+                    const Group G = gp[g];
                     for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
                         for (int l = 0; l < G.nload; l++, ls++) {
-                            const Load L = plan->loads[G.load0 + l];
+                            const Load L = ldp[G.load0 + l];
                             const int s = ls % RING;
                             if (ls >= RING && !mbar_wait(&empty[s], ((ls / RING) & 1) ^ 1, p.status, 11)) {
                                 abort_flag = 1;
@@ -518,7 +546,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             int ls = 0, rg = 0;  // ring and round counters carried across tiles
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
-                    const Group G = plan->groups[g];
+                    const Group G = gp[g];
                     // the group's TMEM buffers must have been drained by the epilogue
                     for (int u = 0; u < G.nr; u++) {
                         const int rr = rg + u;
@@ -532,7 +560,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
                         int nw = 0;  // loads of this K block already waited for
                         for (int o = 0; o < G.nop; o++) {
-                            const Op O = plan->ops[G.op0 + o];
+                            const Op O = opp[G.op0 + o];
                             const int need = O.la > O.lb ? O.la : O.lb;
                             bool ok = true;
                             for (; nw <= need; nw++) {
@@ -595,7 +623,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            const int sh = plan->rounds[r].shift;
+            const int sh = in_smem ? ssh[r] : plan->rounds[r].shift;
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 uint32_t v[32];
@@ -777,7 +805,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     prm.status = ctx->d_status + F4J_ST_TIMEOUT;
     prm.plan = plan;
 
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + PROG_BYTES;
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
@@ -938,7 +966,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.C = C;
     prm.status = misc + 8;
     prm.plan = plan;
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + PROG_BYTES;
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
