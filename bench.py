@@ -42,6 +42,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--case", default="full", choices=["full", "small"])
+    p.add_argument("--n", type=int, default=0, help="override the GEMM size n (profiling)")
     p.add_argument("--skip-extras", action="store_true", help="headline GEMM only (for profiling)")
     p.add_argument("--only-sparse", action="store_true", help="CSR products only (for profiling)")
     return p.parse_args()
@@ -362,7 +363,7 @@ def run_ours(args):
     E = Eng(local)
     L = E.L
     full = args.case == "full"
-    n = 8192 if full else 2048
+    n = args.n if args.n > 0 else (8192 if full else 2048)
     out = {}
 
     # ---- headline: split GEMM n^3, phi = 8
