@@ -212,7 +212,8 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
 // (t, t+1) and each chunk of A-slice indices i, one group holding the round of
 // level t and the round of level t+1 restricted to those i.  Returns the
 // number of rounds, or -1 if a table would overflow.
-__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P) {
+__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int pairing = 1) {
+    const int tstep = pairing ? 2 : 1;  // levels per group
     const int64_t nkb = Kp / BKB;
     int64_t kchunk_blocks = nkb;
     while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
@@ -227,7 +228,7 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
     int nr = 0, ng = 0, nl = 0, no = 0;
     for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
         const int32_t kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
-        for (int t = 2; t <= s + 1; t += 2) {
+        for (int t = 2; t <= s + 1; t += tstep) {
             for (int c0 = 1; c0 <= s; c0 += (int)PP) {
                 const int c1 = c0 + (int)PP - 1 < s ? c0 + (int)PP - 1 : s;
                 if (ng >= MAX_GROUPS || nr + 2 > MAX_ROUNDS) return -1;
@@ -239,7 +240,7 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
                 g.kb0 = (int32_t)kb;
                 g.kb1 = kb1;
                 int lo[2] = {0, 0}, hi[2] = {-1, -1}, pos[2] = {0, 0};
-                for (int u = 0; u < 2; u++) {
+                for (int u = 0; u < tstep; u++) {
                     const int tt = t + u;
                     if (tt > s + 1) continue;
                     int ilo = tt - s > 1 ? tt - s : 1, ihi = tt - 1 < s ? tt - 1 : s;
@@ -305,11 +306,11 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
 // One thread: slice count and the group / round / MMA program from the
 // statistics.  misc: [0] non-finite flag, [1] spread of A x256, [2] of B.
 __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
-                       SplitPlan* __restrict__ plan) {
+                       int pairing, SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
     int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
-    int n = plan_build(s, Kp, klen_cat, plan);
+    int n = plan_build(s, Kp, klen_cat, plan, pairing);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
     plan->spread = (float)spread;
@@ -702,6 +703,12 @@ static int env_slices() {
     return (env && atoi(env) > 0) ? atoi(env) : 0;
 }
 
+// Level pairing in the slice GEMM's schedule (F4J_SPLIT_PAIRING=0 disables it).
+static int env_pairing() {
+    const char* env = getenv("F4J_SPLIT_PAIRING");
+    return (env && env[0] == '0') ? 0 : 1;
+}
+
 static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 
 // Asynchronous split GEMM: statistics -> device plan -> slicing -> slice GEMM,
@@ -771,7 +778,8 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
-    k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(), plan);
+    k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(),
+                                      env_pairing(), plan);
     F4J_LAUNCHED(ctx);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
@@ -935,7 +943,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
                                                                                                  esb, cnb, misc);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
-    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), plan);
+    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_pairing(), plan);
     F4J_CUDA(cudaGetLastError());
     // NaN/Inf operands are rejected, so wait for the plan's verdict
     int hp[4];
