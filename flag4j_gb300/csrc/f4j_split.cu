@@ -34,6 +34,8 @@ constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits ke
 constexpr int BM = 128, BN = 128;  // output tile
 constexpr int BKB = 128;           // K bytes per tile load (one 128B swizzle row)
 constexpr int RING = 12;           // shared-memory ring of operand tiles (A or B slice tiles)
+constexpr int BATCH = 4;           // consecutive tiles sharing one full / empty barrier
+constexpr int NBATCH = RING / BATCH;
 constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns
 constexpr int TILE_BYTES = BM * BKB;  // 16 KB per operand tile
 constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
@@ -449,7 +451,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     unsigned char* smem = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char* sT = smem;  // RING operand tiles of 16 KB
-    __shared__ __align__(8) uint64_t full[RING], empty[RING], accfull[NBUF], accempty[NBUF], mma_done;
+    __shared__ __align__(8) uint64_t full[NBATCH], empty[NBATCH], accfull[NBUF], accempty[NBUF], mma_done;
     __shared__ uint32_t tmem_base_slot;
     __shared__ int abort_flag;
 
@@ -464,7 +466,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
     const int ngroups = plan->ngroups;
     if (threadIdx.x == 0) {
-        for (int i = 0; i < RING; i++) {
+        for (int i = 0; i < NBATCH; i++) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -499,6 +501,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         nloads_total = last.load0 + last.nload;
     }
     const bool in_smem = ngroups <= PG_MAX && nops_total <= PO_MAX && nloads_total <= PL_MAX && nrounds <= PR_MAX;
+    // tile loads this CTA will issue in total (sizes the last, partial batch)
+    int loads_per_tile = 0;
+    for (int g = 0; g < ngroups; g++) loads_per_tile += plan->groups[g].nload * (plan->groups[g].kb1 - plan->groups[g].kb0);
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const int total_loads = loads_per_tile * my_tiles;
     if (in_smem) {
         for (int i = threadIdx.x; i < ngroups; i += blockDim.x) sg[i] = plan->groups[i];
         for (int i = threadIdx.x; i < nops_total; i += blockDim.x) so[i] = plan->ops[i];
@@ -524,27 +531,35 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
                         for (int l = 0; l < G.nload; l++, ls++) {
                             const Load L = ldp[G.load0 + l];
-                            const int s = ls % RING;
-                            if (ls >= RING && !mbar_wait(&empty[s], ((ls / RING) & 1) ^ 1, p.status, 11)) {
-                                abort_flag = 1;
-                                break;
+                            const int b = ls / BATCH, bs = b % NBATCH;
+                            if (ls % BATCH == 0) {
+                                // first tile of a batch: wait for the batch slot, then
+                                // expect all of the batch's bytes on its one barrier
+                                if (b >= NBATCH && !mbar_wait(&empty[bs], ((b / NBATCH) & 1) ^ 1, p.status, 11)) {
+                                    abort_flag = 1;
+                                    break;
+                                }
+                                const int cnt = total_loads - ls < BATCH ? total_loads - ls : BATCH;
+                                mbar_arrive_expect_tx(&full[bs], cnt * TILE_BYTES);
                             }
-                            mbar_arrive_expect_tx(&full[s], TILE_BYTES);
-                            tma_load_3d(sT + s * TILE_BYTES, L.which ? &tmB : &tmA, &full[s], kb * BKB,
+                            tma_load_3d(sT + (ls % RING) * TILE_BYTES, L.which ? &tmB : &tmA, &full[bs], kb * BKB,
                                         L.which ? n0 : m0, L.slice);
                         }
                     }
                 }
             }
             // drain the copies still in flight (bounded)
-            int first = ls > RING ? ls - RING : 0;
-            for (int q = first; q < ls; q++) mbar_wait(&full[q % RING], (q / RING) & 1, nullptr, 0);
+            const int nb = (ls + BATCH - 1) / BATCH;
+            for (int q = nb > NBATCH ? nb - NBATCH : 0; q < nb; q++)
+                mbar_wait(&full[q % NBATCH], (q / NBATCH) & 1, nullptr, 0);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
             constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
-            int ls = 0, rg = 0;  // ring and round counters carried across tiles
+            int ls = 0, rg = 0, wb = 0;  // ring, round and waited-batch counters carried across tiles
+            int relcnt[NBATCH];
+            for (int i = 0; i < NBATCH; i++) relcnt[i] = 0;
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
                     const Group G = gp[g];
@@ -559,14 +574,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     tc_fence_after();
                     bool first0 = true, first1 = true;
                     for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
-                        int nw = 0;  // loads of this K block already waited for
                         for (int o = 0; o < G.nop; o++) {
                             const Op O = opp[G.op0 + o];
-                            const int need = O.la > O.lb ? O.la : O.lb;
+                            const int need_batch = (ls + (O.la > O.lb ? O.la : O.lb)) / BATCH;
                             bool ok = true;
-                            for (; nw <= need; nw++) {
-                                const int q = ls + nw;
-                                if (!mbar_wait(&full[q % RING], (q / RING) & 1, p.status, 13)) {
+                            for (; wb <= need_batch; wb++) {
+                                if (!mbar_wait(&full[wb % NBATCH], (wb / NBATCH) & 1, p.status, 13)) {
                                     ok = false;
                                     break;
                                 }
@@ -588,8 +601,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                                         first ? 0u : 1u);
                                 first = false;
                             }
-                            if (O.rel & 1) umma_commit(&empty[sa]);
-                            if (O.rel & 2) umma_commit(&empty[sb]);
+                            // a batch's slots are released (one commit) after the last
+                            // use of all of its tiles
+                            for (int side = 0; side < 2; side++) {
+                                if (!(O.rel & (1 << side))) continue;
+                                const int q = ls + (side ? O.lb : O.la);
+                                const int b = q / BATCH, bs = b % NBATCH;
+                                const int cnt = total_loads - b * BATCH < BATCH ? total_loads - b * BATCH : BATCH;
+                                if (++relcnt[bs] == cnt) {
+                                    relcnt[bs] = 0;
+                                    umma_commit(&empty[bs]);
+                                }
+                            }
                         }
                         ls += G.nload;
                     }
