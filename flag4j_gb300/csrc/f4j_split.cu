@@ -43,7 +43,7 @@ constexpr int MAX_ROUNDS = 512, MAX_GROUPS = 320, MAX_LOADS = 4096, MAX_OPS = 20
 // Program tables staged in shared memory when they fit (the usual case), so
 // the MMA-issuing thread never waits on a global load between MMAs.
 constexpr int PG_MAX = 128, PO_MAX = 1024, PL_MAX = 2048, PR_MAX = 512;
-constexpr int PROG_BYTES = PG_MAX * 20 + PO_MAX * 4 + PL_MAX * 2 + PR_MAX;
+constexpr int PROG_BYTES = PG_MAX * 24 + PO_MAX * 4 + PL_MAX * 2 + PR_MAX;
 
 struct Round {
     uint8_t level;   // t = i + j
@@ -70,7 +70,10 @@ struct Group {
     int16_t load0, nload;  // load list (per K block)
     int16_t op0, nop;      // MMA list (per K block)
     int32_t kb0, kb1;      // K blocks
+    int32_t flags;         // GF_CONT_IN: keeps accumulating into the previous group's
+                           // buffers; GF_CONT_OUT: its rounds continue in the next group
 };
+constexpr int GF_CONT_IN = 1, GF_CONT_OUT = 2;
 
 // Decided on the device from the exponent statistics (k_plan), so a split
 // GEMM never waits for the host between its kernels.
@@ -214,7 +217,8 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
 // (t, t+1) and each chunk of A-slice indices i, one group holding the round of
 // level t and the round of level t+1 restricted to those i.  Returns the
 // number of rounds, or -1 if a table would overflow.
-__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int pairing = 1) {
+__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int pairing = 1,
+                                          int order = 1) {
     const int tstep = pairing ? 2 : 1;  // levels per group
     const int64_t nkb = Kp / BKB;
     int64_t kchunk_blocks = nkb;
@@ -262,42 +266,61 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
                     P->rounds[nr++] = rd;
                 }
                 if (g.nr == 0) continue;
-                // zig-zag: for each i, the level t+1 product then the level t product
-                int la[S_MAX + 2], lb[S_MAX + 2];
-                for (int q = 0; q < S_MAX + 2; q++) la[q] = lb[q] = -1;
-                for (int i = c0; i <= c1; i++) {
-                    for (int u = 1; u >= 0; u--) {
-                        if (i < lo[u] || i > hi[u]) continue;
-                        const int j = t + u - i;
-                        if (nl + 2 > MAX_LOADS || no + 1 > MAX_OPS) return -1;
-                        if (la[i] < 0) {
-                            P->loads[nl].which = 0;
-                            P->loads[nl].slice = (uint8_t)(i - 1);
-                            la[i] = nl++ - g.load0;
-                        }
-                        if (lb[j] < 0) {
-                            P->loads[nl].which = 1;
-                            P->loads[nl].slice = (uint8_t)(j - 1);
-                            lb[j] = nl++ - g.load0;
-                        }
-                        Op op;
-                        op.la = (uint8_t)la[i];
-                        op.lb = (uint8_t)lb[j];
-                        op.buf = (uint8_t)pos[u];
-                        op.rel = 0;
-                        P->ops[no++] = op;
+                // i range with at least one product (the levels' ranges overlap or touch)
+                int iu0 = s + 1, iu1 = 0;
+                for (int u = 0; u < tstep; u++)
+                    if (lo[u] <= hi[u]) {
+                        iu0 = lo[u] < iu0 ? lo[u] : iu0;
+                        iu1 = hi[u] > iu1 ? hi[u] : iu1;
                     }
+                // order 0: one group for all i (per K block every tile of the round
+                // set once); order 1: one group per i, each streaming all K blocks
+                // of its two or three slice planes before the next i
+                for (int ga = iu0; ga <= iu1;) {
+                    const int gb = order ? ga : iu1;
+                    if (ng >= MAX_GROUPS) return -1;
+                    Group h = g;
+                    h.load0 = (int16_t)nl;
+                    h.op0 = (int16_t)no;
+                    h.flags = (ga > iu0 ? GF_CONT_IN : 0) | (gb < iu1 ? GF_CONT_OUT : 0);
+                    // zig-zag: for each i, the level t+1 product then the level t product
+                    int la[S_MAX + 2], lb[S_MAX + 2];
+                    for (int q = 0; q < S_MAX + 2; q++) la[q] = lb[q] = -1;
+                    for (int i = ga; i <= gb; i++) {
+                        for (int u = 1; u >= 0; u--) {
+                            if (i < lo[u] || i > hi[u]) continue;
+                            const int j = t + u - i;
+                            if (nl + 2 > MAX_LOADS || no + 1 > MAX_OPS) return -1;
+                            if (la[i] < 0) {
+                                P->loads[nl].which = 0;
+                                P->loads[nl].slice = (uint8_t)(i - 1);
+                                la[i] = nl++ - h.load0;
+                            }
+                            if (lb[j] < 0) {
+                                P->loads[nl].which = 1;
+                                P->loads[nl].slice = (uint8_t)(j - 1);
+                                lb[j] = nl++ - h.load0;
+                            }
+                            Op op;
+                            op.la = (uint8_t)la[i];
+                            op.lb = (uint8_t)lb[j];
+                            op.buf = (uint8_t)pos[u];
+                            op.rel = 0;
+                            P->ops[no++] = op;
+                        }
+                    }
+                    h.nload = (int16_t)(nl - h.load0);
+                    h.nop = (int16_t)(no - h.op0);
+                    // release each tile's ring slot after its last use
+                    bool seen[2 * S_MAX + 4];
+                    for (int q = 0; q < 2 * S_MAX + 4; q++) seen[q] = false;
+                    for (int o = no - 1; o >= h.op0; o--) {
+                        if (!seen[P->ops[o].la]) { seen[P->ops[o].la] = true; P->ops[o].rel |= 1; }
+                        if (!seen[P->ops[o].lb]) { seen[P->ops[o].lb] = true; P->ops[o].rel |= 2; }
+                    }
+                    P->groups[ng++] = h;
+                    ga = gb + 1;
                 }
-                g.nload = (int16_t)(nl - g.load0);
-                g.nop = (int16_t)(no - g.op0);
-                // release each tile's ring slot after its last use
-                bool seen[2 * S_MAX + 4];
-                for (int q = 0; q < 2 * S_MAX + 4; q++) seen[q] = false;
-                for (int o = no - 1; o >= g.op0; o--) {
-                    if (!seen[P->ops[o].la]) { seen[P->ops[o].la] = true; P->ops[o].rel |= 1; }
-                    if (!seen[P->ops[o].lb]) { seen[P->ops[o].lb] = true; P->ops[o].rel |= 2; }
-                }
-                P->groups[ng++] = g;
             }
         }
     }
@@ -308,11 +331,11 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
 // One thread: slice count and the group / round / MMA program from the
 // statistics.  misc: [0] non-finite flag, [1] spread of A x256, [2] of B.
 __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
-                       int pairing, SplitPlan* __restrict__ plan) {
+                       int pairing, int order, SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
     int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
-    int n = plan_build(s, Kp, klen_cat, plan, pairing);
+    int n = plan_build(s, Kp, klen_cat, plan, pairing, order);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
     plan->spread = (float)spread;
@@ -560,19 +583,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             int ls = 0, rg = 0, wb = 0;  // ring, round and waited-batch counters carried across tiles
             int relcnt[NBATCH];
             for (int i = 0; i < NBATCH; i++) relcnt[i] = 0;
+            bool first0 = true, first1 = true;  // next MMA into buffer 0 / 1 of the round set overwrites
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
                     const Group G = gp[g];
-                    // the group's TMEM buffers must have been drained by the epilogue
-                    for (int u = 0; u < G.nr; u++) {
-                        const int rr = rg + u;
-                        if (rr >= NBUF && !mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12)) {
-                            abort_flag = 1;
-                            break;
+                    if (!(G.flags & GF_CONT_IN)) {
+                        // the group's TMEM buffers must have been drained by the epilogue
+                        for (int u = 0; u < G.nr; u++) {
+                            const int rr = rg + u;
+                            if (rr >= NBUF && !mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12)) {
+                                abort_flag = 1;
+                                break;
+                            }
                         }
+                        tc_fence_after();
+                        first0 = first1 = true;
                     }
-                    tc_fence_after();
-                    bool first0 = true, first1 = true;
                     for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
                         for (int o = 0; o < G.nop; o++) {
                             const Op O = opp[G.op0 + o];
@@ -616,8 +642,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                         }
                         ls += G.nload;
                     }
-                    for (int u = 0; u < G.nr; u++) umma_commit(&accfull[(rg + u) % NBUF]);
-                    rg += G.nr;
+                    if (!(G.flags & GF_CONT_OUT)) {
+                        for (int u = 0; u < G.nr; u++) umma_commit(&accfull[(rg + u) % NBUF]);
+                        rg += G.nr;
+                    }
                 }
             }
             umma_commit(&mma_done);
@@ -732,6 +760,14 @@ static int env_pairing() {
     return (env && env[0] == '0') ? 0 : 1;
 }
 
+// Schedule order of the slice GEMM (F4J_SPLIT_ORDER): 1 (default) streams all K
+// blocks of one A slice with its partner B slices before the next; 0 walks
+// every slice tile of a round set per K block.
+static int env_order() {
+    const char* env = getenv("F4J_SPLIT_ORDER");
+    return (env && env[0] == '0') ? 0 : 1;
+}
+
 static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 
 // Asynchronous split GEMM: statistics -> device plan -> slicing -> slice GEMM,
@@ -802,7 +838,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
     k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(),
-                                      env_pairing(), plan);
+                                      env_pairing(), env_order(), plan);
     F4J_LAUNCHED(ctx);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
@@ -966,7 +1002,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
                                                                                                  esb, cnb, misc);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
-    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_pairing(), plan);
+    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_pairing(), env_order(), plan);
     F4J_CUDA(cudaGetLastError());
     // NaN/Inf operands are rejected, so wait for the plan's verdict
     int hp[4];
