@@ -455,6 +455,17 @@ __global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int
 }
 
 // ------------------------------------------------------------------ GEMM
+// Development tracing (built only with -DF4J_TRACE): per-role cycle counts of
+// the slice GEMM's barrier waits, summed over CTAs, read by f4j_debug_trace.
+#ifdef F4J_TRACE
+__device__ unsigned long long g_f4j_trace[8];
+#define F4J_T_BEGIN() const long long f4j_t0 = clock64()
+#define F4J_T_ADD(acc) (acc) += (unsigned long long)(clock64() - f4j_t0)
+#else
+#define F4J_T_BEGIN() ((void)0)
+#define F4J_T_ADD(acc) ((void)0)
+#endif
+
 // v * 2^X without a libm call; two in-range factors when X leaves the normal range.
 __device__ __forceinline__ double scale_pow2(double v, int X) {
     if (X >= -1022 && X <= 1023) return v * __longlong_as_double((long long)(X + 1023) << 52);
@@ -546,6 +557,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (warp == 0) {
         // ---------------- TMA producer
         if (lane == 0) {
+#ifdef F4J_TRACE
+            unsigned long long tr_wait = 0;
+            const long long tr_start = clock64();
+#endif
             int ls = 0;  // tile loads issued (ring position), carried across tiles
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
                 const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
@@ -558,7 +573,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                             if (ls % BATCH == 0) {
                                 // first tile of a batch: wait for the batch slot, then
                                 // expect all of the batch's bytes on its one barrier
-                                if (b >= NBATCH && !mbar_wait(&empty[bs], ((b / NBATCH) & 1) ^ 1, p.status, 11)) {
+                                F4J_T_BEGIN();
+                                const bool okw = b < NBATCH || mbar_wait(&empty[bs], ((b / NBATCH) & 1) ^ 1, p.status, 11);
+                                F4J_T_ADD(tr_wait);
+                                if (!okw) {
                                     abort_flag = 1;
                                     break;
                                 }
@@ -571,6 +589,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     }
                 }
             }
+#ifdef F4J_TRACE
+            atomicAdd(&g_f4j_trace[4], (unsigned long long)(clock64() - tr_start));
+            atomicAdd(&g_f4j_trace[5], tr_wait);
+#endif
             // drain the copies still in flight (bounded)
             const int nb = (ls + BATCH - 1) / BATCH;
             for (int q = nb > NBATCH ? nb - NBATCH : 0; q < nb; q++)
@@ -580,6 +602,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
             constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
+#ifdef F4J_TRACE
+            unsigned long long tr_wait = 0, tr_acc = 0, tr_ops = 0;
+            const long long tr_start = clock64();
+#endif
             int ls = 0, rg = 0, wb = 0;  // ring, round and waited-batch counters carried across tiles
             int relcnt[NBATCH];
             for (int i = 0; i < NBATCH; i++) relcnt[i] = 0;
@@ -591,7 +617,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                         // the group's TMEM buffers must have been drained by the epilogue
                         for (int u = 0; u < G.nr; u++) {
                             const int rr = rg + u;
-                            if (rr >= NBUF && !mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12)) {
+                            F4J_T_BEGIN();
+                            const bool okw = rr < NBUF || mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12);
+                            F4J_T_ADD(tr_acc);
+                            if (!okw) {
                                 abort_flag = 1;
                                 break;
                             }
@@ -605,7 +634,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                             const int need_batch = (ls + (O.la > O.lb ? O.la : O.lb)) / BATCH;
                             bool ok = true;
                             for (; wb <= need_batch; wb++) {
-                                if (!mbar_wait(&full[wb % NBATCH], (wb / NBATCH) & 1, p.status, 13)) {
+                                F4J_T_BEGIN();
+                                const bool okw = mbar_wait(&full[wb % NBATCH], (wb / NBATCH) & 1, p.status, 13);
+                                F4J_T_ADD(tr_wait);
+                                if (!okw) {
                                     ok = false;
                                     break;
                                 }
@@ -615,6 +647,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                                 break;
                             }
                             tc_fence_after();
+#ifdef F4J_TRACE
+                            tr_ops++;
+#endif
                             const int sa = (ls + O.la) % RING, sb = (ls + O.lb) % RING;
                             const uint64_t da = umma_desc_sw128(sT + sa * TILE_BYTES);
                             const uint64_t db = umma_desc_sw128(sT + sb * TILE_BYTES);
@@ -648,6 +683,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     }
                 }
             }
+#ifdef F4J_TRACE
+            atomicAdd(&g_f4j_trace[0], (unsigned long long)(clock64() - tr_start));
+            atomicAdd(&g_f4j_trace[1], tr_wait);
+            atomicAdd(&g_f4j_trace[2], tr_acc);
+            atomicAdd(&g_f4j_trace[3], tr_ops);
+#endif
             umma_commit(&mma_done);
             mbar_wait(&mma_done, 0, p.status, 14);
         }
@@ -657,6 +698,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const int h = (warp - 2) / 4;    // column half of the tile
         const int ubits = plan->ubits;
         int rg = 0;
+#ifdef F4J_TRACE
+        unsigned long long tr_wait = 0;
+        const long long tr_start = clock64();
+#endif
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
         const int row = m0 + 32 * q + lane;
@@ -667,7 +712,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int r = 0; r < nrounds; r++, rg++) {
             const int buf = rg % NBUF;
             bool w = true;
-            if (lane == 0) w = mbar_wait(&accfull[buf], (rg / NBUF) & 1, p.status, 15);
+            {
+                F4J_T_BEGIN();
+                if (lane == 0) w = mbar_wait(&accfull[buf], (rg / NBUF) & 1, p.status, 15);
+                F4J_T_ADD(tr_wait);
+            }
             w = __shfl_sync(0xffffffffu, w, 0);
             if (!w || *(volatile int*)&abort_flag) {
                 ok = false;
@@ -722,6 +771,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             }
         }
         }  // tile loop
+#ifdef F4J_TRACE
+        if (warp == 2 && lane == 0) {
+            atomicAdd(&g_f4j_trace[6], (unsigned long long)(clock64() - tr_start));
+            atomicAdd(&g_f4j_trace[7], tr_wait);
+        }
+#endif
     }
     tc_fence_before();
     __syncthreads();
@@ -1042,3 +1097,17 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     if (slices_out) *slices_out = hp[0];
     return F4J_OK;
 }
+
+#ifdef F4J_TRACE
+// Development build only: returns and clears the slice GEMM's trace counters
+// (cycles summed over CTAs): [0] MMA thread total, [1] its full-barrier
+// waits, [2] its accumulator-buffer waits, [3] MMA ops issued, [4] producer
+// total, [5] producer slot waits, [6] epilogue total, [7] epilogue waits.
+extern "C" int f4j_debug_trace(unsigned long long* out8) {
+    F4J_CUDA(cudaDeviceSynchronize());
+    F4J_CUDA(cudaMemcpyFromSymbol(out8, g_f4j_trace, 8 * sizeof(unsigned long long)));
+    unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    F4J_CUDA(cudaMemcpyToSymbol(g_f4j_trace, z, sizeof z));
+    return F4J_OK;
+}
+#endif
