@@ -155,6 +155,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 32 lanes x 32 columns of 32-bit TMEM words set to zero.
+__device__ __forceinline__ void tmem_zero32(uint32_t taddr) {
+    const uint32_t z = 0;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // Shared-memory matrix descriptor for a K-major operand tile written by TMA
 // with 128-byte swizzle: rows of 128 bytes, 8-row swizzle atoms 1024 bytes
 // apart (stride byte offset), leading byte offset unused for this layout.
@@ -166,6 +179,18 @@ __device__ __forceinline__ uint64_t umma_desc_sw128(const void* smem_tile) {
     d |= (uint64_t)(1024 >> 4) << 32;       // bits 32-45: stride byte offset >> 4
     d |= (uint64_t)1 << 46;                 // bits 46-47: descriptor version (sm_100 family)
     d |= (uint64_t)2 << 61;                 // bits 61-63: swizzle mode 2 = 128-byte
+    return d;
+}
+
+// Same for 64-byte rows written with 64-byte swizzle: 8-row atoms of 512 bytes.
+__device__ __forceinline__ uint64_t umma_desc_sw64(const void* smem_tile) {
+    uint64_t addr = smem_u32(smem_tile);
+    uint64_t d = 0;
+    d |= (addr & 0x3FFFFull) >> 4;          // bits 0-13: start address >> 4
+    d |= (uint64_t)(16 >> 4) << 16;         // bits 16-29: leading byte offset >> 4 (ignored)
+    d |= (uint64_t)(512 >> 4) << 32;        // bits 32-45: stride byte offset >> 4
+    d |= (uint64_t)1 << 46;                 // bits 46-47: descriptor version (sm_100 family)
+    d |= (uint64_t)4 << 61;                 // bits 61-63: swizzle mode 4 = 64-byte
     return d;
 }
 

@@ -32,59 +32,65 @@ namespace {
 
 constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits keeps Y < 2^62 in int64
 constexpr int BM = 128, BN = 128;  // output tile
-constexpr int BKB = 128;           // K bytes per tile load (one 128B swizzle row)
-constexpr int RING = 12;           // shared-memory ring of operand tiles (A or B slice tiles)
-constexpr int BATCH = 4;           // consecutive tiles sharing one full / empty barrier
-constexpr int NBATCH = RING / BATCH;
-constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns
-constexpr int TILE_BYTES = BM * BKB;  // 16 KB per operand tile
+constexpr int BKB = 64;            // K bytes per tile load (one 64-byte swizzle row)
+constexpr int STAGE_TILES = 11;    // operand tiles per stage: 2w + band - 1 for w A slices
+constexpr int NSTAGE = 2;          // stages in the shared-memory ring
+constexpr int RING = STAGE_TILES * NSTAGE;
+constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns (= levels per band)
+constexpr int TILE_BYTES = BM * BKB;  // 8 KB per operand tile
 constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
-constexpr int MAX_ROUNDS = 512, MAX_GROUPS = 320, MAX_LOADS = 4096, MAX_OPS = 2048;
-// Program tables staged in shared memory when they fit (the usual case), so
-// the MMA-issuing thread never waits on a global load between MMAs.
-constexpr int PG_MAX = 128, PO_MAX = 1024, PL_MAX = 2048, PR_MAX = 512;
-constexpr int PROG_BYTES = PG_MAX * 24 + PO_MAX * 4 + PL_MAX * 2 + PR_MAX;
+constexpr int MAX_ROUNDS = 16, MAX_GROUPS = 64, MAX_LOADS = 512, MAX_OPS = 256;
 
+// One round: the products A_i B_j of weight level t = i + j over one K chunk,
+// accumulated in one TMEM buffer.
 struct Round {
     uint8_t level;   // t = i + j
     uint8_t i0, i1;  // A slices i0..i1-1 (1-based), B slice t - i
     int8_t shift;    // left shift of this round's integer into the fixed-point accumulator
-    int32_t kb0, kb1;  // K blocks [kb0, kb1)
+    uint8_t buf;     // TMEM buffer: level - t0 of its band
+    uint8_t pad[3];
 };
 
-// A group runs one or two rounds of adjacent levels together: per K block
-// it loads each needed slice tile once and issues the rounds' MMAs in
-// zig-zag order (A_i B_{t+1-i}, A_i B_{t-i}, A_{i+1} B_{t-i}, ...), so a tile
-// feeds up to two MMAs before its ring slot is released.
+// A band is up to NBUF adjacent levels t0..t1, level t in TMEM buffer t - t0
+// (columns (t - t0) * BN ...).  Its products are computed by groups, one per
+// chunk of w consecutive A slices i: per K block a group loads A_i for its i
+// and every B_j with t0 <= i + j <= t1 (one ring stage of at most STAGE_TILES
+// tiles, B tiles in ascending j) and issues each of those products into its
+// level's buffer, so a loaded tile feeds up to NBUF products.  Two products
+// A_i B_j, A_i B_{j+1} of an even and the next odd buffer run as one N = 256
+// MMA: B_j and B_{j+1} are adjacent in shared memory and their buffers
+// adjacent in TMEM.  Consecutive groups of a band keep accumulating into the
+// same buffers, which the epilogue zeroes after reading them.
 struct Load {
     uint8_t which;  // 0: A slice tile, 1: B slice tile
     uint8_t slice;  // 0-based slice plane
 };
 struct Op {
-    uint8_t la, lb;  // indices of the A and B tiles in the group's load list
-    uint8_t buf;     // 0: the group's first round, 1: its second
-    uint8_t rel;     // bit 0: last use of A tile, bit 1: last use of B tile
+    uint16_t a_off, b_off;  // A / B tile offsets in the stage, in 16-byte units (descriptor address field)
+    uint16_t dcol;          // TMEM column of the first product's buffer
+    uint16_t wide;          // 1: N = 256 (B tiles b, b+1 into buffers dcol / BN and the next)
 };
 struct Group {
     int16_t r0, nr;        // rounds [r0, r0 + nr)
     int16_t load0, nload;  // load list (per K block)
     int16_t op0, nop;      // MMA list (per K block)
-    int32_t kb0, kb1;      // K blocks
     int32_t flags;         // GF_CONT_IN: keeps accumulating into the previous group's
                            // buffers; GF_CONT_OUT: its rounds continue in the next group
 };
 constexpr int GF_CONT_IN = 1, GF_CONT_OUT = 2;
 
 // Decided on the device from the exponent statistics (k_plan), so a split
-// GEMM never waits for the host between its kernels.
+// GEMM never waits for the host between its kernels.  The group / round
+// program covers one K chunk; the slice GEMM runs it once per chunk.
 struct SplitPlan {
     int s;          // slices per operand
-    int nrounds;
+    int nrounds;    // rounds per K chunk
     int ubits;      // fixed-point unit exponent: value = acc * 2^(ubits + ea + eb)
     int nonfinite;  // a NaN/Inf was seen (or no plan fits): the split stands down
     float spread;   // measured exponent spread (bits)
-    int ngroups;
-    int pad[2];
+    int ngroups;    // groups per K chunk
+    int nkb;        // K blocks of BKB bytes
+    int kcb;        // K blocks per chunk
     Round rounds[MAX_ROUNDS];
     Group groups[MAX_GROUPS];
     Load loads[MAX_LOADS];
@@ -92,7 +98,7 @@ struct SplitPlan {
 };
 
 struct SplitGemmParams {
-    int M, N, Kp;           // cat sizes; Kp multiple of 128
+    int M, N, Kp;           // cat sizes; Kp multiple of BKB
     int cplx;               // 1: C interleaved complex, N = 2n
     int n_out;              // n (complex output columns) or N
     const int* ea;          // [M]
@@ -209,119 +215,88 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
     return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
 }
 
-// Round table: products A_i B_j with i + j = t (weight level t) accumulate in
-// one TMEM buffer as long as pairs * kchunk * 16 * 16 <= 2^24, which keeps the
-// FP32 accumulator an exact integer; larger levels / K are split into rounds.
-// The fixed-point unit keeps the worst-case accumulator below 2^62.
-// Rounds are emitted group by group: for each K chunk, each level pair
-// (t, t+1) and each chunk of A-slice indices i, one group holding the round of
-// level t and the round of level t+1 restricted to those i.  Returns the
-// number of rounds, or -1 if a table would overflow.
-__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int pairing = 1,
-                                          int order = 1) {
-    const int tstep = pairing ? 2 : 1;  // levels per group
+// Round program: a round accumulates the pairs of one level over one K chunk
+// in FP32, exact as long as pairs * kchunk * 16 * 16 <= 2^24; a level has at
+// most s pairs, so the chunk is the largest power-of-two number of K blocks
+// with s * kchunk * 256 <= 2^24.  The fixed-point unit keeps the worst-case
+// accumulator below 2^62.  Levels 2..s+1 are cut into bands of `band`
+// (<= NBUF) levels, the first band taking the remainder; each band's A-slice range is cut into chunks of
+// w = (STAGE_TILES - band + 1) / 2 slices, one group each, so a group loads
+// at most 2w + band - 1 <= STAGE_TILES tiles per K block.  Returns the
+// number of rounds per chunk, or -1 if a table would overflow.
+__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int band = NBUF) {
+    if (band < 1) band = 1;
+    if (band > NBUF) band = NBUF;
+    const int w = (STAGE_TILES - band + 1) / 2;
     const int64_t nkb = Kp / BKB;
-    int64_t kchunk_blocks = nkb;
-    while (kchunk_blocks > 1 && kchunk_blocks * BKB * 256 > (1ll << 24)) kchunk_blocks = (kchunk_blocks + 1) / 2;
-    const int64_t kchunk = kchunk_blocks * BKB;
-    int64_t PP = (1ll << 24) / (kchunk * 256);  // pairs per round
-    if (PP < 1) PP = 1;
+    int64_t kcb = 1;
+    while (2 * kcb <= nkb && (int64_t)s * (2 * kcb) * BKB * 256 <= (1ll << 24)) kcb *= 2;
+    P->nkb = (int)nkb;
+    P->kcb = (int)kcb;
     int kbits = 0;
     while (kbits < 62 && (1ll << kbits) < (klen_cat > 0 ? klen_cat : 1)) kbits++;  // ceil(log2 k)
     int D = kbits + 9 + 5 * (s - 1) - 62;
     if (D < 0) D = 0;
     P->ubits = -(8 + 5 * (s - 1)) + D;
     int nr = 0, ng = 0, nl = 0, no = 0;
-    for (int64_t kb = 0; kb < nkb; kb += kchunk_blocks) {
-        const int32_t kb1 = (int32_t)(kb + kchunk_blocks < nkb ? kb + kchunk_blocks : nkb);
-        for (int t = 2; t <= s + 1; t += tstep) {
-            for (int c0 = 1; c0 <= s; c0 += (int)PP) {
-                const int c1 = c0 + (int)PP - 1 < s ? c0 + (int)PP - 1 : s;
-                if (ng >= MAX_GROUPS || nr + 2 > MAX_ROUNDS) return -1;
-                Group g;
-                g.r0 = (int16_t)nr;
-                g.nr = 0;
-                g.load0 = (int16_t)nl;
-                g.op0 = (int16_t)no;
-                g.kb0 = (int32_t)kb;
-                g.kb1 = kb1;
-                int lo[2] = {0, 0}, hi[2] = {-1, -1}, pos[2] = {0, 0};
-                for (int u = 0; u < tstep; u++) {
-                    const int tt = t + u;
-                    if (tt > s + 1) continue;
-                    int ilo = tt - s > 1 ? tt - s : 1, ihi = tt - 1 < s ? tt - 1 : s;
-                    if (ilo < c0) ilo = c0;
-                    if (ihi > c1) ihi = c1;
-                    if (ilo > ihi) continue;
-                    lo[u] = ilo;
-                    hi[u] = ihi;
-                    pos[u] = g.nr++;
-                    Round rd;
-                    rd.level = (uint8_t)tt;
-                    rd.i0 = (uint8_t)ilo;
-                    rd.i1 = (uint8_t)(ihi + 1);
-                    rd.shift = (int8_t)(5 * (s + 1 - tt) - D);
-                    rd.kb0 = (int32_t)kb;
-                    rd.kb1 = kb1;
-                    P->rounds[nr++] = rd;
-                }
-                if (g.nr == 0) continue;
-                // i range with at least one product (the levels' ranges overlap or touch)
-                int iu0 = s + 1, iu1 = 0;
-                for (int u = 0; u < tstep; u++)
-                    if (lo[u] <= hi[u]) {
-                        iu0 = lo[u] < iu0 ? lo[u] : iu0;
-                        iu1 = hi[u] > iu1 ? hi[u] : iu1;
-                    }
-                // order 0: one group for all i (per K block every tile of the round
-                // set once); order 1: one group per i, each streaming all K blocks
-                // of its two or three slice planes before the next i
-                for (int ga = iu0; ga <= iu1;) {
-                    const int gb = order ? ga : iu1;
-                    if (ng >= MAX_GROUPS) return -1;
-                    Group h = g;
-                    h.load0 = (int16_t)nl;
-                    h.op0 = (int16_t)no;
-                    h.flags = (ga > iu0 ? GF_CONT_IN : 0) | (gb < iu1 ? GF_CONT_OUT : 0);
-                    // zig-zag: for each i, the level t+1 product then the level t product
-                    int la[S_MAX + 2], lb[S_MAX + 2];
-                    for (int q = 0; q < S_MAX + 2; q++) la[q] = lb[q] = -1;
-                    for (int i = ga; i <= gb; i++) {
-                        for (int u = 1; u >= 0; u--) {
-                            if (i < lo[u] || i > hi[u]) continue;
-                            const int j = t + u - i;
-                            if (nl + 2 > MAX_LOADS || no + 1 > MAX_OPS) return -1;
-                            if (la[i] < 0) {
-                                P->loads[nl].which = 0;
-                                P->loads[nl].slice = (uint8_t)(i - 1);
-                                la[i] = nl++ - h.load0;
-                            }
-                            if (lb[j] < 0) {
-                                P->loads[nl].which = 1;
-                                P->loads[nl].slice = (uint8_t)(j - 1);
-                                lb[j] = nl++ - h.load0;
-                            }
-                            Op op;
-                            op.la = (uint8_t)la[i];
-                            op.lb = (uint8_t)lb[j];
-                            op.buf = (uint8_t)pos[u];
-                            op.rel = 0;
-                            P->ops[no++] = op;
-                        }
-                    }
-                    h.nload = (int16_t)(nl - h.load0);
-                    h.nop = (int16_t)(no - h.op0);
-                    // release each tile's ring slot after its last use
-                    bool seen[2 * S_MAX + 4];
-                    for (int q = 0; q < 2 * S_MAX + 4; q++) seen[q] = false;
-                    for (int o = no - 1; o >= h.op0; o--) {
-                        if (!seen[P->ops[o].la]) { seen[P->ops[o].la] = true; P->ops[o].rel |= 1; }
-                        if (!seen[P->ops[o].lb]) { seen[P->ops[o].lb] = true; P->ops[o].rel |= 2; }
-                    }
-                    P->groups[ng++] = h;
-                    ga = gb + 1;
+    // the first band takes the remainder: low levels have the fewest products
+    const int first = s % band ? s % band : band;
+    for (int t0 = 2; t0 <= s + 1; t0 += (t0 == 2 ? first : band)) {
+        const int t1 = t0 + (t0 == 2 ? first : band) - 1;
+        if (nr + (t1 - t0 + 1) > MAX_ROUNDS) return -1;
+        const int r0 = nr;
+        for (int t = t0; t <= t1; t++) {
+            Round rd;
+            rd.level = (uint8_t)t;
+            rd.i0 = (uint8_t)(t - s > 1 ? t - s : 1);
+            rd.i1 = (uint8_t)((t - 1 < s ? t - 1 : s) + 1);
+            rd.shift = (int8_t)(5 * (s + 1 - t) - D);
+            rd.buf = (uint8_t)(t - t0);
+            rd.pad[0] = rd.pad[1] = rd.pad[2] = 0;
+            P->rounds[nr++] = rd;
+        }
+        // A slices with a partner in the band
+        const int ilo = t0 - s > 1 ? t0 - s : 1, ihi = t1 - 1 < s ? t1 - 1 : s;
+        for (int c0 = ilo; c0 <= ihi; c0 += w) {
+            const int c1 = c0 + w - 1 < ihi ? c0 + w - 1 : ihi;
+            const int jlo = t0 - c1 > 1 ? t0 - c1 : 1, jhi = t1 - c0 < s ? t1 - c0 : s;
+            const int na = c1 - c0 + 1, nb = jhi - jlo + 1;
+            if (ng >= MAX_GROUPS || nl + na + nb > MAX_LOADS || no + na * (t1 - t0 + 1) > MAX_OPS) return -1;
+            if (na + nb > STAGE_TILES) return -1;
+            Group g;
+            g.r0 = (int16_t)r0;
+            g.nr = (int16_t)(t1 - t0 + 1);
+            g.load0 = (int16_t)nl;
+            g.nload = (int16_t)(na + nb);
+            g.op0 = (int16_t)no;
+            g.flags = (c0 > ilo ? GF_CONT_IN : 0) | (c1 < ihi ? GF_CONT_OUT : 0);
+            for (int i = c0; i <= c1; i++) {
+                P->loads[nl].which = 0;
+                P->loads[nl].slice = (uint8_t)(i - 1);
+                nl++;
+            }
+            for (int j = jlo; j <= jhi; j++) {
+                P->loads[nl].which = 1;
+                P->loads[nl].slice = (uint8_t)(j - 1);
+                nl++;
+            }
+            for (int i = c0; i <= c1; i++) {
+                // levels of this i with a B partner: t in [ta, tb]
+                const int ta = i + 1 > t0 ? i + 1 : t0, tb = i + s < t1 ? i + s : t1;
+                for (int t = ta; t <= tb;) {
+                    const bool wide = ((t - t0) % 2 == 0) && t + 1 <= tb;
+                    if (no >= MAX_OPS) return -1;
+                    Op op;
+                    op.a_off = (uint16_t)((i - c0) * (TILE_BYTES >> 4));
+                    op.b_off = (uint16_t)((na + (t - i) - jlo) * (TILE_BYTES >> 4));
+                    op.dcol = (uint16_t)((t - t0) * BN);
+                    op.wide = wide ? 1 : 0;
+                    P->ops[no++] = op;
+                    t += wide ? 2 : 1;
                 }
             }
+            g.nop = (int16_t)(no - g.op0);
+            P->groups[ng++] = g;
         }
     }
     P->ngroups = ng;
@@ -331,11 +306,11 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
 // One thread: slice count and the group / round / MMA program from the
 // statistics.  misc: [0] non-finite flag, [1] spread of A x256, [2] of B.
 __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
-                       int pairing, int order, SplitPlan* __restrict__ plan) {
+                       int band, SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
     int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
-    int n = plan_build(s, Kp, klen_cat, plan, pairing, order);
+    int n = plan_build(s, Kp, klen_cat, plan, band);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
     plan->spread = (float)spread;
@@ -475,17 +450,31 @@ __device__ __forceinline__ double scale_pow2(double v, int X) {
     return (v * __longlong_as_double((long long)(X1 + 1023) << 52)) * __longlong_as_double((long long)(X2 + 1023) << 52);
 }
 
+// Output tile order: bands of TILE_GROUP_M tile rows, column-major inside a
+// band, so the CTAs running at the same time (consecutive tile indices) form a
+// TILE_GROUP_M x ~(grid / TILE_GROUP_M) block: each B slice tile they load is
+// shared by up to TILE_GROUP_M of them in L2, each A slice tile by the rest.
+constexpr int TILE_GROUP_M = 16;
+__device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, int& m0, int& n0) {
+    const int per_group = TILE_GROUP_M * tiles_n;
+    const int g = tile / per_group, first = g * TILE_GROUP_M;
+    const int gm = tiles_m - first < TILE_GROUP_M ? tiles_m - first : TILE_GROUP_M;
+    const int r = tile - g * per_group;
+    m0 = (first + r % gm) * BM;
+    n0 = (r / gm) * BN;
+}
+
 // 10 warps land 3-deep on two of the four SM sub-partitions, so the register
 // file allows at most ~168 registers per thread; launch bounds enforce that.
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ SplitGemmParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte alignment for the 128B-swizzled TMA tiles
+    // 1024-byte alignment for the swizzled TMA tiles
     unsigned char* smem = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char* sT = smem;  // RING operand tiles of 16 KB
-    __shared__ __align__(8) uint64_t full[NBATCH], empty[NBATCH], accfull[NBUF], accempty[NBUF], mma_done;
+    unsigned char* sT = smem;  // RING operand tiles of 8 KB
+    __shared__ __align__(8) uint64_t full[NSTAGE], empty[NSTAGE], accfull[NBUF], accempty[NBUF], mma_done;
     __shared__ uint32_t tmem_base_slot;
     __shared__ int abort_flag;
 
@@ -493,14 +482,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (plan->nonfinite) return;  // the gated plain path computes this product
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int nrounds = plan->nrounds;
-    // persistent: CTA b takes tiles b, b + grid, ...; tiles run along N within
-    // a row of tiles so concurrently active CTAs share A panels in L2
+    // persistent: CTA b takes tiles b, b + grid, ...; see tile_origin for the order
     const int tiles_n = (p.N + BN - 1) / BN, tiles_m = (p.M + BM - 1) / BM;
     const int ntiles = tiles_n * tiles_m;
 
     const int ngroups = plan->ngroups;
     if (threadIdx.x == 0) {
-        for (int i = 0; i < NBATCH; i++) {
+        for (int i = 0; i < NSTAGE; i++) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
@@ -520,71 +508,67 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
     }
-    // stage the group / load / MMA program and the round shifts
-    const Group* gp = plan->groups;
-    const Op* opp = plan->ops;
-    const Load* ldp = plan->loads;
-    Group* sg = reinterpret_cast<Group*>(smem + RING * TILE_BYTES);
-    Op* so = reinterpret_cast<Op*>(sg + PG_MAX);
-    Load* sl = reinterpret_cast<Load*>(so + PO_MAX);
-    int8_t* ssh = reinterpret_cast<int8_t*>(sl + PL_MAX);
-    int nops_total = 0, nloads_total = 0;
-    if (ngroups > 0) {
-        const Group last = plan->groups[ngroups - 1];
-        nops_total = last.op0 + last.nop;
-        nloads_total = last.load0 + last.nload;
-    }
-    const bool in_smem = ngroups <= PG_MAX && nops_total <= PO_MAX && nloads_total <= PL_MAX && nrounds <= PR_MAX;
-    // tile loads this CTA will issue in total (sizes the last, partial batch)
-    int loads_per_tile = 0;
-    for (int g = 0; g < ngroups; g++) loads_per_tile += plan->groups[g].nload * (plan->groups[g].kb1 - plan->groups[g].kb0);
-    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
-    const int total_loads = loads_per_tile * my_tiles;
-    if (in_smem) {
-        for (int i = threadIdx.x; i < ngroups; i += blockDim.x) sg[i] = plan->groups[i];
-        for (int i = threadIdx.x; i < nops_total; i += blockDim.x) so[i] = plan->ops[i];
-        for (int i = threadIdx.x; i < nloads_total; i += blockDim.x) sl[i] = plan->loads[i];
-        for (int i = threadIdx.x; i < nrounds; i += blockDim.x) ssh[i] = plan->rounds[i].shift;
-        gp = sg;
-        opp = so;
-        ldp = sl;
-    }
+    // stage the plan (a few KB) in shared memory: the MMA-issuing thread
+    // never waits on a global load between MMAs
+    static_assert(sizeof(SplitPlan) % 16 == 0, "plan copied in 16-byte words");
+    SplitPlan* sp = reinterpret_cast<SplitPlan*>(smem + RING * TILE_BYTES);
+    for (int i = threadIdx.x; i < (int)(sizeof(SplitPlan) / 16); i += blockDim.x)
+        reinterpret_cast<uint4*>(sp)[i] = reinterpret_cast<const uint4*>(plan)[i];
+    const Group* gp = sp->groups;
+    const Op* opp = sp->ops;
+    const Load* ldp = sp->loads;
+    const int nkb = plan->nkb, kcb = plan->kcb, nchunks = (nkb + kcb - 1) / kcb;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_slot;
+    if (warp >= 2) {
+        // every MMA accumulates: the buffers start at zero (and are zeroed
+        // again by the epilogue after each read)
+        const int q = warp % 4, h = (warp - 2) / 4;
+#pragma unroll
+        for (int b = 0; b < NBUF; b++) {
+            tmem_zero32(tmem + ((uint32_t)(32 * q) << 16) + b * BN + h * 64);
+            tmem_zero32(tmem + ((uint32_t)(32 * q) << 16) + b * BN + h * 64 + 32);
+        }
+        tmem_st_wait();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     if (warp == 0) {
-        // ---------------- TMA producer
+        // ---------------- TMA producer: one stage per K block of a group
         if (lane == 0) {
 #ifdef F4J_TRACE
             unsigned long long tr_wait = 0;
             const long long tr_start = clock64();
 #endif
-            int ls = 0;  // tile loads issued (ring position), carried across tiles
+            int st = 0;  // stages issued, carried across tiles
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
-                const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
-                for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
-                    const Group G = gp[g];
-                    for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
-                        for (int l = 0; l < G.nload; l++, ls++) {
-                            const Load L = ldp[G.load0 + l];
-                            const int b = ls / BATCH, bs = b % NBATCH;
-                            if (ls % BATCH == 0) {
-                                // first tile of a batch: wait for the batch slot, then
-                                // expect all of the batch's bytes on its one barrier
+                int m0, n0;
+                tile_origin(tile, tiles_m, tiles_n, m0, n0);
+                for (int kc = 0; kc < nkb && !*(volatile int*)&abort_flag; kc += kcb) {
+                    const int kend = kc + kcb < nkb ? kc + kcb : nkb;
+                    for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
+                        const Group G = gp[g];
+                        for (int kb = kc; kb < kend; kb++, st++) {
+                            const int s = st % NSTAGE;
+                            if (st >= NSTAGE) {
                                 F4J_T_BEGIN();
-                                const bool okw = b < NBATCH || mbar_wait(&empty[bs], ((b / NBATCH) & 1) ^ 1, p.status, 11);
+                                const bool okw = mbar_wait(&empty[s], ((st / NSTAGE) & 1) ^ 1, p.status, 11);
                                 F4J_T_ADD(tr_wait);
                                 if (!okw) {
                                     abort_flag = 1;
                                     break;
                                 }
-                                const int cnt = total_loads - ls < BATCH ? total_loads - ls : BATCH;
-                                mbar_arrive_expect_tx(&full[bs], cnt * TILE_BYTES);
                             }
-                            tma_load_3d(sT + (ls % RING) * TILE_BYTES, L.which ? &tmB : &tmA, &full[bs], kb * BKB,
-                                        L.which ? n0 : m0, L.slice);
+                            mbar_arrive_expect_tx(&full[s], G.nload * TILE_BYTES);
+                            for (int l = 0; l < G.nload; l++) {
+                                const Load L = ldp[G.load0 + l];
+                                tma_load_3d(sT + (s * STAGE_TILES + l) * TILE_BYTES, L.which ? &tmB : &tmA, &full[s],
+                                            kb * BKB, L.which ? n0 : m0, L.slice);
+                            }
                         }
                     }
                 }
@@ -594,92 +578,77 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             atomicAdd(&g_f4j_trace[5], tr_wait);
 #endif
             // drain the copies still in flight (bounded)
-            const int nb = (ls + BATCH - 1) / BATCH;
-            for (int q = nb > NBATCH ? nb - NBATCH : 0; q < nb; q++)
-                mbar_wait(&full[q % NBATCH], (q / NBATCH) & 1, nullptr, 0);
+            for (int q = st > NSTAGE ? st - NSTAGE : 0; q < st; q++)
+                mbar_wait(&full[q % NSTAGE], (q / NSTAGE) & 1, nullptr, 0);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
-            constexpr uint32_t idesc = umma_idesc_e4m3_f32(BM, BN);
+            constexpr uint32_t idesc128 = umma_idesc_e4m3_f32(BM, BN);
+            constexpr uint32_t idesc256 = umma_idesc_e4m3_f32(BM, 2 * BN);
 #ifdef F4J_TRACE
             unsigned long long tr_wait = 0, tr_acc = 0, tr_ops = 0;
             const long long tr_start = clock64();
 #endif
-            int ls = 0, rg = 0, wb = 0;  // ring, round and waited-batch counters carried across tiles
-            int relcnt[NBATCH];
-            for (int i = 0; i < NBATCH; i++) relcnt[i] = 0;
-            bool first0 = true, first1 = true;  // next MMA into buffer 0 / 1 of the round set overwrites
+            // smem descriptor of tile slot t = base + t * (TILE_BYTES >> 4): the
+            // start-address field is the low bits and never carries out
+            const uint64_t desc0 = umma_desc_sw64(sT);
+            int st = 0;             // stages consumed, carried across tiles
+            uint32_t used = 0;      // bit b: buffer b has been filled before
+            uint32_t drained = 0;   // bit b: parity of the next accempty[b] phase to wait for
             for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
-                for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
-                    const Group G = gp[g];
-                    if (!(G.flags & GF_CONT_IN)) {
-                        // the group's TMEM buffers must have been drained by the epilogue
-                        for (int u = 0; u < G.nr; u++) {
-                            const int rr = rg + u;
+                for (int kc = 0; kc < nkb && !*(volatile int*)&abort_flag; kc += kcb) {
+                    const int kend = kc + kcb < nkb ? kc + kcb : nkb;
+                    for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
+                        const Group G = gp[g];
+                        if (!(G.flags & GF_CONT_IN)) {
+                            // the band's buffers must have been read (and zeroed) by the epilogue
+                            for (int b = 0; b < G.nr; b++) {
+                                if (!((used >> b) & 1)) continue;
+                                F4J_T_BEGIN();
+                                const bool okw = mbar_wait(&accempty[b], (drained >> b) & 1, p.status, 12);
+                                F4J_T_ADD(tr_acc);
+                                drained ^= 1u << b;
+                                if (!okw) {
+                                    abort_flag = 1;
+                                    break;
+                                }
+                            }
+                            tc_fence_after();
+                        }
+                        const Op* ops = opp + G.op0;
+                        for (int kb = kc; kb < kend; kb++, st++) {
+                            const int s = st % NSTAGE;
                             F4J_T_BEGIN();
-                            const bool okw = rr < NBUF || mbar_wait(&accempty[rr % NBUF], ((rr / NBUF) & 1) ^ 1, p.status, 12);
-                            F4J_T_ADD(tr_acc);
+                            const bool okw = mbar_wait(&full[s], (st / NSTAGE) & 1, p.status, 13);
+                            F4J_T_ADD(tr_wait);
                             if (!okw) {
                                 abort_flag = 1;
                                 break;
                             }
-                        }
-                        tc_fence_after();
-                        first0 = first1 = true;
-                    }
-                    for (int kb = G.kb0; kb < G.kb1 && !*(volatile int*)&abort_flag; kb++) {
-                        for (int o = 0; o < G.nop; o++) {
-                            const Op O = opp[G.op0 + o];
-                            const int need_batch = (ls + (O.la > O.lb ? O.la : O.lb)) / BATCH;
-                            bool ok = true;
-                            for (; wb <= need_batch; wb++) {
-                                F4J_T_BEGIN();
-                                const bool okw = mbar_wait(&full[wb % NBATCH], (wb / NBATCH) & 1, p.status, 13);
-                                F4J_T_ADD(tr_wait);
-                                if (!okw) {
-                                    ok = false;
-                                    break;
-                                }
-                            }
-                            if (!ok) {
-                                abort_flag = 1;
-                                break;
-                            }
                             tc_fence_after();
-#ifdef F4J_TRACE
-                            tr_ops++;
-#endif
-                            const int sa = (ls + O.la) % RING, sb = (ls + O.lb) % RING;
-                            const uint64_t da = umma_desc_sw128(sT + sa * TILE_BYTES);
-                            const uint64_t db = umma_desc_sw128(sT + sb * TILE_BYTES);
-                            const uint32_t d_tmem = tmem + ((rg + O.buf) % NBUF) * BN;
-                            bool& first = O.buf ? first1 : first0;
+                            const uint64_t sdesc = desc0 + (uint64_t)(s * STAGE_TILES * (TILE_BYTES >> 4));
+#pragma unroll 2
+                            for (int o = 0; o < G.nop; o++) {
+                                const Op O = ops[o];
+                                const uint64_t da = sdesc + O.a_off, db = sdesc + O.b_off;
+                                const uint32_t dt = tmem + O.dcol;
+                                const uint32_t id = O.wide ? idesc256 : idesc128;
 #pragma unroll
-                            for (int kk = 0; kk < BKB / 32; kk++) {
-                                // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
-                                umma_f8(d_tmem, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), idesc,
-                                        first ? 0u : 1u);
-                                first = false;
-                            }
-                            // a batch's slots are released (one commit) after the last
-                            // use of all of its tiles
-                            for (int side = 0; side < 2; side++) {
-                                if (!(O.rel & (1 << side))) continue;
-                                const int q = ls + (side ? O.lb : O.la);
-                                const int b = q / BATCH, bs = b % NBATCH;
-                                const int cnt = total_loads - b * BATCH < BATCH ? total_loads - b * BATCH : BATCH;
-                                if (++relcnt[bs] == cnt) {
-                                    relcnt[bs] = 0;
-                                    umma_commit(&empty[bs]);
+                                for (int kk = 0; kk < BKB / 32; kk++) {
+                                    // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
+                                    umma_f8(dt, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), id, 1u);
                                 }
+#ifdef F4J_TRACE
+                                tr_ops++;
+#endif
                             }
+                            umma_commit(&empty[s]);
                         }
-                        ls += G.nload;
-                    }
-                    if (!(G.flags & GF_CONT_OUT)) {
-                        for (int u = 0; u < G.nr; u++) umma_commit(&accfull[(rg + u) % NBUF]);
-                        rg += G.nr;
+                        if (!(G.flags & GF_CONT_OUT)) {
+                            for (int b = 0; b < G.nr; b++) umma_commit(&accfull[b]);
+                            used |= (1u << G.nr) - 1u;
+                        }
                     }
                 }
             }
@@ -697,26 +666,31 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const int q = warp % 4;          // TMEM lane quarter this warp may access
         const int h = (warp - 2) / 4;    // column half of the tile
         const int ubits = plan->ubits;
-        int rg = 0;
+        uint32_t filled = 0;  // bit b: parity of the next accfull[b] phase to wait for
 #ifdef F4J_TRACE
         unsigned long long tr_wait = 0;
         const long long tr_start = clock64();
 #endif
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        int m0, n0;
+        tile_origin(tile, tiles_m, tiles_n, m0, n0);
         const int row = m0 + 32 * q + lane;
         long long acc[64];
 #pragma unroll
         for (int c = 0; c < 64; c++) acc[c] = 0;
         bool ok = true;
-        for (int r = 0; r < nrounds; r++, rg++) {
-            const int buf = rg % NBUF;
+        // the round program repeats once per K chunk; the rounds of a band
+        // complete together, in round order
+        for (int rr = 0; rr < nchunks * nrounds; rr++) {
+            const Round R = sp->rounds[rr % nrounds];
+            const int buf = R.buf;
             bool w = true;
             {
                 F4J_T_BEGIN();
-                if (lane == 0) w = mbar_wait(&accfull[buf], (rg / NBUF) & 1, p.status, 15);
+                if (lane == 0) w = mbar_wait(&accfull[buf], (filled >> buf) & 1, p.status, 15);
                 F4J_T_ADD(tr_wait);
             }
+            filled ^= 1u << buf;
             w = __shfl_sync(0xffffffffu, w, 0);
             if (!w || *(volatile int*)&abort_flag) {
                 ok = false;
@@ -724,12 +698,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            const int sh = in_smem ? ssh[r] : plan->rounds[r].shift;
+            const int sh = R.shift;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * BN + h * 64;
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 uint32_t v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + buf * BN + h * 64 + half * 32, v);
+                tmem_ld32(taddr + half * 32, v);
                 tmem_ld_wait();
+                tmem_zero32(taddr + half * 32);
 #pragma unroll
                 for (int c = 0; c < 32; c++) {
                     // rounds are sized so |value| <= 2^24: an int32 holds it exactly
@@ -738,6 +714,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     else acc[half * 32 + c] += (x + (1ll << (-sh - 1))) >> (-sh);
                 }
             }
+            tmem_st_wait();
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&accempty[buf]);
@@ -797,7 +774,7 @@ static int make_slice_map(CUtensorMap* map, const void* base, uint64_t Kp, uint6
     cuuint32_t box[3] = {BKB, BM, 1};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<void*>(base), dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return f4j_fail(F4J_ERR_CUDA, "cuTensorMapEncodeTiled (slices) failed (%d)", (int)r);
     return F4J_OK;
@@ -809,18 +786,11 @@ static int env_slices() {
     return (env && atoi(env) > 0) ? atoi(env) : 0;
 }
 
-// Level pairing in the slice GEMM's schedule (F4J_SPLIT_PAIRING=0 disables it).
-static int env_pairing() {
-    const char* env = getenv("F4J_SPLIT_PAIRING");
-    return (env && env[0] == '0') ? 0 : 1;
-}
-
-// Schedule order of the slice GEMM (F4J_SPLIT_ORDER): 1 (default) streams all K
-// blocks of one A slice with its partner B slices before the next; 0 walks
-// every slice tile of a round set per K block.
-static int env_order() {
-    const char* env = getenv("F4J_SPLIT_ORDER");
-    return (env && env[0] == '0') ? 0 : 1;
+// Levels per band in the slice GEMM's schedule (F4J_SPLIT_BAND, 1..4; default 4).
+static int env_band() {
+    const char* env = getenv("F4J_SPLIT_BAND");
+    const int b = env ? atoi(env) : 0;
+    return (b >= 1 && b <= NBUF) ? b : NBUF;
 }
 
 static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
@@ -893,7 +863,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
     k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(),
-                                      env_pairing(), env_order(), plan);
+                                      env_band(), plan);
     F4J_LAUNCHED(ctx);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
@@ -927,7 +897,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     prm.status = ctx->d_status + F4J_ST_TIMEOUT;
     prm.plan = plan;
 
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + PROG_BYTES;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan);
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
@@ -1057,7 +1027,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
                                                                                                  esb, cnb, misc);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
-    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_pairing(), env_order(), plan);
+    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_band(), plan);
     F4J_CUDA(cudaGetLastError());
     // NaN/Inf operands are rejected, so wait for the plan's verdict
     int hp[4];
@@ -1088,7 +1058,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.C = C;
     prm.status = misc + 8;
     prm.plan = plan;
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + PROG_BYTES;
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan);
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
