@@ -33,8 +33,16 @@ namespace {
 constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits keeps Y < 2^62 in int64
 constexpr int BM = 128, BN = 128;  // output tile
 constexpr int BKB = 64;            // K bytes per tile load (one 64-byte swizzle row)
-constexpr int STAGE_TILES = 11;    // operand tiles per stage: 2w + band - 1 for w A slices
-constexpr int NSTAGE = 2;          // stages in the shared-memory ring
+// Ring geometry (compile-time): operand tiles per stage (2w + band - 1 for w
+// A slices per group) and stages in the shared-memory ring.
+#ifndef F4J_SPLIT_STAGE_TILES
+#define F4J_SPLIT_STAGE_TILES 9
+#endif
+#ifndef F4J_SPLIT_NSTAGE
+#define F4J_SPLIT_NSTAGE 3
+#endif
+constexpr int STAGE_TILES = F4J_SPLIT_STAGE_TILES;
+constexpr int NSTAGE = F4J_SPLIT_NSTAGE;
 constexpr int RING = STAGE_TILES * NSTAGE;
 constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns (= levels per band)
 constexpr int TILE_BYTES = BM * BKB;  // 8 KB per operand tile
@@ -319,12 +327,23 @@ __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int6
 }
 
 // ------------------------------------------------------------------ split
-__device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
-    int v = d < 0 ? -d : d;
-    if (v == 0) return 0u;
-    int e = 31 - __clz(v);
-    int mant = (e >= 3) ? ((v >> (e - 3)) & 7) : ((v << (3 - e)) & 7);
-    return (uint32_t)(((e + 7) << 3) | mant | (d < 0 ? 0x80 : 0));
+
+// Exact float of an integer |d| < 2^22: d added to the bit pattern of 1.5 * 2^23.
+__device__ __forceinline__ float float_of_small_int(int d) {
+    return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
+// Eight small integers (exact in E4M3) as E4M3 bytes, stored as 8 bytes.
+__device__ __forceinline__ void store_e4m3x8(uint8_t* dst, const float (&f)[8]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        uint16_t h;
+        // the first source operand goes to the upper byte
+        asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(h) : "f"(f[2 * u + 1]), "f"(f[2 * u]));
+        w[u] = h;
+    }
+    *reinterpret_cast<uint2*>(dst) = make_uint2(w[0] | (w[1] << 16), w[2] | (w[3] << 16));
 }
 
 // Fixed-point integer of x relative to 2^e with F fractional bits:
@@ -397,35 +416,48 @@ __global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int
     const int nparts = cplx ? (role == 0 ? 2 : 4) : 1;
     for (int part = 0; part < nparts; part++) {
         // part: 0 -> (row r, col q) ; 1 -> (row r, col Kh+q) ; 2 -> (row n+r, col q) ; 3 -> (row n+r, col Kh+q)
-        long long Y[8];
+        // Y = H * 2^30 + L with 0 <= L < 2^30: the low six digits come from L,
+        // the rest from H (plus the carry out of L), all in 32-bit arithmetic
+        int L[8], H[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             double v;
             double a = sre[rr][qs + j], b = sim[rr][qs + j];
             if (role == 0) v = (part == 0) ? a : b;
             else v = (part == 0) ? a : (part == 1) ? -b : (part == 2) ? b : a;
-            Y[j] = fixed_of(v, e, F);
+            const long long y = fixed_of(v, e, F);
+            L[j] = (int)(y & 0x3FFFFFFFll);
+            H[j] = (int)(y >> 30);
         }
         const int64_t orow = (part >= 2) ? (targets + r) : r;
         const int64_t ocol = ((part & 1) ? Kh : 0) + q0 + qs;
         uint8_t* base = out + orow * Kp + ocol;
-        // digits from the least significant slice up
-        for (int p = s - 1; p >= 0; p--) {
-            uint32_t lo = 0, hi = 0;
+        // balanced base-32 digits from the least significant slice (p = s - 1) up
+#pragma unroll
+        for (int c = 0; c < S_MAX - 1; c++) {
+            if (c >= s - 1) break;
+            float f[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 int d;
-                if (p == 0) d = (int)Y[j];
-                else {
-                    d = (int)(((Y[j] + 16) & 31) - 16);
-                    Y[j] = (Y[j] - d) >> 5;
+                if (c < 6) {
+                    d = ((L[j] + 16) & 31) - 16;
+                    L[j] = (L[j] - d) >> 5;
+                    if (c == 5) H[j] += L[j];  // carry out of the low 30 bits: 0 or 1
+                } else {
+                    d = ((H[j] + 16) & 31) - 16;
+                    H[j] = (H[j] - d) >> 5;
                 }
-                uint32_t byte = e4m3_of_digit(d);
-                if (j < 4) lo |= byte << (8 * j);
-                else hi |= byte << (8 * (j - 4));
+                f[j] = float_of_small_int(d);
             }
-            *reinterpret_cast<uint2*>(base + (int64_t)p * rows_out * Kp) = make_uint2(lo, hi);
+            store_e4m3x8(base + (int64_t)(s - 1 - c) * rows_out * Kp, f);
         }
+        // the most significant digit is what remains
+        float f[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            f[j] = float_of_small_int(s - 1 < 6 ? L[j] + H[j] * (1 << (30 - 5 * (s - 1))) : H[j]);
+        store_e4m3x8(base, f);
     }
 }
 
@@ -454,7 +486,10 @@ __device__ __forceinline__ double scale_pow2(double v, int X) {
 // band, so the CTAs running at the same time (consecutive tile indices) form a
 // TILE_GROUP_M x ~(grid / TILE_GROUP_M) block: each B slice tile they load is
 // shared by up to TILE_GROUP_M of them in L2, each A slice tile by the rest.
-constexpr int TILE_GROUP_M = 16;
+#ifndef F4J_SPLIT_GROUP_M
+#define F4J_SPLIT_GROUP_M 16
+#endif
+constexpr int TILE_GROUP_M = F4J_SPLIT_GROUP_M;
 __device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, int& m0, int& n0) {
     const int per_group = TILE_GROUP_M * tiles_n;
     const int g = tile / per_group, first = g * TILE_GROUP_M;
