@@ -481,6 +481,10 @@ def run_ours(args):
     Ch = np.empty((n, n))
     for arr in (Ah, Bh, Ch):
         E.check(E.lib.f4j_host_register(arr.ctypes.data, arr.nbytes))
+    # upload A, B; product; download C (writing C in place into the pinned
+    # host array through an f4j_buf_wrap handle measured about 1 ms slower at
+    # 8192^3: the epilogue's scattered stores across the host link cost more
+    # than one bulk download)
     A2, B2, C2 = E.ctx.alloc(Ah.nbytes), E.ctx.alloc(Bh.nbytes), E.ctx.alloc(Ch.nbytes)
 
     def e2e():
@@ -490,6 +494,7 @@ def run_ours(args):
         C2.download(Ch, sync=False)
     e2e_ms = E.timed(e2e, max(3, args.steps // 3), 2)
     e2e_ms = dist.max(e2e_ms)
+    C2.free()
     for arr in (Ah, Bh, Ch):
         E.lib.f4j_host_unregister(arr.ctypes.data)
 
@@ -512,7 +517,9 @@ def run_ours(args):
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": ws * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes},
+                    "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes,
+                    "path": "f4j_buf_upload_async of A, B from pinned host memory; f4j_dgemm (split); "
+                            "f4j_buf_download_async of C to pinned host memory"},
             "gpu_launches": launches, "clocks": clocks}
     line.update(out)
     print(json.dumps(line))

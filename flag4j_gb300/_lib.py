@@ -55,6 +55,7 @@ SIGNATURES = {
     "f4j_profile_read": (_i, [_v, _i, _pd, _pi64]),
     "f4j_profile_reset": (_i, [_v]),
     "f4j_buf_alloc": (_i, [_v, _sz, _pv]),
+    "f4j_buf_wrap": (_i, [_v, _v, _sz, _pv]),
     "f4j_buf_free": (_i, [_v, _v]),
     "f4j_buf_size": (_sz, [_v]),
     "f4j_buf_device_ptr": (_v, [_v]),

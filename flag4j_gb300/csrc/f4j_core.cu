@@ -245,7 +245,39 @@ extern "C" int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out) {
         cudaGetLastError();
         return f4j_fail(F4J_ERR_OOM, "device buffer of %zu bytes: %s", bytes, cudaGetErrorString(e));
     }
-    *out = new f4j_buf_s{p, bytes};
+    *out = new f4j_buf_s{p, bytes, true};
+    return F4J_OK;
+}
+
+extern "C" int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out) {
+    F4J_CHECK_CTX(ctx);
+    if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!ptr) return f4j_fail(F4J_ERR_ARG, "null memory to wrap");
+    if (reinterpret_cast<uintptr_t>(ptr) & 15) return f4j_fail(F4J_ERR_ARG, "wrapped memory must be 16-byte aligned");
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return f4j_fail(F4J_ERR_ARG, "cannot query the memory to wrap: %s", cudaGetErrorString(e));
+    }
+    void* dev = nullptr;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+        if (a.type == cudaMemoryTypeDevice && a.device != ctx->device)
+            return f4j_fail(F4J_ERR_ARG, "wrapped device memory belongs to device %d, context is on %d", a.device,
+                            ctx->device);
+        dev = ptr;
+    } else if (a.type == cudaMemoryTypeHost) {
+        dev = a.devicePointer;  // pinned / registered host memory, mapped into the device's address space
+    } else {
+        int pageable = 0;
+        F4J_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, ctx->device));
+        if (!pageable)
+            return f4j_fail(F4J_ERR_ARG, "the device cannot address unregistered host memory (register it first)");
+        dev = ptr;
+    }
+    if (!dev) return f4j_fail(F4J_ERR_ARG, "the memory to wrap has no device address");
+    *out = new f4j_buf_s{dev, bytes, false};
     return F4J_OK;
 }
 
@@ -253,7 +285,7 @@ extern "C" int f4j_buf_free(f4j_ctx* ctx, f4j_buf b) {
     F4J_CHECK_CTX(ctx);
     if (!b) return F4J_OK;
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    cudaFree(b->ptr);
+    if (b->owned) cudaFree(b->ptr);
     delete b;
     return F4J_OK;
 }

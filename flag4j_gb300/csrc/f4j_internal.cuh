@@ -14,6 +14,7 @@
 struct f4j_buf_s {
     void* ptr;
     size_t bytes;
+    bool owned;  // false for f4j_buf_wrap handles
 };
 
 struct f4j_csr_s {

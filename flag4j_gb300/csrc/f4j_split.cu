@@ -228,7 +228,7 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
 // most s pairs, so the chunk is the largest power-of-two number of K blocks
 // with s * kchunk * 256 <= 2^24.  The fixed-point unit keeps the worst-case
 // accumulator below 2^62.  Levels 2..s+1 are cut into bands of `band`
-// (<= NBUF) levels, the first band taking the remainder; each band's A-slice range is cut into chunks of
+// (<= NBUF) levels, the lowest band taking the remainder; each band's A-slice range is cut into chunks of
 // w = (STAGE_TILES - band + 1) / 2 slices, one group each, so a group loads
 // at most 2w + band - 1 <= STAGE_TILES tiles per K block.  Returns the
 // number of rounds per chunk, or -1 if a table would overflow.
@@ -247,10 +247,15 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
     if (D < 0) D = 0;
     P->ubits = -(8 + 5 * (s - 1)) + D;
     int nr = 0, ng = 0, nl = 0, no = 0;
-    // the first band takes the remainder: low levels have the fewest products
+    // the lowest band takes the remainder (low levels have the fewest
+    // products); bands run from the highest levels down, so a tile starts
+    // with its longest band and the epilogue's final stores of the previous
+    // tile overlap that band's MMAs
     const int first = s % band ? s % band : band;
-    for (int t0 = 2; t0 <= s + 1; t0 += (t0 == 2 ? first : band)) {
-        const int t1 = t0 + (t0 == 2 ? first : band) - 1;
+    const int nbands = 1 + (s - first) / band;
+    for (int bi = nbands - 1; bi >= 0; bi--) {
+        const int t0 = bi == 0 ? 2 : 2 + first + (bi - 1) * band;
+        const int t1 = bi == 0 ? 1 + first : t0 + band - 1;
         if (nr + (t1 - t0 + 1) > MAX_ROUNDS) return -1;
         const int r0 = nr;
         for (int t = t0; t <= t1; t++) {

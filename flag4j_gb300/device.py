@@ -36,13 +36,17 @@ def check(rc):
 
 
 class DeviceBuffer:
-    """An f4j_buf: device memory owned by a Context."""
+    """An f4j_buf: device memory owned by a Context, or (wrap) memory the
+    device can address in place, such as pinned host memory."""
 
-    def __init__(self, ctx, nbytes):
+    def __init__(self, ctx, nbytes, wrap_ptr=None):
         self.ctx = ctx
         self.nbytes = int(nbytes)
         h = ctypes.c_void_p()
-        check(ctx.lib.f4j_buf_alloc(ctx.handle, self.nbytes, ctypes.byref(h)))
+        if wrap_ptr is None:
+            check(ctx.lib.f4j_buf_alloc(ctx.handle, self.nbytes, ctypes.byref(h)))
+        else:
+            check(ctx.lib.f4j_buf_wrap(ctx.handle, ctypes.c_void_p(wrap_ptr), self.nbytes, ctypes.byref(h)))
         self.handle = h
 
     def upload(self, arr, offset=0, sync=True):
@@ -88,6 +92,14 @@ class Context:
 
     def alloc(self, nbytes):
         return DeviceBuffer(self, nbytes)
+
+    def wrap(self, arr):
+        """Buffer over a C-contiguous numpy array's memory (no copy): kernels
+        read and write it in place across the host link.  The array must stay
+        alive (and, unless the device walks host page tables, be registered
+        with f4j_host_register) while the buffer is in use."""
+        assert arr.flags["C_CONTIGUOUS"]
+        return DeviceBuffer(self, arr.nbytes, wrap_ptr=arr.ctypes.data)
 
     def from_numpy(self, arr):
         arr = np.ascontiguousarray(arr)

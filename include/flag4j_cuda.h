@@ -107,6 +107,18 @@ int f4j_buf_zero(f4j_ctx* ctx, f4j_buf buf);
 /* Pin / unpin caller-owned host memory (e.g. a Java MemorySegment). */
 int f4j_host_register(void* host, size_t bytes);
 int f4j_host_unregister(void* host);
+/* A buffer handle over memory the device can address, without copying it:
+ * device memory from another allocator, host memory pinned with
+ * f4j_host_register, or plain host memory where the device walks the host's
+ * page tables.  Kernels then read and write that memory in place; for host
+ * memory each access crosses the host link (on GB300 a split product writing
+ * its 8192^2 C this way ran about 1 ms slower than writing device memory and
+ * downloading it, so this is for callers that cannot spare the device copy).
+ * ptr must be 16-byte aligned.  The handle does not own the
+ * memory: f4j_buf_free releases the handle only.  F4J_ERR_ARG if the device
+ * cannot address ptr.  No counterpart in Flag4j, whose matrices live in Java
+ * heap arrays. */
+int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out);
 
 /* ---- dense products ------------------------------------------------------ */
 /* C(m x n) = op(A) * op(B), op(A) m x k, op(B) k x n, real float64.

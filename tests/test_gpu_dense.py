@@ -347,3 +347,39 @@ def test_dense_adjoint_finite_differences(f4j, mode):
         Bm_[i, j] -= h
         fd = central(prod(A, Bp), prod(A, Bm_))
         assert abs(fd - dB[i, j]) <= 1e-7 * max(1.0, abs(dB[i, j]))
+
+
+@pytest.mark.parametrize("mode", ["plain", "split"])
+def test_wrapped_host_output_matches_device_output(f4j, mode):
+    """C written in place into pinned host memory (f4j_buf_wrap) is bitwise the
+    C written to device memory; freeing the wrap handle leaves the array alone."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    m, n, k = 300, 260, 520
+    A = synth.scaled(m, k, 4, 11, "row")
+    B = synth.scaled(k, n, 4, 12, "col")
+    ref, _ = run_gemm(f4j, A, B, mode=mode)
+    dA, dB = ctx.from_numpy(A), ctx.from_numpy(B)
+    Ch = np.full((m, n), np.nan)
+    check(ctx.lib.f4j_host_register(Ch.ctypes.data, Ch.nbytes))
+    try:
+        wC = ctx.wrap(Ch)
+        check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, 0, dB.handle, 0, wC.handle, _lib.MODES[mode], None))
+        ctx.sync()
+        assert np.array_equal(Ch, ref)
+        wC.free()
+        Ch[0, 0] = 1.5  # still the caller's memory
+    finally:
+        check(ctx.lib.f4j_host_unregister(Ch.ctypes.data))
+
+
+def test_wrap_rejects_misaligned_and_null(f4j):
+    from flag4j_gb300.device import check, IllegalArgumentException
+    ctx = f4j.default_context()
+    buf = np.zeros(64)
+    h = ctypes.c_void_p()
+    with pytest.raises(IllegalArgumentException):
+        check(ctx.lib.f4j_buf_wrap(ctx.handle, ctypes.c_void_p(buf.ctypes.data + 8), 64, ctypes.byref(h)))
+    with pytest.raises(IllegalArgumentException):
+        check(ctx.lib.f4j_buf_wrap(ctx.handle, None, 64, ctypes.byref(h)))
