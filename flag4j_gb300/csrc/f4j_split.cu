@@ -1035,7 +1035,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     if (need > F4J_NOALLOC_SCRATCH_BYTES)
         return f4j_fail(F4J_ERR_ARG,
                         "f4j_dgemm_split_noalloc: m=%lld n=%lld k=%lld needs %zu bytes of scratch, more than the "
-                        "%u-byte static limit ((m+n)*roundup(k,128)*12 + small); use f4j_dgemm",
+                        "%u-byte static limit ((m+n)*roundup(k,64)*12 + small); use f4j_dgemm",
                         (long long)m, (long long)n, (long long)k, need, F4J_NOALLOC_SCRATCH_BYTES);
     void* base;
     int rc = noalloc_scratch(&base);

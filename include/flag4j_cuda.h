@@ -158,7 +158,7 @@ int f4j_zgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, 
  * caller's device pointers, `stream` a cudaStream_t (NULL = default stream).
  * Scratch comes from a static 32 MiB device array inside the library (held on
  * every GPU that loads it until exit), so sizes with
- *   (m + n) * roundup(k, 128) * 12 + 64 * (m + n) + 4096 > 32 MiB
+ *   (m + n) * roundup(k, 64) * 12 + 64 * (m + n) + 4096 > 32 MiB
  * are rejected with F4J_ERR_ARG; NaN/Inf operands are rejected too.  The first
  * call on a device looks up the array's address, so make that call before
  * any stream capture.  All calls share the array: calls whose GPU work
