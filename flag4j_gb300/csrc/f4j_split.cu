@@ -46,7 +46,15 @@ constexpr int NSTAGE = F4J_SPLIT_NSTAGE;
 constexpr int RING = STAGE_TILES * NSTAGE;
 constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns (= levels per band)
 constexpr int TILE_BYTES = BM * BKB;  // 8 KB per operand tile
-constexpr int GEMM_THREADS = 320;     // warp0 TMA, warp1 MMA, warps 2..9 epilogue
+// Epilogue warps (compile-time, 8 or 16): each owns one TMEM lane quarter and
+// BN / (EPI_WARPS / 4) columns of the tile.
+#ifndef F4J_SPLIT_EPI_WARPS
+#define F4J_SPLIT_EPI_WARPS 8
+#endif
+constexpr int EPI_WARPS = F4J_SPLIT_EPI_WARPS;
+static_assert(EPI_WARPS == 8 || EPI_WARPS == 16, "8 or 16 epilogue warps");
+constexpr int EPI_COLS = BN / (EPI_WARPS / 4);
+constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA, warps 2.. epilogue
 constexpr int MAX_ROUNDS = 16, MAX_GROUPS = 64, MAX_LOADS = 512, MAX_OPS = 256;
 
 // One round: the products A_i B_j of weight level t = i + j over one K chunk,
@@ -504,8 +512,11 @@ __device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, 
     n0 = (r / gm) * BN;
 }
 
-// 10 warps land 3-deep on two of the four SM sub-partitions, so the register
-// file allows at most ~168 registers per thread; launch bounds enforce that.
+// One CTA per SM: the register file is shared by GEMM_THREADS threads.  With
+// 8 epilogue warps (320 threads) three warps share two of the four SM
+// sub-partitions, which caps a thread at 168 registers; the epilogue keeps 64
+// int64 accumulators and reads TMEM 16 columns at a time to stay inside it.
+// (16 epilogue warps cap a thread at 96 registers and measured 5 % slower.)
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const __grid_constant__ SplitGemmParams p) {
@@ -534,7 +545,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
         for (int i = 0; i < NBUF; i++) {
             mbar_init(&accfull[i], 1);
-            mbar_init(&accempty[i], 8);
+            mbar_init(&accempty[i], EPI_WARPS);
         }
         mbar_init(&mma_done, 1);
         abort_flag = 0;
@@ -567,10 +578,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // again by the epilogue after each read)
         const int q = warp % 4, h = (warp - 2) / 4;
 #pragma unroll
-        for (int b = 0; b < NBUF; b++) {
-            tmem_zero32(tmem + ((uint32_t)(32 * q) << 16) + b * BN + h * 64);
-            tmem_zero32(tmem + ((uint32_t)(32 * q) << 16) + b * BN + h * 64 + 32);
-        }
+        for (int b = 0; b < NBUF; b++)
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; c += 32) tmem_zero32(tmem + ((uint32_t)(32 * q) << 16) + b * BN + h * EPI_COLS + c);
         tmem_st_wait();
     }
     tc_fence_before();
@@ -578,48 +588,60 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc_fence_after();
 
     if (warp == 0) {
-        // ---------------- TMA producer: one stage per K block of a group
-        if (lane == 0) {
+        // ---------------- TMA producer: one stage per K block of a group.  The
+        // whole warp issues a stage: lane 0 waits for the slot and arms its
+        // barrier, then lane l copies the stage's tile l (issuing the loads from
+        // one thread was measured to limit the ring's fill rate).
+        {
 #ifdef F4J_TRACE
             unsigned long long tr_wait = 0;
             const long long tr_start = clock64();
 #endif
             int st = 0;  // stages issued, carried across tiles
-            for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
                 int m0, n0;
                 tile_origin(tile, tiles_m, tiles_n, m0, n0);
-                for (int kc = 0; kc < nkb && !*(volatile int*)&abort_flag; kc += kcb) {
+                for (int kc = 0; kc < nkb && ok; kc += kcb) {
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
-                    for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
+                    for (int g = 0; g < ngroups && ok; g++) {
                         const Group G = gp[g];
+                        // this lane's tile of every stage of the group
+                        Load L{};
+                        if (lane < G.nload) L = ldp[G.load0 + lane];
+                        const CUtensorMap* map = L.which ? &tmB : &tmA;
+                        const int row0 = L.which ? n0 : m0;
                         for (int kb = kc; kb < kend; kb++, st++) {
                             const int s = st % NSTAGE;
-                            if (st >= NSTAGE) {
-                                F4J_T_BEGIN();
-                                const bool okw = mbar_wait(&empty[s], ((st / NSTAGE) & 1) ^ 1, p.status, 11);
-                                F4J_T_ADD(tr_wait);
-                                if (!okw) {
-                                    abort_flag = 1;
-                                    break;
+                            if (lane == 0) {
+                                if (st >= NSTAGE) {
+                                    F4J_T_BEGIN();
+                                    ok = mbar_wait(&empty[s], ((st / NSTAGE) & 1) ^ 1, p.status, 11) &&
+                                         !*(volatile int*)&abort_flag;
+                                    F4J_T_ADD(tr_wait);
                                 }
+                                if (ok) mbar_arrive_expect_tx(&full[s], G.nload * TILE_BYTES);
+                                else abort_flag = 1;
                             }
-                            mbar_arrive_expect_tx(&full[s], G.nload * TILE_BYTES);
-                            for (int l = 0; l < G.nload; l++) {
-                                const Load L = ldp[G.load0 + l];
-                                tma_load_3d(sT + (s * STAGE_TILES + l) * TILE_BYTES, L.which ? &tmB : &tmA, &full[s],
-                                            kb * BKB, L.which ? n0 : m0, L.slice);
-                            }
+                            ok = __shfl_sync(0xffffffffu, ok, 0);
+                            if (!ok) break;
+                            if (lane < G.nload)
+                                tma_load_3d(sT + (s * STAGE_TILES + lane) * TILE_BYTES, map, &full[s], kb * BKB, row0,
+                                            L.slice);
                         }
                     }
                 }
             }
 #ifdef F4J_TRACE
-            atomicAdd(&g_f4j_trace[4], (unsigned long long)(clock64() - tr_start));
-            atomicAdd(&g_f4j_trace[5], tr_wait);
+            if (lane == 0) {
+                atomicAdd(&g_f4j_trace[4], (unsigned long long)(clock64() - tr_start));
+                atomicAdd(&g_f4j_trace[5], tr_wait);
+            }
 #endif
             // drain the copies still in flight (bounded)
-            for (int q = st > NSTAGE ? st - NSTAGE : 0; q < st; q++)
-                mbar_wait(&full[q % NSTAGE], (q / NSTAGE) & 1, nullptr, 0);
+            if (lane == 0)
+                for (int q = st > NSTAGE ? st - NSTAGE : 0; q < st; q++)
+                    mbar_wait(&full[q % NSTAGE], (q / NSTAGE) & 1, nullptr, 0);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer (one thread)
@@ -702,9 +724,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             mbar_wait(&mma_done, 0, p.status, 14);
         }
     } else {
-        // ---------------- epilogue warps 2..9
+        // ---------------- epilogue warps
         const int q = warp % 4;          // TMEM lane quarter this warp may access
-        const int h = (warp - 2) / 4;    // column half of the tile
+        const int h = (warp - 2) / 4;    // column slice of the tile: columns h * EPI_COLS ...
         const int ubits = plan->ubits;
         uint32_t filled = 0;  // bit b: parity of the next accfull[b] phase to wait for
 #ifdef F4J_TRACE
@@ -715,9 +737,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         int m0, n0;
         tile_origin(tile, tiles_m, tiles_n, m0, n0);
         const int row = m0 + 32 * q + lane;
-        long long acc[64];
+        long long acc[EPI_COLS];
 #pragma unroll
-        for (int c = 0; c < 64; c++) acc[c] = 0;
+        for (int c = 0; c < EPI_COLS; c++) acc[c] = 0;
         bool ok = true;
         // the round program repeats once per K chunk; the rounds of a band
         // complete together, in round order
@@ -739,21 +761,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             }
             tc_fence_after();
             const int sh = R.shift;
-            const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * BN + h * 64;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * BN + h * EPI_COLS;
 #pragma unroll
-            for (int half = 0; half < 2; half++) {
-                uint32_t v[32];
-                tmem_ld32(taddr + half * 32, v);
+            for (int part = 0; part < EPI_COLS / 16; part++) {
+                uint32_t v[16];
+                tmem_ld16(taddr + part * 16, v);
                 tmem_ld_wait();
-                tmem_zero32(taddr + half * 32);
 #pragma unroll
-                for (int c = 0; c < 32; c++) {
+                for (int c = 0; c < 16; c++) {
                     // rounds are sized so |value| <= 2^24: an int32 holds it exactly
                     long long x = (long long)__float2int_rn(__uint_as_float(v[c]));
-                    if (sh >= 0) acc[half * 32 + c] += x << sh;
-                    else acc[half * 32 + c] += (x + (1ll << (-sh - 1))) >> (-sh);
+                    if (sh >= 0) acc[part * 16 + c] += x << sh;
+                    else acc[part * 16 + c] += (x + (1ll << (-sh - 1))) >> (-sh);
                 }
             }
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; c += 32) tmem_zero32(taddr + c);
             tmem_st_wait();
             tc_fence_before();
             __syncwarp();
@@ -763,8 +786,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (row < p.M) {
             const int ea = p.ea[row];
 #pragma unroll
-            for (int c = 0; c < 64; c += 2) {
-                const int col = n0 + h * 64 + c;
+            for (int c = 0; c < EPI_COLS; c += 2) {
+                const int col = n0 + h * EPI_COLS + c;
                 double v0 = 0, v1 = 0;
                 if (col < p.N) v0 = scale_pow2((double)acc[c], ubits + ea + p.eb[col]);
                 if (col + 1 < p.N) v1 = scale_pow2((double)acc[c + 1], ubits + ea + p.eb[col + 1]);
