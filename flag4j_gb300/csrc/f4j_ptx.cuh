@@ -131,6 +131,23 @@ __device__ __forceinline__ void umma_f8(uint32_t d_tmem, uint64_t a_desc, uint64
         : "memory");
 }
 
+// Two MMAs accumulating into d_tmem over consecutive K = 32 steps of 64-byte
+// swizzled rows: descriptor low words a_lo, b_lo (the second step 32 bytes on),
+// shared high word hi.
+__device__ __forceinline__ void umma_f8_k64(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo, uint32_t hi,
+                                            uint32_t idesc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t.reg .b32 a1, b1;\n\t"
+        "setp.ne.b32 p, %5, 0;\n\t"
+        "mov.b64 da, {%1, %3};\n\tmov.b64 db, {%2, %3};\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], da, db, %4, p;\n\t"
+        "add.u32 a1, %1, 2;\n\tadd.u32 b1, %2, 2;\n\t"
+        "mov.b64 da, {a1, %3};\n\tmov.b64 db, {b1, %3};\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], da, db, %4, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_lo), "r"(b_lo), "r"(hi), "r"(idesc), "r"(1u)
+        : "memory");
+}
+
 // Arrive on `bar` once all prior tcgen05.mma of this thread have completed.
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(

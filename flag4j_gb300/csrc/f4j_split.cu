@@ -32,7 +32,7 @@ namespace {
 
 constexpr int S_MAX = 12;          // at most 12 slices: F = 4 + 55 = 59 bits keeps Y < 2^62 in int64
 constexpr int BM = 128, BN = 128;  // output tile
-constexpr int BKB = 64;            // K bytes per tile load (one 64-byte swizzle row)
+constexpr int BKB = 64;            // K bytes per tile load (one 64-byte swizzle row; two K = 32 MMAs)
 // Ring geometry (compile-time): operand tiles per stage (2w + band - 1 for w
 // A slices per group) and stages in the shared-memory ring.
 #ifndef F4J_SPLIT_STAGE_TILES
@@ -46,6 +46,7 @@ constexpr int NSTAGE = F4J_SPLIT_NSTAGE;
 constexpr int RING = STAGE_TILES * NSTAGE;
 constexpr int NBUF = 4;            // TMEM accumulator buffers of BN columns (= levels per band)
 constexpr int TILE_BYTES = BM * BKB;  // 8 KB per operand tile
+static_assert(BKB == 64, "umma_f8_k64 issues the two K = 32 steps of one 64-byte K block");
 // Epilogue warps (compile-time, 8 or 16): each owns one TMEM lane quarter and
 // BN / (EPI_WARPS / 4) columns of the tile.
 #ifndef F4J_SPLIT_EPI_WARPS
@@ -55,7 +56,7 @@ constexpr int EPI_WARPS = F4J_SPLIT_EPI_WARPS;
 static_assert(EPI_WARPS == 8 || EPI_WARPS == 16, "8 or 16 epilogue warps");
 constexpr int EPI_COLS = BN / (EPI_WARPS / 4);
 constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA, warps 2.. epilogue
-constexpr int MAX_ROUNDS = 16, MAX_GROUPS = 64, MAX_LOADS = 512, MAX_OPS = 256;
+constexpr int MAX_ROUNDS = 16, MAX_GROUPS = 64, MAX_LOADS = 512, MAX_OPS = 96;
 
 // One round: the products A_i B_j of weight level t = i + j over one K chunk,
 // accumulated in one TMEM buffer.
@@ -82,9 +83,10 @@ struct Load {
     uint8_t slice;  // 0-based slice plane
 };
 struct Op {
-    uint16_t a_off, b_off;  // A / B tile offsets in the stage, in 16-byte units (descriptor address field)
-    uint16_t dcol;          // TMEM column of the first product's buffer
-    uint16_t wide;          // 1: N = 256 (B tiles b, b+1 into buffers dcol / BN and the next)
+    uint32_t a_off, b_off;  // A / B tile offsets in the stage, in 16-byte units (descriptor address field)
+    uint32_t dcol;          // TMEM column of the first product's buffer
+    uint32_t idesc;         // instruction descriptor: N = 256 (B tiles b, b+1 into buffers dcol / BN and
+                            // the next) or N = 128
 };
 struct Group {
     int16_t r0, nr;        // rounds [r0, r0 + nr)
@@ -308,10 +310,10 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
                     const bool wide = ((t - t0) % 2 == 0) && t + 1 <= tb;
                     if (no >= MAX_OPS) return -1;
                     Op op;
-                    op.a_off = (uint16_t)((i - c0) * (TILE_BYTES >> 4));
-                    op.b_off = (uint16_t)((na + (t - i) - jlo) * (TILE_BYTES >> 4));
-                    op.dcol = (uint16_t)((t - t0) * BN);
-                    op.wide = wide ? 1 : 0;
+                    op.a_off = (uint32_t)((i - c0) * (TILE_BYTES >> 4));
+                    op.b_off = (uint32_t)((na + (t - i) - jlo) * (TILE_BYTES >> 4));
+                    op.dcol = (uint32_t)((t - t0) * BN);
+                    op.idesc = umma_idesc_e4m3_f32(BM, wide ? 2 * BN : BN);
                     P->ops[no++] = op;
                     t += wide ? 2 : 1;
                 }
@@ -566,13 +568,24 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     for (int i = threadIdx.x; i < (int)(sizeof(SplitPlan) / 16); i += blockDim.x)
         reinterpret_cast<uint4*>(sp)[i] = reinterpret_cast<const uint4*>(plan)[i];
     const Group* gp = sp->groups;
-    const Op* opp = sp->ops;
     const Load* ldp = sp->loads;
+    // per ring slot, the ops with absolute descriptor low words and TMEM addresses
+    Op* opx = reinterpret_cast<Op*>(reinterpret_cast<unsigned char*>(sp) + sizeof(SplitPlan));
     const int nkb = plan->nkb, kcb = plan->kcb, nchunks = (nkb + kcb - 1) / kcb;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_slot;
+    {
+        const int nops = ngroups > 0 ? gp[ngroups - 1].op0 + gp[ngroups - 1].nop : 0;
+        const uint32_t lo0 = (uint32_t)umma_desc_sw64(sT);
+        for (int i = threadIdx.x; i < NSTAGE * nops; i += blockDim.x) {
+            const int st = i / nops, o = i % nops;
+            const Op O = sp->ops[o];
+            const uint32_t slot = lo0 + (uint32_t)(st * STAGE_TILES * (TILE_BYTES >> 4));
+            opx[st * MAX_OPS + o] = Op{slot + O.a_off, slot + O.b_off, tmem + O.dcol, O.idesc};
+        }
+    }
     if (warp >= 2) {
         // every MMA accumulates: the buffers start at zero (and are zeroed
         // again by the epilogue after each read)
@@ -646,15 +659,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     } else if (warp == 1) {
         // ---------------- MMA issuer (one thread)
         if (lane == 0) {
-            constexpr uint32_t idesc128 = umma_idesc_e4m3_f32(BM, BN);
-            constexpr uint32_t idesc256 = umma_idesc_e4m3_f32(BM, 2 * BN);
 #ifdef F4J_TRACE
             unsigned long long tr_wait = 0, tr_acc = 0, tr_ops = 0;
             const long long tr_start = clock64();
 #endif
-            // smem descriptor of tile slot t = base + t * (TILE_BYTES >> 4): the
-            // start-address field is the low bits and never carries out
-            const uint64_t desc0 = umma_desc_sw64(sT);
+            // smem descriptors differ only in the start-address field, the low 14
+            // bits of the low word (shared memory < 256 KB, so the op tables'
+            // precomputed low words never carry into the rest)
+            const uint32_t desc_hi = (uint32_t)(umma_desc_sw64(sT) >> 32);
             int st = 0;             // stages consumed, carried across tiles
             uint32_t used = 0;      // bit b: buffer b has been filled before
             uint32_t drained = 0;   // bit b: parity of the next accempty[b] phase to wait for
@@ -678,7 +690,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                             }
                             tc_fence_after();
                         }
-                        const Op* ops = opp + G.op0;
+                        const Op* ops = opx + G.op0;
                         for (int kb = kc; kb < kend; kb++, st++) {
                             const int s = st % NSTAGE;
                             F4J_T_BEGIN();
@@ -689,18 +701,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                                 break;
                             }
                             tc_fence_after();
-                            const uint64_t sdesc = desc0 + (uint64_t)(s * STAGE_TILES * (TILE_BYTES >> 4));
+                            const Op* so = ops + s * MAX_OPS;
 #pragma unroll 2
                             for (int o = 0; o < G.nop; o++) {
-                                const Op O = ops[o];
-                                const uint64_t da = sdesc + O.a_off, db = sdesc + O.b_off;
-                                const uint32_t dt = tmem + O.dcol;
-                                const uint32_t id = O.wide ? idesc256 : idesc128;
-#pragma unroll
-                                for (int kk = 0; kk < BKB / 32; kk++) {
-                                    // advance 32 bytes (= K 32 of e4m3) inside the swizzled row
-                                    umma_f8(dt, da + (uint64_t)(kk * 32 >> 4), db + (uint64_t)(kk * 32 >> 4), id, 1u);
-                                }
+                                const Op O = so[o];
+                                // K = 64: two K = 32 MMAs, the second 32 bytes on in the swizzled rows
+                                umma_f8_k64(O.dcol, O.a_off, O.b_off, desc_hi, O.idesc);
 #ifdef F4J_TRACE
                                 tr_ops++;
 #endif
@@ -960,7 +966,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     prm.status = ctx->d_status + F4J_ST_TIMEOUT;
     prm.plan = plan;
 
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan);
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
@@ -1121,7 +1127,7 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.C = C;
     prm.status = misc + 8;
     prm.plan = plan;
-    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan);
+    const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);

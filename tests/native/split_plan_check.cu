@@ -37,8 +37,10 @@ int main() {
         Op O = P.ops[G.op0 + o];
         const int U = TILE_BYTES >> 4;
         if (O.a_off % U || O.b_off % U || O.dcol % BN) { printf("op alignment\n"); bad++; continue; }
-        int la = O.a_off / U, lb = O.b_off / U, b0 = O.dcol / BN, nprod = O.wide ? 2 : 1;
-        if (O.wide && (b0 % 2)) { printf("wide op at odd buffer\n"); bad++; }
+        const bool wide = O.idesc == umma_idesc_e4m3_f32(BM, 2 * BN);
+        if (!wide && O.idesc != umma_idesc_e4m3_f32(BM, BN)) { printf("instruction descriptor\n"); bad++; }
+        int la = O.a_off / U, lb = O.b_off / U, b0 = O.dcol / BN, nprod = wide ? 2 : 1;
+        if (wide && (b0 % 2)) { printf("wide op at odd buffer\n"); bad++; }
         for (int u = 0; u < nprod; u++) {
           if (la >= G.nload || lb + u >= G.nload || b0 + u >= G.nr) { printf("op index\n"); bad++; continue; }
           Load a = P.loads[G.load0 + la], b = P.loads[G.load0 + lb + u];
