@@ -93,9 +93,12 @@ struct Group {
     int16_t load0, nload;  // load list (per K block)
     int16_t op0, nop;      // MMA list (per K block)
     int32_t flags;         // GF_CONT_IN: keeps accumulating into the previous group's
-                           // buffers; GF_CONT_OUT: its rounds continue in the next group
+                           // buffers; GF_CONT_OUT: its rounds continue in the next group;
+                           // bits 8-11: buffers first used in the band by this group (the
+                           // epilogue must have drained them before its MMAs); bits 12-15:
+                           // buffers last used in the band by this group (complete after it)
 };
-constexpr int GF_CONT_IN = 1, GF_CONT_OUT = 2;
+constexpr int GF_CONT_IN = 1, GF_CONT_OUT = 2, GF_ACQ_SHIFT = 8, GF_REL_SHIFT = 12;
 
 // Decided on the device from the exponent statistics (k_plan), so a split
 // GEMM never waits for the host between its kernels.  The group / round
@@ -280,6 +283,7 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
         }
         // A slices with a partner in the band
         const int ilo = t0 - s > 1 ? t0 - s : 1, ihi = t1 - 1 < s ? t1 - 1 : s;
+        const int gband = ng;  // the band's first group
         for (int c0 = ilo; c0 <= ihi; c0 += w) {
             const int c1 = c0 + w - 1 < ihi ? c0 + w - 1 : ihi;
             const int jlo = t0 - c1 > 1 ? t0 - c1 : 1, jhi = t1 - c0 < s ? t1 - c0 : s;
@@ -321,6 +325,26 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
             g.nop = (int16_t)(no - g.op0);
             P->groups[ng++] = g;
         }
+        // each buffer is acquired by the first group of the band that uses it and
+        // released by the last one (a buffer no group uses: first / last group)
+        const uint32_t all = (1u << (t1 - t0 + 1)) - 1u;
+        uint32_t seen = 0, later = 0;
+        for (int q = gband; q < ng; q++) {
+            uint32_t m = 0;
+            for (int o = P->groups[q].op0; o < P->groups[q].op0 + P->groups[q].nop; o++)
+                m |= (P->ops[o].idesc == umma_idesc_e4m3_f32(BM, 2 * BN) ? 3u : 1u) << (P->ops[o].dcol / BN);
+            P->groups[q].flags |= (int32_t)((m & ~seen) << GF_ACQ_SHIFT);
+            seen |= m;
+            P->groups[q].flags |= (int32_t)(m << 16);  // scratch: this group's use mask
+        }
+        for (int q = ng - 1; q >= gband; q--) {
+            const uint32_t m = ((uint32_t)P->groups[q].flags >> 16) & 15u;
+            P->groups[q].flags &= 0xFFFF;
+            P->groups[q].flags |= (int32_t)((m & ~later) << GF_REL_SHIFT);
+            later |= m;
+        }
+        P->groups[gband].flags |= (int32_t)((all & ~seen) << GF_ACQ_SHIFT);
+        P->groups[ng - 1].flags |= (int32_t)((all & ~seen) << GF_REL_SHIFT);
     }
     P->ngroups = ng;
     return nr;
@@ -675,18 +699,20 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
                     for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
                         const Group G = gp[g];
-                        if (!(G.flags & GF_CONT_IN)) {
-                            // the band's buffers must have been read (and zeroed) by the epilogue
-                            for (int b = 0; b < G.nr; b++) {
-                                if (!((used >> b) & 1)) continue;
+                        const uint32_t acq = ((uint32_t)G.flags >> GF_ACQ_SHIFT) & 15u;
+                        const uint32_t rel = ((uint32_t)G.flags >> GF_REL_SHIFT) & 15u;
+                        if (acq & used) {
+                            // buffers this group is first in its band to use must have
+                            // been read (and zeroed) by the epilogue
+                            uint32_t wq = acq & used;
+                            while (wq) {
+                                const int b = __ffs(wq) - 1;
+                                wq &= wq - 1;
                                 F4J_T_BEGIN();
                                 const bool okw = mbar_wait(&accempty[b], (drained >> b) & 1, p.status, 12);
                                 F4J_T_ADD(tr_acc);
                                 drained ^= 1u << b;
-                                if (!okw) {
-                                    abort_flag = 1;
-                                    break;
-                                }
+                                if (!okw) abort_flag = 1;
                             }
                             tc_fence_after();
                         }
@@ -713,9 +739,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                             }
                             umma_commit(&empty[s]);
                         }
-                        if (!(G.flags & GF_CONT_OUT)) {
-                            for (int b = 0; b < G.nr; b++) umma_commit(&accfull[b]);
-                            used |= (1u << G.nr) - 1u;
+                        if (rel) {
+                            // buffers whose level is complete: to the epilogue
+                            for (uint32_t wr = rel; wr; wr &= wr - 1) umma_commit(&accfull[__ffs(wr) - 1]);
+                            used |= rel;
                         }
                     }
                 }

@@ -4,8 +4,10 @@
 // product A_i B_j with i + j <= s + 1 exactly once per K block, that every MMA's
 // tile and TMEM indices are in range (wide MMAs start at an even buffer and
 // cover two adjacent levels), that a stage never exceeds STAGE_TILES tiles,
-// that each round respects the exact-FP32 budget s * kchunk * 256 <= 2^24, and
-// that continuation chains between groups are well formed.  Exit status 0 on
+// that each round respects the exact-FP32 budget s * kchunk * 256 <= 2^24,
+// that continuation chains between groups are well formed, and that within a
+// band every TMEM buffer is acquired once before its first MMA and released
+// once after its last.  Exit status 0 on
 // success.  Launches no kernel.
 #include "../../flag4j_gb300/csrc/f4j_split.cu"
 #include <cstdio>
@@ -25,8 +27,13 @@ int main() {
     std::multiset<int> seen;
     long long mmas = 0, instr = 0;
     int prev_out = 0, prev_r0 = -1;
+    unsigned held = 0, acq_all = 0, rel_all = 0;
     for (int g = 0; g < P.ngroups; g++) {
       Group G = P.groups[g];
+      const unsigned acq = ((unsigned)G.flags >> GF_ACQ_SHIFT) & 15u, rel = ((unsigned)G.flags >> GF_REL_SHIFT) & 15u;
+      if (!(G.flags & GF_CONT_IN)) { held = 0; acq_all = 0; rel_all = 0; }
+      if ((acq & acq_all) || (acq & held)) { printf("buffer acquired twice\n"); bad++; }
+      held |= acq; acq_all |= acq;
       if (G.nr > NBUF || G.nr < 1) { printf("nr\n"); bad++; }
       if (G.nload > STAGE_TILES) { printf("stage size %d\n", G.nload); bad++; }
       bool cin = G.flags & GF_CONT_IN;
@@ -47,12 +54,19 @@ int main() {
           if (a.which != 0 || b.which != 1) { printf("operand kind\n"); bad++; }
           Round R = P.rounds[G.r0 + b0 + u];
           if (R.buf != b0 + u) { printf("round buffer\n"); bad++; }
+          if (!((held >> (b0 + u)) & 1)) { printf("op on a buffer not held\n"); bad++; }
           int i = a.slice + 1, j = b.slice + 1;
           if (i + j != R.level || i < R.i0 || i >= R.i1) { printf("op level mismatch\n"); bad++; }
           seen.insert(i * 64 + j);
           mmas += 1;
         }
         instr++;
+      }
+      if ((rel & ~held) || (rel & rel_all)) { printf("release of a buffer not held\n"); bad++; }
+      held &= ~rel; rel_all |= rel;
+      if (!(G.flags & GF_CONT_OUT)) {
+        const unsigned all = (1u << G.nr) - 1u;
+        if (held || acq_all != all || rel_all != all) { printf("band buffers not acquired and released once\n"); bad++; }
       }
     }
     if (prev_out) { printf("dangling continuation\n"); bad++; }
