@@ -335,7 +335,8 @@ def run_reference(args):
 
 # ---------------------------------------------------------------- sparse products
 def sparse_section(E, full, steps=20):
-    """CSR SpMV / SpMM (32 columns) at 2^20 rows, Poisson(16) row lengths."""
+    """CSR SpMV / SpMM (32 and 64 columns), S^T dC and SDDMM (64 columns), COO sort and COO -> CSR,
+    at 2^20 rows with Poisson(16) row lengths."""
     from flag4j_gb300 import synth
     rows = (1 << 20) if full else (1 << 16)
     rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
@@ -357,7 +358,59 @@ def sparse_section(E, full, steps=20):
            "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
            "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
            "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True}
-    del x, y, X, Y, S
+    del x, y, X, Y
+
+    # ---- structure: stable COO sort of shuffled triplets, then COO -> CSR
+    # (CooMatrix.sortIndices, CooMatrix.toCsr); each timed around the call only
+    r_s, c_s, v_s = synth.coo_shuffled(rp, ci, v, seed=7)
+    r_s, c_s = r_s.astype(np.int32), c_s.astype(np.int32)
+    dr, dc, dv = E.ctx.alloc(4 * nnz), E.ctx.alloc(4 * nnz), E.ctx.alloc(8 * nnz)
+    sort_ms = []
+    for i in range(3 + steps // 4):
+        dr.upload(r_s), dc.upload(c_s), dv.upload(v_s)
+        E.ctx.sync()
+        E.ctx.timer_record(0)
+        E.check(E.lib.f4j_coo_sort(E.ctx.handle, nnz, dr.handle, dc.handle, dv.handle))
+        E.ctx.timer_record(1)
+        if i >= 3:
+            sort_ms.append(E.ctx.timer_elapsed(0, 1))
+    conv_ms = []
+    for i in range(3 + steps // 4):
+        h = ctypes.c_void_p()
+        E.ctx.sync()
+        E.ctx.timer_record(0)
+        E.check(E.lib.f4j_csr_from_coo(E.ctx.handle, rows, rows, nnz, dr.handle, dc.handle, dv.handle,
+                                       ctypes.byref(h)))
+        E.ctx.timer_record(1)
+        if i >= 3:
+            conv_ms.append(E.ctx.timer_elapsed(0, 1))
+        E.lib.f4j_csr_free(E.ctx.handle, h)
+    t_sort, t_conv = statistics.median(sort_ms), statistics.median(conv_ms)
+    b_sort = 2 * 16.0 * nnz  # triplets read and written once (algorithmic; a radix pass moves them more)
+    b_conv = 16.0 * nnz + 4.0 * nnz + 8.0 * nnz + 4.0 * (rows + 1)  # triplets in; cols, vals, rowptr out
+    res.update({"coo_sort_ms": t_sort, "coo_sort_gbs": b_sort / t_sort / 1e6,
+                "coo_to_csr_ms": t_conv, "coo_to_csr_gbs": b_conv / t_conv / 1e6,
+                "coo_to_csr_note": "time includes the new handle's device allocations and the range checks"})
+    del dr, dc, dv
+
+    # ---- sparse adjoint at 64 columns (S^T dC through the cached permutation, SDDMM)
+    X64 = E.dev(synth.normal(rows, 64, 8))
+    dC64 = E.dev(synth.normal(rows, 64, 9))
+    Y64 = E.ctx.alloc(8 * rows * 64)
+    dS = E.ctx.alloc(8 * nnz)
+    t_spmm64 = E.timed(lambda: E.check(E.lib.f4j_spmm(E.ctx.handle, hS, X64.handle, 64, Y64.handle, None)), steps, 3)
+    t_spmmt = E.timed(lambda: E.check(E.lib.f4j_spmm_t(E.ctx.handle, hS, dC64.handle, 64, Y64.handle, None)),
+                      steps, 3)
+    t_sddmm = E.timed(lambda: E.check(E.lib.f4j_sddmm(E.ctx.handle, hS, dC64.handle, X64.handle, 64, dS.handle,
+                                                      None)), steps, 3)
+    b_spmm64 = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 64 * rows
+    b_spmmt = b_spmm64 + 4.0 * nnz
+    b_sddmm = 4.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 64 * rows + 8.0 * nnz
+    res.update({"spmm64_ms": t_spmm64, "spmm64_gbs_compulsory": b_spmm64 / t_spmm64 / 1e6,
+                "spmm_t64_ms": t_spmmt, "spmm_t64_gbs_compulsory": b_spmmt / t_spmmt / 1e6,
+                "sddmm64_ms": t_sddmm, "sddmm64_gbs_compulsory": b_sddmm / t_sddmm / 1e6,
+                "sddmm64_gflops": 2.0 * 64 * nnz / t_sddmm / 1e6})
+    del X64, dC64, Y64, dS, S
     return res
 
 

@@ -526,7 +526,7 @@ __device__ __forceinline__ double scale_pow2(double v, int X) {
 // TILE_GROUP_M x ~(grid / TILE_GROUP_M) block: each B slice tile they load is
 // shared by up to TILE_GROUP_M of them in L2, each A slice tile by the rest.
 #ifndef F4J_SPLIT_GROUP_M
-#define F4J_SPLIT_GROUP_M 16
+#define F4J_SPLIT_GROUP_M 8
 #endif
 constexpr int TILE_GROUP_M = F4J_SPLIT_GROUP_M;
 __device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, int& m0, int& n0) {
