@@ -8,7 +8,7 @@ This package mirrors the reference types that reach those products.
 """
 from ._lib import Flag4jDeviceException, load as load_library  # noqa: F401
 from .adjoint import MatMulNode, SpMMNode  # noqa: F401
-from .arrays import CMatrix, CooMatrix, CsrMatrix, Matrix, Shape, Vector  # noqa: F401
+from .arrays import CMatrix, CooMatrix, CsrCMatrix, CsrMatrix, CVector, Matrix, Shape, Vector  # noqa: F401
 from .device import (Context, IllegalArgumentException, LinearAlgebraException, default_context,  # noqa: F401
                      gemm_mode, set_gemm_mode)
 

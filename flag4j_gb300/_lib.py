@@ -82,6 +82,7 @@ SIGNATURES = {
     "f4j_csr_transpose_perm": (_i, [_v, _v, _v]),
     "f4j_spmv": (_i, [_v, _v, _v, _v, _rep]),
     "f4j_spmm": (_i, [_v, _v, _v, _i64, _v, _rep]),
+    "f4j_zspmm": (_i, [_v, _v, _v, _i64, _v, _rep]),
     "f4j_spmm_t": (_i, [_v, _v, _v, _i64, _v, _rep]),
     "f4j_sddmm": (_i, [_v, _v, _v, _v, _i64, _v, _rep]),
 }

@@ -122,6 +122,25 @@ class Vector(_Dense):
     __hash__ = None
 
 
+class CVector(_Dense):
+    """Complex128 dense vector (interleaved re/im on the device)."""
+
+    _dtype = np.complex128
+
+    def __init__(self, entries):
+        arr = np.asarray(entries, dtype=np.complex128).reshape(-1)
+        self._init_host(Shape(arr.size), arr)
+
+    @property
+    def size(self):
+        return self.shape[0]
+
+    def __eq__(self, other):
+        return isinstance(other, CVector) and self.shape == other.shape and _nan_equal(self.data, other.data)
+
+    __hash__ = None
+
+
 class Matrix(_Dense):
     """Real dense matrix: Matrix(double[][]), Matrix(Shape, double...), Matrix(rows, cols)."""
 
@@ -163,8 +182,18 @@ class Matrix(_Dense):
             bm = Matrix._from_device(Shape(b.size, 1), b.device(), b._ctx)
             out = _gemm(self, bm, _lib.OP_N, _lib.OP_N, self.numRows, 1, self.numCols, mode, report)
             return Vector._from_device(Shape(self.numRows), out._dev, out._ctx)
-        if isinstance(b, CMatrix):
-            raise NotImplementedError("mixed real x complex products are not on this engine's path")
+        if isinstance(b, (CMatrix, CVector)):
+            # Matrix.mult(CMatrix / CVector) (MatrixMultiplyDispatcher.java:71-200): every variant sums
+            # a[i][k] * b[k][j] per real / imaginary part in ascending k, so the product is the real
+            # GEMM of this matrix with b's interleaved storage read as a real k x 2n matrix
+            vec = isinstance(b, CVector)
+            n = 1 if vec else b.numCols
+            ensure_mat_mult_shapes(self.shape, Shape(b.size, 1) if vec else b.shape)
+            ctx = self._ctx or b._ctx or default_context()
+            out = _gemm_bufs(ctx, False, self.numRows, 2 * n, self.numCols, self.device(ctx), _lib.OP_N,
+                             b.device(ctx), _lib.OP_N, mode, report)
+            return (CVector._from_device(Shape(self.numRows), out, ctx) if vec
+                    else CMatrix._from_device(Shape(self.numRows, n), out, ctx))
         ensure_mat_mult_shapes(self.shape, b.shape)
         return _gemm(self, b, _lib.OP_N, _lib.OP_N, self.numRows, b.numCols, self.numCols, mode, report)
 
@@ -220,9 +249,22 @@ class CMatrix(_Dense):
         return CMatrix(self.toNumpy().conj().T.copy())
 
     def mult(self, b, mode=None, report=None):
-        """CMatrix.mult(CMatrix) on the GPU."""
-        ensure_mat_mult_shapes(self.shape, b.shape)
-        return _gemm(self, b, _lib.OP_N, _lib.OP_N, self.numRows, b.numCols, self.numCols, mode, report)
+        """CMatrix.mult(CMatrix / CVector / Matrix / Vector) on the GPU.
+
+        A real operand (CMatrix.mult(Matrix), MatrixMultiplyDispatcher.java:201-260) is promoted to
+        complex with zero imaginary parts: each extra product is a signed zero, which leaves every
+        k-ascending sum unchanged, so EXACT mode stays bit-identical."""
+        vec = isinstance(b, (Vector, CVector))
+        if isinstance(b, (Matrix, Vector)):
+            arr = b.toNumpy() if isinstance(b, Matrix) else b.data
+            b = (CVector if vec else CMatrix)(np.asarray(arr, dtype=np.complex128))
+        n = 1 if vec else b.numCols
+        ensure_mat_mult_shapes(self.shape, Shape(b.size, 1) if vec else b.shape)
+        ctx = self._ctx or b._ctx or default_context()
+        out = _gemm_bufs(ctx, True, self.numRows, n, self.numCols, self.device(ctx), _lib.OP_N, b.device(ctx),
+                         _lib.OP_N, mode, report)
+        return (CVector._from_device(Shape(self.numRows), out, ctx) if vec
+                else CMatrix._from_device(Shape(self.numRows, n), out, ctx))
 
     def __eq__(self, other):
         return isinstance(other, CMatrix) and self.shape == other.shape and _nan_equal(self.data, other.data)
@@ -230,17 +272,22 @@ class CMatrix(_Dense):
     __hash__ = None
 
 
-def _gemm(a, b, opA, opB, m, n, k, mode, report):
-    ctx = a._ctx or b._ctx or default_context()
-    cplx = isinstance(a, CMatrix)
+def _gemm_bufs(ctx, cplx, m, n, k, abuf, opA, bbuf, opB, mode, report):
+    """f4j_zgemm / f4j_dgemm on device buffers; returns the new output buffer."""
     out = ctx.alloc(max(m * n * (16 if cplx else 8), 8))
     rep = _lib.f4j_report()
     fn = ctx.lib.f4j_zgemm if cplx else ctx.lib.f4j_dgemm
     md = gemm_mode() if mode is None else _lib.MODES.get(mode, mode)
-    check(fn(ctx.handle, m, n, k, a.device(ctx).handle, opA, b.device(ctx).handle, opB, out.handle, md,
-             ctypes.byref(rep)))
+    check(fn(ctx.handle, m, n, k, abuf.handle, opA, bbuf.handle, opB, out.handle, md, ctypes.byref(rep)))
     if report is not None:
         report.update(rep.as_dict())
+    return out
+
+
+def _gemm(a, b, opA, opB, m, n, k, mode, report):
+    ctx = a._ctx or b._ctx or default_context()
+    cplx = isinstance(a, CMatrix)
+    out = _gemm_bufs(ctx, cplx, m, n, k, a.device(ctx), opA, b.device(ctx), opB, mode, report)
     cls = CMatrix if cplx else Matrix
     return cls._from_device(Shape(m, n), out, ctx)
 
@@ -285,9 +332,11 @@ def validate_csr(shape, nnz, row_pointers, col_indices):
 class CsrMatrix:
     """CSR matrix: CsrMatrix(Shape, double[] data, int[] rowPointers, int[] colIndices)."""
 
+    _vdtype = np.float64
+
     def __init__(self, shape, data, row_pointers, col_indices, validate=True):
         self.shape = Shape(shape)
-        self._data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        self._data = np.ascontiguousarray(data, dtype=self._vdtype).reshape(-1)
         self._rp = np.ascontiguousarray(row_pointers, dtype=np.int32).reshape(-1)
         self._ci = np.ascontiguousarray(col_indices, dtype=np.int32).reshape(-1)
         self.nnz = int(self._data.size)
@@ -317,7 +366,7 @@ class CsrMatrix:
         L, h = self._ctx.lib, self._ctx.handle
         self._rp = np.empty(self.numRows + 1, np.int32)
         self._ci = np.empty(self.nnz, np.int32)
-        self._data = np.empty(self.nnz, np.float64)
+        self._data = np.empty(self.nnz, self._vdtype)
         for buf, arr in ((rp, self._rp), (ci, self._ci), (v, self._data)):
             if arr.nbytes:
                 check(L.f4j_buf_download(h, buf, arr.ctypes.data, arr.nbytes, 0))
@@ -346,7 +395,7 @@ class CsrMatrix:
         if self._handle is None or self._ctx is not ctx:
             rp = ctx.from_numpy(self._rp)
             ci = ctx.from_numpy(self._ci if self.nnz else np.zeros(1, np.int32))
-            v = ctx.from_numpy(self._data if self.nnz else np.zeros(1))
+            v = ctx.from_numpy(self._data if self.nnz else np.zeros(1, self._vdtype))
             h = ctypes.c_void_p()
             check(ctx.lib.f4j_csr_wrap(ctx.handle, self.numRows, self.numCols, self.nnz, rp.handle, ci.handle,
                                        v.handle, 0, ctypes.byref(h)))
@@ -370,6 +419,22 @@ class CsrMatrix:
             check(ctx.lib.f4j_spmm(ctx.handle, self.handle(ctx), b.device(ctx).handle, b.numCols, y.handle,
                                    ctypes.byref(rep)))
             out = Matrix._from_device(Shape(self.numRows, b.numCols), y, ctx)
+        elif isinstance(b, (CMatrix, CVector)):
+            # CsrMatrix.mult(CMatrix) -> RealFieldDenseCsrMatMult.standard (RealFieldDenseCsrMatMult.java:62-91):
+            # y[i][j] += x[col][j] * v per part in storage order, i.e. the real SpMM over b's interleaved
+            # storage with 2 * ncols real columns
+            vec = isinstance(b, CVector)
+            nc = 1 if vec else b.numCols
+            if vec:
+                ensure_all_equal(self.numCols, b.size)
+            else:
+                ensure_mat_mult_shapes(self.shape, b.shape)
+            ctx = self._ctx or b._ctx or default_context()
+            y = ctx.alloc(max(16 * self.numRows * nc, 16))
+            check(ctx.lib.f4j_spmm(ctx.handle, self.handle(ctx), b.device(ctx).handle, 2 * nc, y.handle,
+                                   ctypes.byref(rep)))
+            out = (CVector._from_device(Shape(self.numRows), y, ctx) if vec
+                   else CMatrix._from_device(Shape(self.numRows, nc), y, ctx))
         else:
             raise NotImplementedError("CsrMatrix.mult(%s) is not on this engine's path" % type(b).__name__)
         if report is not None:
@@ -422,6 +487,52 @@ class CsrMatrix:
             self.close()
         except Exception:
             pass
+
+
+class CsrCMatrix(CsrMatrix):
+    """Complex CSR matrix: CsrCMatrix(Shape, Complex128[] data, int[] rowPointers, int[] colIndices)."""
+
+    _vdtype = np.complex128
+
+    def mult(self, b, report=None):
+        """CsrCMatrix.mult(CMatrix / CVector) -> DenseCsrSemiringMatMult.standard / standardVector
+        (DenseCsrSemiringMatMult.java:59-98, :140-160), bit-identical."""
+        if not isinstance(b, (CMatrix, CVector)):
+            raise NotImplementedError("CsrCMatrix.mult(%s) is not on this engine's path" % type(b).__name__)
+        vec = isinstance(b, CVector)
+        nc = 1 if vec else b.numCols
+        if vec:
+            ensure_all_equal(self.numCols, b.size)
+        else:
+            ensure_mat_mult_shapes(self.shape, b.shape)
+        ctx = self._ctx or b._ctx or default_context()
+        rep = _lib.f4j_report()
+        y = ctx.alloc(max(16 * self.numRows * nc, 16))
+        check(ctx.lib.f4j_zspmm(ctx.handle, self.handle(ctx), b.device(ctx).handle, nc, y.handle, ctypes.byref(rep)))
+        if report is not None:
+            report.update(rep.as_dict())
+        return (CVector._from_device(Shape(self.numRows), y, ctx) if vec
+                else CMatrix._from_device(Shape(self.numRows, nc), y, ctx))
+
+    def multTransposeLeft(self, b):
+        raise NotImplementedError("complex CSR transposes are not on this engine's path")
+
+    def T(self):
+        raise NotImplementedError("complex CSR transposes are not on this engine's path")
+
+    def toDense(self):
+        out = np.zeros(self.shape, np.complex128)
+        rp, ci, v = self.rowPointers, self.colIndices, self.data
+        for i in range(self.numRows):
+            out[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        return CMatrix(out)
+
+    def __eq__(self, other):
+        if not isinstance(other, CsrCMatrix) or self.shape != other.shape:
+            return False
+        return self.toDense() == other.toDense()
+
+    __hash__ = None
 
 
 class CooMatrix:

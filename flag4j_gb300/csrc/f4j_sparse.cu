@@ -126,6 +126,50 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Complex CSR x complex dense (CsrCMatrix.mult(CMatrix) ->
+// DenseCsrSemiringMatMult.standard, src/main/java/org/flag4j/linalg/ops/
+// dense_sparse/csr/semiring_ops/DenseCsrSemiringMatMult.java:59-98): a group
+// of G lanes owns one row, a lane one complex column; per nonzero in storage
+// order y += x * v with Complex128.mult's rounding (Complex128.java:336-341):
+// pr = xr*vr - xi*vi, pi = xr*vi + xi*vr, each product and sum rounded.
+__global__ void __launch_bounds__(256)
+    k_zspmm(int64_t rows, int64_t ncols, int G, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+            const double2* __restrict__ vals, const double2* __restrict__ X, double2* __restrict__ Y) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x % G;
+    if (row >= rows) return;
+    const int q0 = rowptr[row], q1 = rowptr[row + 1];
+    for (int64_t c0 = lane; c0 < ncols; c0 += G) {
+        double ar = 0.0, ai = 0.0;
+        int q = q0;
+        constexpr int UN = 8;  // nonzeros whose X entries are in flight together
+        for (; q + UN <= q1; q += UN) {
+            double2 v[UN], x[UN];
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+                v[u] = __ldg(&vals[q + u]);
+                x[u] = __ldg(&X[(int64_t)__ldg(&colidx[q + u]) * ncols + c0]);
+            }
+#pragma unroll
+            for (int u = 0; u < UN; u++) {
+                const double pr = __dsub_rn(__dmul_rn(x[u].x, v[u].x), __dmul_rn(x[u].y, v[u].y));
+                const double pi = __dadd_rn(__dmul_rn(x[u].x, v[u].y), __dmul_rn(x[u].y, v[u].x));
+                ar = __dadd_rn(ar, pr);
+                ai = __dadd_rn(ai, pi);
+            }
+        }
+        for (; q < q1; q++) {
+            const double2 v = __ldg(&vals[q]);
+            const double2 x = __ldg(&X[(int64_t)__ldg(&colidx[q]) * ncols + c0]);
+            const double pr = __dsub_rn(__dmul_rn(x.x, v.x), __dmul_rn(x.y, v.y));
+            const double pi = __dadd_rn(__dmul_rn(x.x, v.y), __dmul_rn(x.y, v.x));
+            ar = __dadd_rn(ar, pr);
+            ai = __dadd_rn(ai, pi);
+        }
+        Y[row * ncols + c0] = make_double2(ar, ai);
+    }
+}
+
 // ------------------------------------------------------------------ SDDMM
 // Warp per row of S; half-warps take alternate nonzeros; a lane owns 4
 // columns of each 64-column pass (sequential), then a 16-lane tree sum.
@@ -795,6 +839,37 @@ extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_b
         *rep = f4j_report{};
         rep->flops = 2.0 * S->nnz * ncols;
         rep->bytes = 12.0 * S->nnz + 4.0 * (S->rows + 1) + 8.0 * ncols * (S->cols + S->rows);
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}
+
+extern "C" int f4j_zspmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!S || !X || !Y) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
+    if (S->vals->bytes < (size_t)S->nnz * 16)
+        return f4j_fail(F4J_ERR_ARG, "complex CSR values need 16 bytes per nonzero (nnz=%lld)", (long long)S->nnz);
+    if (X->bytes < (size_t)S->cols * ncols * 16) return f4j_fail(F4J_ERR_ARG, "X buffer too small");
+    if (Y->bytes < (size_t)S->rows * ncols * 16) return f4j_fail(F4J_ERR_ARG, "Y buffer too small");
+    if (!f4j_aligned16(S->vals->ptr) || !f4j_aligned16(X->ptr) || !f4j_aligned16(Y->ptr))
+        return f4j_fail(F4J_ERR_ARG, "complex buffers must be 16-byte aligned");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    if (S->rows && ncols) {
+        int G = 1;
+        while (G < 32 && G < ncols) G *= 2;
+        f4j_prof_begin(ctx);
+        k_zspmm<<<(unsigned)f4j_cdiv(S->rows * G, 256), 256, 0, ctx->stream>>>(
+            S->rows, ncols, G, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double2*)S->vals->ptr,
+            (const double2*)X->ptr, (double2*)Y->ptr);
+        f4j_prof_end(ctx);
+        F4J_LAUNCHED(ctx);
+    }
+    if (rep) {
+        *rep = f4j_report{};
+        rep->flops = 8.0 * S->nnz * ncols;
+        rep->bytes = 20.0 * S->nnz + 4.0 * (S->rows + 1) + 16.0 * ncols * (S->cols + S->rows);
         rep->launches = (int32_t)(ctx->launches - l0);
     }
     return F4J_OK;

@@ -214,6 +214,16 @@ int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* report);
  * -> RealCsrDenseMatMult.standard (CsrMatrix.java:1498-1499,
  * RealCsrDenseMatMult.java:55-82).  Bit-identical. */
 int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* report);
+/* Y(rows x ncols) = S X for a complex CSR S and complex dense X, Y
+ * (interleaved re/im): S is a CSR handle whose value buffer holds nnz complex
+ * values (16 bytes each, as CsrCMatrix.data).  Bit-identical to
+ * CsrCMatrix.mult(CMatrix) -> DenseCsrSemiringMatMult.standard
+ * (src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/semiring_ops/
+ * DenseCsrSemiringMatMult.java:59-98), ncols = 1 for CsrCMatrix.mult(CVector).
+ * A real CSR times a complex dense matrix (CsrMatrix.mult(CMatrix),
+ * RealFieldDenseCsrMatMult.java:62-91) is f4j_spmm on X's interleaved storage
+ * with 2 * ncols real columns. */
+int f4j_zspmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* report);
 /* dX(cols x ncols) = S^T dC without forming S^T: gathers through a cached
  * transpose permutation (built on first use); atomic-free.  Bit-identical to
  * S.T().mult(dC) in the reference. */

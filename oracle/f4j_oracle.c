@@ -191,6 +191,62 @@ void orc_zgemm(int64_t m, int64_t n, int64_t k, const double* A, const double* B
 }
 
 /* ------------------------------------------------------------------ */
+/* Mixed real / complex dense products                                  */
+/* RealFieldDenseMatMult.reordered (…/dense/real_field_ops/              */
+/* RealFieldDenseMatMult.java:99-135), the order of every variant the   */
+/* MatrixMultiplyDispatcher picks for Matrix.mult(CMatrix) (:139-200):  */
+/*   dest[i][j] = dest[i][j].add(B[k][j].mult(a[i][k])), k ascending;    */
+/* Complex128.mult(double) scales both parts, so each part is a real    */
+/* k-ascending no-FMA sum.  CMatrix.mult(Matrix) (:201-260, kernels     */
+/* :618-655): dest[i][j] += A[i][k].mult(b[k][j]), the same per part.   */
+/* ------------------------------------------------------------------ */
+static void orc_rzgemm_rows(void* p, int64_t r0, int64_t r1) {
+    orc_gemm_args* g = (orc_gemm_args*)p;  /* A real m x k, B complex k x n */
+    const int64_t n = g->n, k = g->k;
+    for (int64_t i = r0; i < r1; i++) {
+        double* dst = g->C + 2 * i * n;
+        for (int64_t j = 0; j < 2 * n; j++) dst[j] = 0.0;
+        for (int64_t kk = 0; kk < k; kk++) {
+            const double a = g->A[i * k + kk];
+            const double* brow = g->B + 2 * kk * n;
+            for (int64_t j = 0; j < n; j++) {
+                double pr = brow[2 * j] * a, pi = brow[2 * j + 1] * a;
+                dst[2 * j] = dst[2 * j] + pr;
+                dst[2 * j + 1] = dst[2 * j + 1] + pi;
+            }
+        }
+    }
+}
+
+void orc_rzgemm(int64_t m, int64_t n, int64_t k, const double* A, const double* B, double* C, int threads) {
+    orc_gemm_args g = {m, n, k, A, B, C};
+    orc_parallel_rows(m, threads, orc_rzgemm_rows, &g);
+}
+
+static void orc_zrgemm_rows(void* p, int64_t r0, int64_t r1) {
+    orc_gemm_args* g = (orc_gemm_args*)p;  /* A complex m x k, B real k x n */
+    const int64_t n = g->n, k = g->k;
+    for (int64_t i = r0; i < r1; i++) {
+        double* dst = g->C + 2 * i * n;
+        for (int64_t j = 0; j < 2 * n; j++) dst[j] = 0.0;
+        for (int64_t kk = 0; kk < k; kk++) {
+            const double ar = g->A[2 * (i * k + kk)], ai = g->A[2 * (i * k + kk) + 1];
+            const double* brow = g->B + kk * n;
+            for (int64_t j = 0; j < n; j++) {
+                double pr = ar * brow[j], pi = ai * brow[j];
+                dst[2 * j] = dst[2 * j] + pr;
+                dst[2 * j + 1] = dst[2 * j + 1] + pi;
+            }
+        }
+    }
+}
+
+void orc_zrgemm(int64_t m, int64_t n, int64_t k, const double* A, const double* B, double* C, int threads) {
+    orc_gemm_args g = {m, n, k, A, B, C};
+    orc_parallel_rows(m, threads, orc_zrgemm_rows, &g);
+}
+
+/* ------------------------------------------------------------------ */
 /* CSR x dense                                                          */
 /* RealCsrDenseMatMult.standardVector (…/dense_sparse/csr/real/          */
 /* RealCsrDenseMatMult.java:172-192): y[i] += v*x[col] in storage order. */
@@ -244,6 +300,65 @@ void orc_spmm(int64_t rows, int64_t ncols, const int32_t* rowptr, const int32_t*
               const double* vals, const double* X, double* Y, int threads) {
     orc_csr_args a = {ncols, rowptr, colidx, vals, X, Y};
     orc_parallel_rows(rows, threads, orc_spmm_rows, &a);
+}
+
+/* Real CSR x complex dense: RealFieldDenseCsrMatMult.standard          */
+/* (…/dense_sparse/csr/real_field_ops/RealFieldDenseCsrMatMult.java:    */
+/* 62-91): Y[i][j] = Y[i][j].add(X[col][j].mult(v)) in storage order.   */
+/* Complex CSR x complex dense: DenseCsrSemiringMatMult.standard        */
+/* (…/dense_sparse/csr/semiring_ops/DenseCsrSemiringMatMult.java:59-98) */
+/* over Complex128: Y[i][j] = Y[i][j].add(X[col][j].mult(v)) with        */
+/* Complex128.mult (Complex128.java:336-341) of x = X[col][j] by v:      */
+/*   pr = xr*vr - xi*vi ; pi = xr*vi + xi*vr.                            */
+/* X, Y interleaved complex; vals interleaved complex for the latter.   */
+static void orc_spmm_rz_rows(void* p, int64_t r0, int64_t r1) {
+    orc_csr_args* a = (orc_csr_args*)p;
+    const int64_t nc = a->ncols;
+    for (int64_t i = r0; i < r1; i++) {
+        double* dst = a->Y + 2 * i * nc;
+        for (int64_t j = 0; j < 2 * nc; j++) dst[j] = 0.0;
+        for (int32_t q = a->rowptr[i]; q < a->rowptr[i + 1]; q++) {
+            const double v = a->vals[q];
+            const double* xr = a->X + 2 * (int64_t)a->colidx[q] * nc;
+            for (int64_t j = 0; j < nc; j++) {
+                double pr = xr[2 * j] * v, pi = xr[2 * j + 1] * v;
+                dst[2 * j] = dst[2 * j] + pr;
+                dst[2 * j + 1] = dst[2 * j + 1] + pi;
+            }
+        }
+    }
+}
+
+void orc_spmm_rz(int64_t rows, int64_t ncols, const int32_t* rowptr, const int32_t* colidx,
+                 const double* vals, const double* X, double* Y, int threads) {
+    orc_csr_args a = {ncols, rowptr, colidx, vals, X, Y};
+    orc_parallel_rows(rows, threads, orc_spmm_rz_rows, &a);
+}
+
+static void orc_zspmm_rows(void* p, int64_t r0, int64_t r1) {
+    orc_csr_args* a = (orc_csr_args*)p;
+    const int64_t nc = a->ncols;
+    for (int64_t i = r0; i < r1; i++) {
+        double* dst = a->Y + 2 * i * nc;
+        for (int64_t j = 0; j < 2 * nc; j++) dst[j] = 0.0;
+        for (int32_t q = a->rowptr[i]; q < a->rowptr[i + 1]; q++) {
+            const double vr = a->vals[2 * q], vi = a->vals[2 * q + 1];
+            const double* xr = a->X + 2 * (int64_t)a->colidx[q] * nc;
+            for (int64_t j = 0; j < nc; j++) {
+                const double x_r = xr[2 * j], x_i = xr[2 * j + 1];
+                double t1 = x_r * vr, t2 = x_i * vi, t3 = x_r * vi, t4 = x_i * vr;
+                double pr = t1 - t2, pi = t3 + t4;
+                dst[2 * j] = dst[2 * j] + pr;
+                dst[2 * j + 1] = dst[2 * j + 1] + pi;
+            }
+        }
+    }
+}
+
+void orc_zspmm(int64_t rows, int64_t ncols, const int32_t* rowptr, const int32_t* colidx,
+               const double* vals, const double* X, double* Y, int threads) {
+    orc_csr_args a = {ncols, rowptr, colidx, vals, X, Y};
+    orc_parallel_rows(rows, threads, orc_zspmm_rows, &a);
 }
 
 /* ------------------------------------------------------------------ */

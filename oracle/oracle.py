@@ -43,6 +43,10 @@ def lib():
                 "orc_dgemm_abt": [i64, i64, i64, p, p, p, i32],
                 "orc_dgemv_blocked": [i64, i64, p, p, p, i64],
                 "orc_zgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_rzgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_zrgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_spmm_rz": [i64, i64, p, p, p, p, p, i32],
+                "orc_zspmm": [i64, i64, p, p, p, p, p, i32],
                 "orc_spmv": [i64, p, p, p, p, p, i32],
                 "orc_spmm": [i64, i64, p, p, p, p, p, i32],
                 "orc_coo_to_csr": [i64, i64, p, p],
@@ -119,6 +123,30 @@ def zgemm(A, B, threads=1):
     return C
 
 
+def rzgemm(A, B, threads=1):
+    """Matrix.mult(CMatrix): real A (m x k) times complex B (k x n)."""
+    A = _f64(A)
+    B = np.ascontiguousarray(B, dtype=np.complex128)
+    m, k = A.shape
+    assert B.shape[0] == k
+    n = B.shape[1]
+    C = np.empty((m, n), np.complex128)
+    lib().orc_rzgemm(m, n, k, _p(A), _p(B), _p(C), threads)
+    return C
+
+
+def zrgemm(A, B, threads=1):
+    """CMatrix.mult(Matrix): complex A (m x k) times real B (k x n)."""
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    B = _f64(B)
+    m, k = A.shape
+    assert B.shape[0] == k
+    n = B.shape[1]
+    C = np.empty((m, n), np.complex128)
+    lib().orc_zrgemm(m, n, k, _p(A), _p(B), _p(C), threads)
+    return C
+
+
 def absgemm(A, B, threads=1):
     A, B = _f64(A), _f64(B)
     m, k = A.shape
@@ -165,6 +193,29 @@ def spmm(rowptr, colidx, vals, X, threads=1):
     nc = X.shape[1]
     Y = np.empty((rows, nc), np.float64)
     lib().orc_spmm(rows, nc, _p(rowptr), _p(colidx), _p(vals), _p(X), _p(Y), threads)
+    return Y
+
+
+def spmm_rz(rowptr, colidx, vals, X, threads=1):
+    """CsrMatrix.mult(CMatrix): real CSR times complex dense X (rows of S x ncols)."""
+    rowptr, colidx, vals = _i32(rowptr), _i32(colidx), _f64(vals)
+    X = np.ascontiguousarray(X, dtype=np.complex128)
+    rows = len(rowptr) - 1
+    nc = X.shape[1]
+    Y = np.empty((rows, nc), np.complex128)
+    lib().orc_spmm_rz(rows, nc, _p(rowptr), _p(colidx), _p(vals), _p(X), _p(Y), threads)
+    return Y
+
+
+def zspmm(rowptr, colidx, vals, X, threads=1):
+    """CsrCMatrix.mult(CMatrix): complex CSR (complex vals) times complex dense X."""
+    rowptr, colidx = _i32(rowptr), _i32(colidx)
+    vals = np.ascontiguousarray(vals, dtype=np.complex128)
+    X = np.ascontiguousarray(X, dtype=np.complex128)
+    rows = len(rowptr) - 1
+    nc = X.shape[1]
+    Y = np.empty((rows, nc), np.complex128)
+    lib().orc_zspmm(rows, nc, _p(rowptr), _p(colidx), _p(vals), _p(X), _p(Y), threads)
     return Y
 
 

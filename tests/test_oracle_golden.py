@@ -108,3 +108,35 @@ def test_truth_oracle_is_compensated(oracle):
     B = np.array([[1.0], [1.0], [1.0]])
     hi, lo, ab = oracle.truth_sampled(A, B, [0], [0])
     assert hi[0] + lo[0] == 1.0 and oracle.dgemm(A, B)[0, 0] == 0.0
+
+
+def test_real_times_complex_golden(oracle, golden):
+    # MatrixMultTests.java:66-86 (Matrix.mult(CMatrix)) and MatrixVectorTests.java:66-81
+    # (Matrix.mult(CVector)): RealFieldDenseMatMult's k-ascending order, bit-exact
+    c = [c for c in golden["matrix_mult"] if c["line"] == 85 and c["call"] == "assertEquals"][0]
+    v = c["vars"]
+    A, B, exp = np.array(v["aEntries"]), cplx(v["bEntries"]), cplx(v["expCEntries"])
+    assert np.array_equal(oracle.rzgemm(A, B), exp)
+    # complex x real is the transposed restatement: (B^T A^T)^T with B^T complex
+    assert np.array_equal(oracle.zrgemm(B.T.copy(), A.T.copy()).T, oracle.rzgemm(A, B))
+    c = [c for c in golden["matrix_vector"] if c["line"] == 81 and c["call"] == "assertEquals"][0]
+    v = c["vars"]
+    A, x, exp = np.array(v["aEntries"]), cplx(v["bEntries"]), cplx(v["expCEntries"])
+    assert np.array_equal(oracle.rzgemm(A, x[:, None]).ravel(), exp)
+
+
+def test_mixed_sparse_restatements_agree_with_dense(oracle):
+    # RealFieldDenseCsrMatMult.java:62-91 and DenseCsrSemiringMatMult.java:59-98 on a
+    # matrix with one nonzero per row equal the dense products exactly (one term per sum)
+    rng = np.random.default_rng(3)
+    rows, cols, nc = 7, 9, 5
+    ci = rng.integers(0, cols, size=rows).astype(np.int32)
+    rp = np.arange(rows + 1, dtype=np.int32)
+    vr = rng.standard_normal(rows)
+    vz = vr + 1j * rng.standard_normal(rows)
+    X = rng.standard_normal((cols, nc)) + 1j * rng.standard_normal((cols, nc))
+    Dr = np.zeros((rows, cols)); Dr[np.arange(rows), ci] = vr
+    Dz = np.zeros((rows, cols), np.complex128); Dz[np.arange(rows), ci] = vz
+    assert np.array_equal(oracle.spmm_rz(rp, ci, vr, X), oracle.rzgemm(Dr, X))
+    # one term per sum: x * v with Complex128.mult's rounding, equal to zgemm's (a * x) products
+    assert np.array_equal(oracle.zspmm(rp, ci, vz, X), oracle.zgemm(Dz, X))
