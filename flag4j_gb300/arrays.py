@@ -266,6 +266,12 @@ class CMatrix(_Dense):
         return (CVector._from_device(Shape(self.numRows), out, ctx) if vec
                 else CMatrix._from_device(Shape(self.numRows, n), out, ctx))
 
+    def multTranspose(self, b, mode=None, report=None):
+        """CMatrix.multTranspose (AbstractDenseSemiringMatrix.java:330-334 ->
+        DenseSemiringMatMultTranspose, k ascending): this * b^T, b read transposed in place."""
+        ensure_all_equal(self.numCols, b.numCols)
+        return _gemm(self, b, _lib.OP_N, _lib.OP_T, self.numRows, b.numRows, self.numCols, mode, report)
+
     def __eq__(self, other):
         return isinstance(other, CMatrix) and self.shape == other.shape and _nan_equal(self.data, other.data)
 

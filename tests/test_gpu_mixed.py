@@ -131,3 +131,16 @@ def test_mixed_shape_errors(f4j):
         S.mult(f4j.CVector(np.ones(5, np.complex128)))
     with pytest.raises(LinearAlgebraException):
         S.mult(f4j.CMatrix(np.ones((5, 2), np.complex128)))
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (45, 33, 70), (130, 64, 129)])
+def test_complex_mult_transpose_and_matvec_exact(f4j, oracle, m, n, k):
+    # CMatrix.multTranspose -> DenseSemiringMatMultTranspose.java:54-150 (k ascending, running sums)
+    # and CMatrix.mult(CVector): both bit-identical to the k-ascending complex restatement
+    rng = np.random.default_rng(m + n + k)
+    A, B = crand(rng, m, k), crand(rng, n, k)
+    got = f4j.CMatrix(A).multTranspose(f4j.CMatrix(B), mode="exact").toNumpy()
+    assert np.array_equal(got, oracle.zgemm(A, B.T.copy()))
+    x = crand(rng, k)
+    got = f4j.CMatrix(A).mult(f4j.CVector(x), mode="exact").data
+    assert np.array_equal(got, oracle.zgemm(A, x[:, None]).ravel())
