@@ -88,7 +88,13 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
         if (ctx->ev_init[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->prof_init)
         for (int i = 0; i < 1024; i++) cudaEventDestroy(ctx->prof_ev[i]);
-    for (int i = 0; i < 4; i++)
+    if (ctx->aux_stream) {
+        cudaStreamSynchronize(ctx->aux_stream);
+        cudaStreamDestroy(ctx->aux_stream);
+        cudaEventDestroy(ctx->ev_fork);
+        cudaEventDestroy(ctx->ev_join);
+    }
+    for (int i = 0; i < 8; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -201,7 +207,7 @@ int f4j_status_take(f4j_ctx* ctx, int idx, int* value) {
 }
 
 int f4j_workspace(f4j_ctx* ctx, int slot, size_t bytes, void** out) {
-    if (slot < 0 || slot >= 4) return f4j_fail(F4J_ERR_ARG, "workspace slot %d", slot);
+    if (slot < 0 || slot >= 8) return f4j_fail(F4J_ERR_ARG, "workspace slot %d", slot);
     if (bytes == 0) bytes = 256;
     if (bytes > ctx->ws_bytes[slot]) {
         F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -372,7 +378,9 @@ static int check_gemm_args(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_
 }
 
 int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
-                  int opA, const double* B, int opB, double* C, int mode, f4j_report* rep) {
+                  int opA, const double* B, int opB, double* C, int mode, f4j_report* rep,
+                  const int** gate_out) {
+    if (gate_out) *gate_out = nullptr;
     int64_t l0 = ctx->launches;
     if (rep) {
         *rep = f4j_report{};
@@ -401,6 +409,7 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
         // the reference.  Nothing here waits for the GPU.
         const int* gate = nullptr;
         rc = f4j_gemm_split(ctx, cplx, m, n, k, A, opA, B, opB, C, 0, rep, &gate);
+        if (gate_out) *gate_out = gate;
         used = F4J_MODE_SPLIT;
         if (rc == F4J_OK) rc = f4j_gemm_dmma(ctx, cplx, m, n, k, A, opA, B, opB, C, gate);
         if (rc == F4J_OK && rep && rep->slices == 0) used = F4J_MODE_PLAIN;
@@ -439,6 +448,67 @@ static int adjoint(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j
     const int opH = cplx ? F4J_OP_C : F4J_OP_T;
     f4j_report r1{}, r2{};
     int64_t l0 = ctx->launches;
+    if (dA && dB) {
+        // Both products at once: dA on the context stream, dB on a second stream
+        // with its own split workspace (slots 4-5).  Each product's persistent
+        // kernel leaves a partly empty last wave; on two streams the other
+        // product's CTAs fill those SMs.  No report is read until both are queued.
+        int rc = check_gemm_args(ctx, cplx, m, k, n, dC, F4J_OP_N, B, opH, dA, mode);
+        if (rc) return rc;
+        rc = check_gemm_args(ctx, cplx, k, n, m, A, opH, dC, F4J_OP_N, dB, mode);
+        if (rc) return rc;
+        if (!ctx->aux_stream) {
+            F4J_CUDA(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+            F4J_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+            F4J_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+        }
+        F4J_CUDA(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        F4J_CUDA(cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_fork, 0));
+        const int* g1 = nullptr;
+        const int* g2 = nullptr;
+        rc = f4j_gemm_impl(ctx, cplx, m, k, n, (const double*)dC->ptr, F4J_OP_N, (const double*)B->ptr, opH,
+                           (double*)dA->ptr, mode, nullptr, &g1);
+        const cudaStream_t main_stream = ctx->stream;
+        if (rc == F4J_OK) {
+            ctx->stream = ctx->aux_stream;
+            ctx->ws_base = 4;
+            rc = f4j_gemm_impl(ctx, cplx, k, n, m, (const double*)A->ptr, opH, (const double*)dC->ptr, F4J_OP_N,
+                               (double*)dB->ptr, mode, nullptr, &g2);
+            ctx->stream = main_stream;
+            ctx->ws_base = 0;
+        }
+        F4J_CUDA(cudaEventRecord(ctx->ev_join, ctx->aux_stream));
+        F4J_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+        if (rc) return rc;
+        if (rep) {
+            *rep = f4j_report{};
+            rep->flops = 2.0 * (cplx ? 8.0 : 2.0) * (double)m * (double)n * (double)k;
+            rep->mode_used = mode == F4J_MODE_AUTO && rep->flops / 2 <= (double)(1 << 24) ? F4J_MODE_EXACT : mode;
+            rep->launches = (int32_t)(ctx->launches - l0);
+            if (g1 || g2) {
+                // the plans' headers: s, nrounds, ubits, nonfinite, spread (the gate is nonfinite)
+                F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+                int h[2][5] = {};
+                if (g1) F4J_CUDA(cudaMemcpy(h[0], g1 - 3, sizeof h[0], cudaMemcpyDeviceToHost));
+                if (g2) F4J_CUDA(cudaMemcpy(h[1], g2 - 3, sizeof h[1], cudaMemcpyDeviceToHost));
+                int s = 0, nonfinite = 0;
+                float spread = 0.f;
+                for (int u = 0; u < 2; u++) {
+                    if (!(u ? g2 : g1)) continue;
+                    float sp;
+                    memcpy(&sp, &h[u][4], 4);
+                    s = h[u][0] > s ? h[u][0] : s;
+                    nonfinite |= h[u][3];
+                    spread = sp > spread ? sp : spread;
+                }
+                rep->slices = nonfinite ? 0 : s;
+                rep->frac_bits = s ? 4 + 5 * (s - 1) : 0;
+                rep->exp_spread = spread;
+                rep->mode_used = nonfinite ? F4J_MODE_PLAIN : F4J_MODE_SPLIT;
+            }
+        }
+        return F4J_OK;
+    }
     if (dA) {  // dA (m x k) = dC (m x n) * op(B) (n x k), B stored k x n
         int rc = check_gemm_args(ctx, cplx, m, k, n, dC, F4J_OP_N, B, opH, dA, mode);
         if (rc) return rc;

@@ -34,8 +34,11 @@ struct f4j_ctx {
     int sm_count;
     cudaStream_t stream;
     bool own_stream;
-    void* ws[4];       // grow-only workspaces (slot 0: bulk, 1: small/stats, 2-3: sparse)
-    size_t ws_bytes[4];
+    void* ws[8];       // grow-only workspaces (slot ws_base + 0: split bulk, ws_base + 1: split
+    size_t ws_bytes[8];  // small/stats; 2-3: sparse; 4-5: the second product of an adjoint)
+    int ws_base;       // first split workspace slot (0, or 4 while an adjoint's second product is queued)
+    cudaStream_t aux_stream;  // second stream of an adjoint (created on first use)
+    cudaEvent_t ev_fork, ev_join;
     int* d_status;     // device status words (bounded-wait timeouts, validation)
     cudaEvent_t ev[16];
     bool ev_init[16];
@@ -106,8 +109,12 @@ static inline int64_t f4j_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline bool f4j_aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 // Internal GEMM entry points shared by the dense front ends.
+// `gate_out` (may be null): for a split product, the device word of its plan
+// that flags a NaN/Inf stand-down; the plan's header (s, nrounds, ubits,
+// nonfinite, spread) ends at that word, so a caller can read it after a sync.
 int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
-                  int opA, const double* B, int opB, double* C, int mode, f4j_report* rep);
+                  int opA, const double* B, int opB, double* C, int mode, f4j_report* rep,
+                  const int** gate_out = nullptr);
 // `gate` (device int, may be null): the DMMA kernel computes only when *gate
 // is non-zero -- the split path's NaN/Inf fallback, decided on the device.
 int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,

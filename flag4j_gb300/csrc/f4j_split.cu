@@ -915,9 +915,9 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     // ---- bulk workspace (slot 0): S_MAX slice planes per operand
     const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
     void *ws1, *ws0;
-    int rc = f4j_workspace(ctx, 1, small_bytes, &ws1);
+    int rc = f4j_workspace(ctx, ctx->ws_base + 1, small_bytes, &ws1);
     if (rc) return rc;
-    rc = f4j_workspace(ctx, 0, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX), &ws0);
+    rc = f4j_workspace(ctx, ctx->ws_base, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX), &ws0);
     if (rc) return rc;
     char* w = (char*)ws1;
     unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
