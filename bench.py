@@ -349,6 +349,11 @@ def sparse_section(E, full, steps=20):
     Y = E.ctx.alloc(8 * rows * 32)
     t_spmv = E.timed(lambda: E.check(E.lib.f4j_spmv(E.ctx.handle, hS, x.handle, y.handle, None)), steps, 3)
     t_spmm = E.timed(lambda: E.check(E.lib.f4j_spmm(E.ctx.handle, hS, X.handle, 32, Y.handle, None)), steps, 3)
+    FMA = E.L.SPARSE_FMA
+    t_spmv_f = E.timed(lambda: E.check(E.lib.f4j_spmv_ex(E.ctx.handle, hS, x.handle, y.handle, FMA, None)),
+                       steps, 3)
+    t_spmm_f = E.timed(lambda: E.check(E.lib.f4j_spmm_ex(E.ctx.handle, hS, X.handle, 32, Y.handle, FMA, None)),
+                       steps, 3)
     b_spmv = 12.0 * nnz + 4.0 * (rows + 1) + 16.0 * rows
     b_spmm = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 32 * rows
     b_spmm_g = 12.0 * nnz + 8.0 * 32 * nnz + 8.0 * 32 * rows
@@ -357,7 +362,12 @@ def sparse_section(E, full, steps=20):
            "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm / 1e6,
            "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
            "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
-           "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True}
+           "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True,
+           "fma_mode": {"spmm_ms": t_spmm_f, "spmm_gbs_compulsory": b_spmm / t_spmm_f / 1e6,
+                        "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm_f / 1e6,
+                        "spmm_frac_gather_inclusive": b_spmm_g / t_spmm_f / 1e6 / hbm,
+                        "spmv_ms": t_spmv_f, "spmv_gbs": b_spmv / t_spmv_f / 1e6,
+                        "bound": "|y - y_ref| <= 2 k u |S||x| per row"}}
     del x, y, X, Y
 
     # ---- structure: stable COO sort of shuffled triplets, then COO -> CSR

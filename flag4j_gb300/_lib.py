@@ -21,6 +21,8 @@ F4J_ERR_UNSUPPORTED = -7
 
 OP_N, OP_T, OP_C = 0, 1, 2
 MODE_PLAIN, MODE_SPLIT, MODE_AUTO, MODE_EXACT = 0, 1, 2, 3
+SPARSE_EXACT, SPARSE_FMA = 0, 1
+SPARSE_MODES = {"exact": SPARSE_EXACT, "fma": SPARSE_FMA}
 MODES = {"plain": MODE_PLAIN, "split": MODE_SPLIT, "auto": MODE_AUTO, "exact": MODE_EXACT}
 
 
@@ -81,8 +83,10 @@ SIGNATURES = {
     "f4j_csr_transpose": (_i, [_v, _v, _pv]),
     "f4j_csr_transpose_perm": (_i, [_v, _v, _v]),
     "f4j_spmv": (_i, [_v, _v, _v, _v, _rep]),
+    "f4j_spmv_ex": (_i, [_v, _v, _v, _v, _i, _rep]),
     "f4j_spmm": (_i, [_v, _v, _v, _i64, _v, _rep]),
     "f4j_zspmm": (_i, [_v, _v, _v, _i64, _v, _rep]),
+    "f4j_spmm_ex": (_i, [_v, _v, _v, _i64, _v, _i, _rep]),
     "f4j_spmm_t": (_i, [_v, _v, _v, _i64, _v, _rep]),
     "f4j_sddmm": (_i, [_v, _v, _v, _v, _i64, _v, _rep]),
 }

@@ -408,22 +408,31 @@ class CsrMatrix:
             self._handle, self._bufs, self._ctx = h, (rp, ci, v), ctx
         return self._handle
 
-    def mult(self, b, report=None):
+    def mult(self, b, mode=None, report=None):
         """CsrMatrix.mult(Vector) (IllegalArgumentException on size mismatch) and
-        CsrMatrix.mult(Matrix) (LinearAlgebraException on shape mismatch)."""
+        CsrMatrix.mult(Matrix) (LinearAlgebraException on shape mismatch).
+
+        mode "exact" (the default) keeps the reference's rounding: each product and
+        each running sum rounded, in storage order.  mode "fma" fuses them
+        (fma(v, x, acc), same order), within |y - y_ref| <= 2 k u |S||x|; it applies
+        to the real right-hand sides."""
         rep = _lib.f4j_report()
+        md = _lib.SPARSE_EXACT if mode is None else _lib.SPARSE_MODES.get(mode, mode)
+        if md not in (_lib.SPARSE_EXACT, _lib.SPARSE_FMA):
+            raise IllegalArgumentException("unknown sparse mode %r" % (mode,))
         if isinstance(b, Vector):
             ensure_all_equal(self.numCols, b.size)
             ctx = self._ctx or b._ctx or default_context()
             y = ctx.alloc(max(8 * self.numRows, 8))
-            check(ctx.lib.f4j_spmv(ctx.handle, self.handle(ctx), b.device(ctx).handle, y.handle, ctypes.byref(rep)))
+            check(ctx.lib.f4j_spmv_ex(ctx.handle, self.handle(ctx), b.device(ctx).handle, y.handle, md,
+                                      ctypes.byref(rep)))
             out = Vector._from_device(Shape(self.numRows), y, ctx)
         elif isinstance(b, Matrix):
             ensure_mat_mult_shapes(self.shape, b.shape)
             ctx = self._ctx or b._ctx or default_context()
             y = ctx.alloc(max(8 * self.numRows * b.numCols, 8))
-            check(ctx.lib.f4j_spmm(ctx.handle, self.handle(ctx), b.device(ctx).handle, b.numCols, y.handle,
-                                   ctypes.byref(rep)))
+            check(ctx.lib.f4j_spmm_ex(ctx.handle, self.handle(ctx), b.device(ctx).handle, b.numCols, y.handle, md,
+                                      ctypes.byref(rep)))
             out = Matrix._from_device(Shape(self.numRows, b.numCols), y, ctx)
         elif isinstance(b, (CMatrix, CVector)):
             # CsrMatrix.mult(CMatrix) -> RealFieldDenseCsrMatMult.standard (RealFieldDenseCsrMatMult.java:62-91):
@@ -437,8 +446,8 @@ class CsrMatrix:
                 ensure_mat_mult_shapes(self.shape, b.shape)
             ctx = self._ctx or b._ctx or default_context()
             y = ctx.alloc(max(16 * self.numRows * nc, 16))
-            check(ctx.lib.f4j_spmm(ctx.handle, self.handle(ctx), b.device(ctx).handle, 2 * nc, y.handle,
-                                   ctypes.byref(rep)))
+            check(ctx.lib.f4j_spmm_ex(ctx.handle, self.handle(ctx), b.device(ctx).handle, 2 * nc, y.handle, md,
+                                      ctypes.byref(rep)))
             out = (CVector._from_device(Shape(self.numRows), y, ctx) if vec
                    else CMatrix._from_device(Shape(self.numRows, nc), y, ctx))
         else:

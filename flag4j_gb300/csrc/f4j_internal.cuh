@@ -107,6 +107,7 @@ f4j_encode_tiled_fn f4j_encode_fn();
 
 static inline int64_t f4j_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline bool f4j_aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+static inline bool f4j_aligned(const void* p, uintptr_t n) { return (reinterpret_cast<uintptr_t>(p) % n) == 0; }
 
 // Internal GEMM entry points shared by the dense front ends.
 // `gate_out` (may be null): for a split product, the device word of its plan

@@ -12,55 +12,87 @@
 #include <vector>
 
 #include "f4j_internal.cuh"
+#include "f4j_ptx.cuh"
 
 namespace {
 
 // ------------------------------------------------------------------ SpMV
-// Each warp owns 32 consecutive rows.  It walks their nonzeros in chunks of
-// SPMV_CHUNK: lanes gather x[col] and form the rounded products v * x[col]
-// cooperatively (coalesced index/value loads, SPMV_CHUNK/32 independent
-// gathers in flight per lane) into shared memory; then each lane adds its own
-// row's products in storage order.  Products and sums round exactly as
-// RealCsrDenseMatMult.standardVector does, so y is bit-identical.
-constexpr int SPMV_WARPS = 8, SPMV_CHUNK = 256;
+// Each warp owns 32 consecutive rows, one per lane, and walks their nonzeros
+// in chunks of up to CAP (normally the whole span at once):
+//   1. lanes copy the chunk's column indices and values to shared memory with
+//      asynchronous copies (coalesced, all in flight together);
+//   2. each lane gathers x[col] for its CAP/32 entries into registers, all
+//      gathers in flight together, and forms the rounded products v * x[col]
+//      in place (dense FP64 instructions);
+//   3. each lane adds its row's products in storage order.
+// Products and sums round exactly as RealCsrDenseMatMult.standardVector does,
+// so y is bit-identical.  With uniformly scattered columns the random 8-byte
+// gathers of x (one L2 sector each) bound the kernel; GB300's FP64 pipe
+// (2 lane-operations per clock per SM) comes next.
+// FUSED (the opt-in FMA mode) keeps values and gathered x and accumulates
+// fma(v, x, acc) in storage order, one FP64 instruction per nonzero instead
+// of two, within the reference's componentwise bound.
+constexpr int SPMV_WARPS = 8;
+template <bool FUSED>
+struct SpmvShape {
+    static constexpr int CAP = FUSED ? 576 : 640;  // entries per warp chunk, a multiple of 32
+    // shared memory per warp: values / products, column indices, gathered x (FUSED)
+    static constexpr size_t WARP_BYTES = (size_t)CAP * (FUSED ? 20 : 12);
+    static constexpr size_t SMEM = SPMV_WARPS * WARP_BYTES;
+};
 
+template <bool FUSED>
 __global__ void __launch_bounds__(SPMV_WARPS * 32)
     k_spmv(int64_t rows, const int* __restrict__ rowptr, const int* __restrict__ colidx,
            const double* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
-    __shared__ double sprod[SPMV_WARPS][SPMV_CHUNK];
+    constexpr int CAP = SpmvShape<FUSED>::CAP, PER = CAP / 32;
+    extern __shared__ __align__(16) unsigned char spmv_smem[];
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    double* sv = reinterpret_cast<double*>(spmv_smem + warp * SpmvShape<FUSED>::WARP_BYTES);
+    int* si = reinterpret_cast<int*>(sv + CAP);
+    double* sx = reinterpret_cast<double*>(si + CAP);  // FUSED only
     const int64_t wrow0 = ((int64_t)blockIdx.x * SPMV_WARPS + warp) * 32;
     if (wrow0 >= rows) return;
-    const int64_t row = wrow0 + lane;
     const int64_t wrow1 = wrow0 + 32 < rows ? wrow0 + 32 : rows;
     const int p0 = __ldg(&rowptr[wrow0]), p1 = __ldg(&rowptr[wrow1]);
-    int q = 0, qend = 0;
+    const int64_t row = wrow0 + lane;
+    int q = p1, qend = p1;
     if (row < rows) {
         q = __ldg(&rowptr[row]);
         qend = __ldg(&rowptr[row + 1]);
     }
     double acc = 0.0;
-    for (int c0 = p0; c0 < p1; c0 += SPMV_CHUNK) {
-        const int cn = (p1 - c0) < SPMV_CHUNK ? (p1 - c0) : SPMV_CHUNK;
-        if (cn == SPMV_CHUNK) {
-            int c[SPMV_CHUNK / 32];
-            double v[SPMV_CHUNK / 32], xv[SPMV_CHUNK / 32];
+    for (int c0 = p0; c0 < p1;) {
+        const int cn = (p1 - c0) < CAP ? (p1 - c0) : CAP;
+        for (int e = lane; e < cn; e += 32) {
+            cp_async4(&si[e], &colidx[c0 + e]);
+            cp_async8(&sv[e], &vals[c0 + e]);
+        }
+        cp_async_wait_all();
+        __syncwarp();
+        double xv[PER];
 #pragma unroll
-            for (int u = 0; u < SPMV_CHUNK / 32; u++) {
-                c[u] = __ldg(&colidx[c0 + lane + 32 * u]);
-                v[u] = __ldg(&vals[c0 + lane + 32 * u]);
+        for (int u = 0; u < PER; u++) {
+            const int e = lane + 32 * u;
+            xv[u] = e < cn ? __ldg(&x[si[e]]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int e = lane + 32 * u;
+            if (e < cn) {
+                if (FUSED) sx[e] = xv[u];
+                else sv[e] = __dmul_rn(sv[e], xv[u]);
             }
-#pragma unroll
-            for (int u = 0; u < SPMV_CHUNK / 32; u++) xv[u] = __ldg(&x[c[u]]);
-#pragma unroll
-            for (int u = 0; u < SPMV_CHUNK / 32; u++) sprod[warp][lane + 32 * u] = __dmul_rn(v[u], xv[u]);
-        } else {
-            for (int e = lane; e < cn; e += 32) sprod[warp][e] = __dmul_rn(__ldg(&vals[c0 + e]), __ldg(&x[__ldg(&colidx[c0 + e])]));
         }
         __syncwarp();
-        const int stop = qend < c0 + cn ? qend : c0 + cn;
-        for (; q < stop; q++) acc = __dadd_rn(acc, sprod[warp][q - c0]);
+        const int cend = c0 + cn;
+        const int stop = qend < cend ? qend : cend;
+        if (FUSED)
+            for (; q < stop; q++) acc = __fma_rn(sv[q - c0], sx[q - c0], acc);
+        else
+            for (; q < stop; q++) acc = __dadd_rn(acc, sv[q - c0]);
         __syncwarp();
+        c0 = cend;
     }
     if (row < rows) y[row] = acc;
 }
@@ -70,8 +102,14 @@ __global__ void __launch_bounds__(SPMV_WARPS * 32)
 // (128-bit loads of X rows) and sums over the row's nonzeros in storage order.
 // For S^T products the same kernel reads values through the transpose
 // permutation and row indices from the cached S^T structure.
-template <bool VEC2, bool PERM>
-__global__ void __launch_bounds__(256)
+// FUSED (the opt-in FMA mode): one fma(v, x, acc) per nonzero and column, in
+// storage order; within the reference's componentwise bound.  Its FP64 work
+// is half the exact mode's, so the X gathers' latency decides its speed: it
+// runs 8 blocks per SM (32 registers) to keep more of them in flight; the
+// exact mode runs 6 (40 registers), its best balance of loads in flight per
+// warp against warps.
+template <bool VEC2, bool PERM, bool FUSED = false>
+__global__ void __launch_bounds__(256, FUSED ? 8 : 6)
     k_spmm(int64_t rows, int64_t ncols, int G, const int* __restrict__ rowptr, const int* __restrict__ colidx,
            const double* __restrict__ vals, const int* __restrict__ perm, const double* __restrict__ X,
            double* __restrict__ Y) {
@@ -99,15 +137,20 @@ __global__ void __launch_bounds__(256)
                 for (int u = 0; u < UN; u++) xv[u] = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c[u] * ncols + cbase));
 #pragma unroll
                 for (int u = 0; u < UN; u++) {
-                    a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u].x));
-                    a1 = __dadd_rn(a1, __dmul_rn(v[u], xv[u].y));
+                    if (FUSED) {
+                        a0 = __fma_rn(v[u], xv[u].x, a0);
+                        a1 = __fma_rn(v[u], xv[u].y, a1);
+                    } else {
+                        a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u].x));
+                        a1 = __dadd_rn(a1, __dmul_rn(v[u], xv[u].y));
+                    }
                 }
             } else {
                 double xv[UN];
 #pragma unroll
                 for (int u = 0; u < UN; u++) xv[u] = __ldg(X + (int64_t)c[u] * ncols + cbase);
 #pragma unroll
-                for (int u = 0; u < UN; u++) a0 = __dadd_rn(a0, __dmul_rn(v[u], xv[u]));
+                for (int u = 0; u < UN; u++) a0 = FUSED ? __fma_rn(v[u], xv[u], a0) : __dadd_rn(a0, __dmul_rn(v[u], xv[u]));
             }
         }
         for (; q < q1; q++) {
@@ -115,10 +158,11 @@ __global__ void __launch_bounds__(256)
             const double v = PERM ? __ldg(&vals[__ldg(&perm[q])]) : __ldg(&vals[q]);
             if (VEC2) {
                 const double2 xv = __ldg(reinterpret_cast<const double2*>(X + (int64_t)c * ncols + cbase));
-                a0 = __dadd_rn(a0, __dmul_rn(v, xv.x));
-                a1 = __dadd_rn(a1, __dmul_rn(v, xv.y));
+                a0 = FUSED ? __fma_rn(v, xv.x, a0) : __dadd_rn(a0, __dmul_rn(v, xv.x));
+                a1 = FUSED ? __fma_rn(v, xv.y, a1) : __dadd_rn(a1, __dmul_rn(v, xv.y));
             } else {
-                a0 = __dadd_rn(a0, __dmul_rn(v, __ldg(X + (int64_t)c * ncols + cbase)));
+                const double xe = __ldg(X + (int64_t)c * ncols + cbase);
+                a0 = FUSED ? __fma_rn(v, xe, a0) : __dadd_rn(a0, __dmul_rn(v, xe));
             }
         }
         if (VEC2) *reinterpret_cast<double2*>(Y + row * ncols + cbase) = make_double2(a0, a1);
@@ -535,16 +579,23 @@ fail:
 }
 
 static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp, const int* ci, const double* v,
-                       const int* perm, const double* X, double* Y) {
+                       const int* perm, const double* X, double* Y, bool fused = false) {
     if (rows == 0 || ncols == 0) return F4J_OK;
-    const bool vec2 = (ncols % 2 == 0) && f4j_aligned16(X) && f4j_aligned16(Y);
+    // one row per warp from 17 columns on (the FP64 instructions of a warp then
+    // never wait on a second row of another length); 128-bit X loads only
+    // where a warp of 2-column lanes is still needed for the width
+    const bool vec2 = ncols > 32 && (ncols % 2 == 0) && f4j_aligned16(X) && f4j_aligned16(Y);
     const int64_t per_lane = vec2 ? 2 : 1;
     int G = 1;
     while (G < 32 && G * per_lane < ncols) G *= 2;
     const int64_t threads = rows * G;
     const unsigned blocks = (unsigned)f4j_cdiv(threads, 256);
     f4j_prof_begin(ctx);
-    if (vec2) {
+    if (fused) {
+        // the FMA mode (products with no reference order to keep): no transpose variant
+        if (vec2) k_spmm<true, false, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+        else k_spmm<false, false, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
+    } else if (vec2) {
         if (perm) k_spmm<true, true><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
         else k_spmm<true, false><<<blocks, 256, 0, ctx->stream>>>(rows, ncols, G, rp, ci, v, perm, X, Y);
     } else {
@@ -575,6 +626,8 @@ extern "C" int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nn
         return f4j_fail(F4J_ERR_CSR, "Expecting rowPointers to have length (numRows + 1)=%lld", (long long)(rows + 1));
     if (colidx->bytes < (size_t)nnz * 4 || vals->bytes < (size_t)nnz * 8)
         return f4j_fail(F4J_ERR_CSR, "column index / value buffers shorter than nnz=%lld", (long long)nnz);
+    if (!f4j_aligned(rowptr->ptr, 4) || !f4j_aligned(colidx->ptr, 4) || !f4j_aligned(vals->ptr, 8))
+        return f4j_fail(F4J_ERR_ARG, "CSR buffers must be aligned to their element size");
     F4J_CUDA(cudaSetDevice(ctx->device));
     if (validate) {
         void* ws;
@@ -797,21 +850,32 @@ extern "C" int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out)
     return F4J_OK;
 }
 
-extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* rep) {
+extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mode, f4j_report* rep) {
     F4J_CHECK_CTX(ctx);
+    if (mode != F4J_SPARSE_EXACT && mode != F4J_SPARSE_FMA) return f4j_fail(F4J_ERR_ARG, "unknown sparse mode %d", mode);
     if (!S || !x || !y) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (x->bytes < (size_t)S->cols * 8)
         return f4j_fail(F4J_ERR_ARG, "Expecting values to be equal but got: [%lld, %lld]", (long long)S->cols,
                         (long long)(x->bytes / 8));
     if (y->bytes < (size_t)S->rows * 8) return f4j_fail(F4J_ERR_ARG, "y buffer too small");
+    if (!f4j_aligned(x->ptr, 8) || !f4j_aligned(y->ptr, 8)) return f4j_fail(F4J_ERR_ARG, "x and y must be 8-byte aligned");
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     if (S->rows) {
         const unsigned blocks = (unsigned)f4j_cdiv(S->rows, SPMV_WARPS * 32);
+        const bool fused = mode == F4J_SPARSE_FMA;
+        const size_t smem = fused ? SpmvShape<true>::SMEM : SpmvShape<false>::SMEM;
+        F4J_CUDA(cudaFuncSetAttribute(fused ? k_spmv<true> : k_spmv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
         f4j_prof_begin(ctx);
-        k_spmv<<<blocks, SPMV_WARPS * 32, 0, ctx->stream>>>(S->rows, (const int*)S->rowptr->ptr,
-                                                            (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
-                                                            (const double*)x->ptr, (double*)y->ptr);
+        if (fused)
+            k_spmv<true><<<blocks, SPMV_WARPS * 32, smem, ctx->stream>>>(
+                S->rows, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
+                (const double*)x->ptr, (double*)y->ptr);
+        else
+            k_spmv<false><<<blocks, SPMV_WARPS * 32, smem, ctx->stream>>>(
+                S->rows, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
+                (const double*)x->ptr, (double*)y->ptr);
         f4j_prof_end(ctx);
         F4J_LAUNCHED(ctx);
     }
@@ -824,16 +888,24 @@ extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_repor
     return F4J_OK;
 }
 
-extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* rep) {
+    return f4j_spmv_ex(ctx, S, x, y, F4J_SPARSE_EXACT, rep);
+}
+
+extern "C" int f4j_spmm_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, int mode,
+                           f4j_report* rep) {
     F4J_CHECK_CTX(ctx);
+    if (mode != F4J_SPARSE_EXACT && mode != F4J_SPARSE_FMA) return f4j_fail(F4J_ERR_ARG, "unknown sparse mode %d", mode);
     if (!S || !X || !Y) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
     if (X->bytes < (size_t)S->cols * ncols * 8) return f4j_fail(F4J_ERR_ARG, "X buffer too small");
     if (Y->bytes < (size_t)S->rows * ncols * 8) return f4j_fail(F4J_ERR_ARG, "Y buffer too small");
+    if (!f4j_aligned(X->ptr, 8) || !f4j_aligned(Y->ptr, 8)) return f4j_fail(F4J_ERR_ARG, "X and Y must be 8-byte aligned");
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     int rc = launch_spmm(ctx, S->rows, ncols, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr,
-                         (const double*)S->vals->ptr, nullptr, (const double*)X->ptr, (double*)Y->ptr);
+                         (const double*)S->vals->ptr, nullptr, (const double*)X->ptr, (double*)Y->ptr,
+                         mode == F4J_SPARSE_FMA);
     if (rc) return rc;
     if (rep) {
         *rep = f4j_report{};
@@ -842,6 +914,10 @@ extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_b
         rep->launches = (int32_t)(ctx->launches - l0);
     }
     return F4J_OK;
+}
+
+extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+    return f4j_spmm_ex(ctx, S, X, ncols, Y, F4J_SPARSE_EXACT, rep);
 }
 
 extern "C" int f4j_zspmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {

@@ -214,6 +214,15 @@ int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* report);
  * -> RealCsrDenseMatMult.standard (CsrMatrix.java:1498-1499,
  * RealCsrDenseMatMult.java:55-82).  Bit-identical. */
 int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* report);
+/* Rounding modes of the real CSR products: F4J_SPARSE_EXACT is the reference's
+ * order (each product and each sum rounded; f4j_spmv / f4j_spmm); F4J_SPARSE_FMA
+ * accumulates fma(v, x, acc) in the same storage order, one FP64 instruction
+ * per term instead of two, within the componentwise bound
+ * |y - y_ref| <= 2 k u |S||x| (k = the row length).  GB300's FP64 pipe bounds
+ * the exact products; FMA halves that work.  No counterpart in Flag4j. */
+enum { F4J_SPARSE_EXACT = 0, F4J_SPARSE_FMA = 1 };
+int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mode, f4j_report* report);
+int f4j_spmm_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, int mode, f4j_report* report);
 /* Y(rows x ncols) = S X for a complex CSR S and complex dense X, Y
  * (interleaved re/im): S is a CSR handle whose value buffer holds nnz complex
  * values (16 bytes each, as CsrCMatrix.data).  Bit-identical to

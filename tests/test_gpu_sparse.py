@@ -72,6 +72,27 @@ def test_empty_rows_and_empty_matrix(f4j, oracle):
     assert not Z.mult(f4j.Vector(np.ones(4))).data.any()
 
 
+def test_rows_longer_than_a_staging_chunk(f4j, oracle):
+    """Rows of 5000 and 1600 nonzeros (longer than the SpMV kernel's shared-memory
+    chunk) between empty and short rows; SpMV and SpMM stay bit-identical."""
+    rng = np.random.default_rng(17)
+    rows, cols = 200, 6000
+    lens = rng.integers(0, 40, rows)
+    lens[[0, 63, 64, 127, 199]] = [5000, 1600, 0, 3100, 2000]
+    lens[100:110] = 0
+    rp = np.zeros(rows + 1, np.int32)
+    np.cumsum(lens, out=rp[1:])
+    ci = np.concatenate([np.sort(rng.choice(cols, n, replace=False)) for n in lens]).astype(np.int32)
+    v = rng.standard_normal(len(ci))
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    X = rng.standard_normal((cols, 3))
+    for j in range(3):
+        assert np.array_equal(S.mult(f4j.Vector(X[:, j])).data, oracle.spmv(rp, ci, v, X[:, j]))
+        y = S.mult(f4j.Vector(X[:, j]), mode="fma").data
+        assert np.all(np.abs(y - oracle.spmv(rp, ci, v, X[:, j])) <= fma_bound(oracle, rp, ci, v, X[:, j:j + 1])[:, 0])
+    assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X))
+
+
 def test_full_config_csr_products(f4j, oracle):
     """2^20 x 2^20, Poisson(16) row lengths: SpMV and SpMM (32 columns) bit-identical."""
     from flag4j_gb300 import synth
@@ -82,6 +103,65 @@ def test_full_config_csr_products(f4j, oracle):
     assert np.array_equal(S.mult(f4j.Vector(x)).data, oracle.spmv(rp, ci, v, x, threads=8))
     X = synth.normal(n, 32, 6)
     assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X, threads=8))
+
+
+def fma_bound(oracle, rp, ci, v, X, threads=1):
+    """2 k u (|S||X|) per row, k = the row's length (the fused and the reference
+    rounding each stay within k u |S||X| of the exact product)."""
+    k = np.diff(rp).astype(np.float64)[:, None]
+    return 2 * k * U * oracle.spmm(rp, ci, np.abs(v), np.abs(X), threads=threads)
+
+
+@pytest.mark.parametrize("rows,cols,lam,hi", [(1, 1, 1.0, 1), (5000, 4000, 16.0, 256), (2000, 3000, 200.0, 256)])
+@pytest.mark.parametrize("ncols", [1, 3, 32, 64, 100])
+def test_spmm_spmv_fma_mode_within_bound(f4j, oracle, rows, cols, lam, hi, ncols):
+    from flag4j_gb300 import synth
+    rp, ci, v = synth.csr_poisson(rows, cols, lam=lam, hi=hi, seed=7 * rows + ncols)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    X = synth.normal(cols, ncols, 11)
+    ref = oracle.spmm(rp, ci, v, X)
+    bound = fma_bound(oracle, rp, ci, v, X)
+    got = S.mult(f4j.Matrix(X), mode="fma").toNumpy()
+    assert np.all(np.abs(got - ref) <= bound)
+    # the default stays the reference's rounding
+    assert np.array_equal(S.mult(f4j.Matrix(X)).toNumpy(), ref)
+    if ncols == 1:
+        y = S.mult(f4j.Vector(X[:, 0]), mode="fma").data
+        assert np.all(np.abs(y - ref[:, 0]) <= bound[:, 0])
+
+
+def test_fma_mode_full_config_and_complex_rhs(f4j, oracle):
+    """2^20 x 2^20, Poisson(16): SpMV and SpMM (32 columns) in the FMA mode within
+    the bound; CsrMatrix.mult(CMatrix) in the FMA mode within it per part."""
+    from flag4j_gb300 import synth
+    n = 1 << 20
+    rp, ci, v = synth.csr_poisson(n, n, seed=2024)
+    S = f4j.CsrMatrix((n, n), v, rp, ci)
+    x = synth.normal(n, 1, 5)
+    y = S.mult(f4j.Vector(x.ravel()), mode="fma").data
+    assert np.all(np.abs(y - oracle.spmv(rp, ci, v, x.ravel(), threads=8)) <= fma_bound(oracle, rp, ci, v, x, 8)[:, 0])
+    X = synth.normal(n, 32, 6)
+    got = S.mult(f4j.Matrix(X), mode="fma").toNumpy()
+    assert np.all(np.abs(got - oracle.spmm(rp, ci, v, X, threads=8)) <= fma_bound(oracle, rp, ci, v, X, 8))
+    rng = np.random.default_rng(3)
+    m = 4096
+    rp, ci, v = synth.csr_poisson(m, m, seed=31)
+    Xz = rng.standard_normal((m, 5)) + 1j * rng.standard_normal((m, 5))
+    got = f4j.CsrMatrix((m, m), v, rp, ci).mult(f4j.CMatrix(Xz), mode="fma").toNumpy()
+    ref = oracle.spmm_rz(rp, ci, v, Xz)
+    assert np.all(np.abs(got.real - ref.real) <= fma_bound(oracle, rp, ci, v, Xz.real))
+    assert np.all(np.abs(got.imag - ref.imag) <= fma_bound(oracle, rp, ci, v, Xz.imag))
+
+
+def test_sparse_mode_rejected(f4j):
+    S = f4j.CsrMatrix((2, 2), np.ones(2), np.array([0, 1, 2]), np.array([0, 1]))
+    with pytest.raises(f4j.IllegalArgumentException):
+        S.mult(f4j.Vector(np.ones(2)), mode="fast")
+    ctx = f4j.default_context()
+    X = ctx.from_numpy(np.ones((2, 3)))
+    Y = ctx.alloc(2 * 3 * 8)
+    assert ctx.lib.f4j_spmm_ex(ctx.handle, S.handle(ctx), X.handle, 3, Y.handle, 7, None) != 0
+    assert ctx.lib.f4j_spmv_ex(ctx.handle, S.handle(ctx), X.handle, Y.handle, -1, None) != 0
 
 
 # ------------------------------------------------------------------ structure
