@@ -337,6 +337,14 @@ __global__ void k_iota(int64_t n, int* __restrict__ v) {
         v[i] = (int)i;
 }
 
+// keys[i] = src[perm ? perm[i] : i], with the sign bit flipped when `flip`
+// (so unsigned order is signed int order)
+__global__ void k_flip_copy(int64_t n, const int* __restrict__ perm, const int* __restrict__ src, bool flip,
+                            unsigned* __restrict__ keys) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = (unsigned)src[perm ? perm[i] : i] ^ (flip ? 0x80000000u : 0u);
+}
+
 template <typename T>
 __global__ void k_gather(int64_t n, const int* __restrict__ perm, const T* __restrict__ src, T* __restrict__ dst) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -455,6 +463,122 @@ __global__ void __launch_bounds__(RS_T) k_radix_scatter(int64_t n, const unsigne
             keys_out[pos] = key;
             vals_out[pos] = val;
         }
+        __syncthreads();
+    }
+}
+
+// ---------------- COO sort by (row, col), stable
+// Sorting by (row, col) stably is sorting by the unique key (row, col, input
+// index).  The triplets are bucketed by row through per-row atomic cursors
+// (which leaves each row's order arbitrary), then each row's segment is
+// sorted by (col, input index), packed as one 64-bit key, in registers (rows
+// of up to 32 entries, a warp per row) or in shared memory (bitonic, up to
+// SEG_CAP entries, a block per row).  The values follow through the input
+// index.  Longer rows, and negative indices, take the radix path.
+constexpr int SEG_CAP = 4096;
+
+__global__ void k_coo_minmax(int64_t n, const int* __restrict__ r, const int* __restrict__ c, int* __restrict__ mm) {
+    int lo = INT32_MAX, hr = INT32_MIN, hc = INT32_MIN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int a = __ldg(&r[i]), b = __ldg(&c[i]);
+        lo = min(lo, min(a, b));
+        hr = max(hr, a);
+        hc = max(hc, b);
+    }
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hr = max(hr, __shfl_xor_sync(0xffffffffu, hr, o));
+        hc = max(hc, __shfl_xor_sync(0xffffffffu, hc, o));
+    }
+    if (threadIdx.x % 32 == 0) {
+        atomicMin(&mm[0], lo);
+        atomicMax(&mm[1], hr);
+        atomicMax(&mm[2], hc);
+    }
+}
+
+__global__ void k_count_rows(int64_t n, const int* __restrict__ r, int* __restrict__ cnt) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[__ldg(&r[i])], 1);
+}
+
+__global__ void k_max_int(int64_t n, const int* __restrict__ v, int* __restrict__ out) {
+    int m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, __ldg(&v[i]));
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x % 32 == 0) atomicMax(out, m);
+}
+
+// rp: exclusive row offsets (rows + 1); cur: per-row cursors, zeroed
+__global__ void k_coo_bucket(int64_t n, const int* __restrict__ r, const int* __restrict__ c,
+                             const int* __restrict__ rp, int* __restrict__ cur, unsigned long long* __restrict__ key) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int row = __ldg(&r[i]);
+        const int pos = __ldg(&rp[row]) + atomicAdd(&cur[row], 1);
+        key[pos] = ((unsigned long long)(unsigned)__ldg(&c[i]) << 32) | (unsigned)i;
+    }
+}
+
+// writes one sorted entry: row, column, and the value of its input index
+__device__ __forceinline__ void coo_emit(int64_t pos, int row, unsigned long long k, int* __restrict__ ro,
+                                         int* __restrict__ co, const double* __restrict__ vin,
+                                         double* __restrict__ vo) {
+    ro[pos] = row;
+    co[pos] = (int)(k >> 32);
+    if (vo) vo[pos] = __ldg(&vin[(unsigned)k]);
+}
+
+// a warp per row; rows of up to 32 entries are ranked in registers (keys are
+// unique), longer ones are listed for k_coo_seg_block
+__global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const unsigned long long* __restrict__ key,
+                               int* __restrict__ ro, int* __restrict__ co, const double* __restrict__ vin,
+                               double* __restrict__ vo, int* __restrict__ longlist, int* __restrict__ nlong) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= rows) return;
+    const int q0 = __ldg(&rp[row]), len = __ldg(&rp[row + 1]) - q0;
+    if (len > 32) {
+        if (lane == 0) longlist[atomicAdd(nlong, 1)] = (int)row;
+        return;
+    }
+    const unsigned long long k = lane < len ? key[q0 + lane] : ~0ull;
+    int rank = 0;
+    for (int j = 0; j < len; j++) rank += __shfl_sync(0xffffffffu, k, j) < k;
+    if (lane < len) coo_emit(q0 + rank, (int)row, k, ro, co, vin, vo);
+}
+
+// a block per listed row (33 .. SEG_CAP entries): bitonic sort in shared memory
+__global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ longlist, const int* __restrict__ nlong,
+                                                       const int* __restrict__ rp,
+                                                       const unsigned long long* __restrict__ key,
+                                                       int* __restrict__ ro, int* __restrict__ co,
+                                                       const double* __restrict__ vin, double* __restrict__ vo) {
+    __shared__ unsigned long long sk[SEG_CAP];
+    const int nl = *nlong;
+    for (int b = blockIdx.x; b < nl; b += gridDim.x) {
+        const int row = longlist[b];
+        const int q0 = rp[row], len = rp[row + 1] - q0;
+        int P = 64;
+        while (P < len) P <<= 1;
+        for (int i = threadIdx.x; i < P; i += blockDim.x) sk[i] = i < len ? key[q0 + i] : ~0ull;
+        __syncthreads();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+                    const int lo = 2 * t - (t & (stride - 1));
+                    const int hi = lo + stride;
+                    const bool up = (lo & size) == 0;
+                    const unsigned long long a = sk[lo], c = sk[hi];
+                    if ((a > c) == up) {
+                        sk[lo] = c;
+                        sk[hi] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < len; i += blockDim.x) coo_emit(q0 + i, row, sk[i], ro, co, vin, vo);
         __syncthreads();
     }
 }
@@ -773,14 +897,11 @@ extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_
     return F4J_OK;
 }
 
-extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
-    F4J_CHECK_CTX(ctx);
-    if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
-    if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
-    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || (vals && vals->bytes < (size_t)nnz * 8))
-        return f4j_fail(F4J_ERR_ARG, "COO buffers shorter than nnz");
-    if (nnz <= 1) return F4J_OK;
-    F4J_CUDA(cudaSetDevice(ctx->device));
+// Radix path of f4j_coo_sort: stable LSD by column, then by row, over the
+// keys' significant bits (all 32 with a sign flip when an index is negative,
+// so negative indices order first as the reference's int comparison has them).
+static int coo_sort_radix(f4j_ctx* ctx, int64_t nnz, int* rowidx, int* colidx, double* vals, int rbits, int cbits,
+                          bool flip) {
     unsigned* keys = nullptr;
     int *perm = nullptr, *tmp = nullptr;
     double* vtmp = nullptr;
@@ -789,25 +910,26 @@ extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf c
     if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 4, (void**)&tmp);
     if (!rc && vals) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&vtmp);
     if (!rc) {
-        // LSD: stable by column, then stable by row == stable lexicographic (row, col).
         k_iota<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm);
-        cudaMemcpyAsync(keys, colidx->ptr, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
-        rc = radix_sort_pairs(ctx, keys, perm, nnz, 31);
+        k_flip_copy<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, nullptr, colidx, flip, keys);
+        ctx->launches += 2;
+        rc = radix_sort_pairs(ctx, keys, perm, nnz, cbits);
     }
     if (!rc) {
-        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)rowidx->ptr, (int*)keys);
-        rc = radix_sort_pairs(ctx, keys, perm, nnz, 31);
+        k_flip_copy<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, rowidx, flip, keys);
+        ctx->launches++;
+        rc = radix_sort_pairs(ctx, keys, perm, nnz, rbits);
     }
     if (!rc) {
-        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)rowidx->ptr, tmp);
-        cudaMemcpyAsync(rowidx->ptr, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
-        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const int*)colidx->ptr, tmp);
-        cudaMemcpyAsync(colidx->ptr, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, rowidx, tmp);
+        cudaMemcpyAsync(rowidx, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        k_gather<int><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, colidx, tmp);
+        cudaMemcpyAsync(colidx, tmp, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
         if (vals) {
-            k_gather<double><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, (const double*)vals->ptr, vtmp);
-            cudaMemcpyAsync(vals->ptr, vtmp, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+            k_gather<double><<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, perm, vals, vtmp);
+            cudaMemcpyAsync(vals, vtmp, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream);
         }
-        ctx->launches += vals ? 5 : 4;
+        ctx->launches += vals ? 3 : 2;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
     }
@@ -815,6 +937,96 @@ extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf c
     f4j_dev_free(ctx, perm);
     f4j_dev_free(ctx, tmp);
     f4j_dev_free(ctx, vtmp);
+    return rc;
+}
+
+extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
+    F4J_CHECK_CTX(ctx);
+    if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
+    if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
+    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || (vals && vals->bytes < (size_t)nnz * 8))
+        return f4j_fail(F4J_ERR_ARG, "COO buffers shorter than nnz");
+    if (nnz <= 1) return F4J_OK;
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int* r = (int*)rowidx->ptr;
+    int* c = (int*)colidx->ptr;
+    double* v = vals ? (double*)vals->ptr : nullptr;
+    const unsigned red_grid = (unsigned)std::min<int64_t>(grid1(nnz), (int64_t)ctx->sm_count * 8);
+
+    // index range: mm = {min of rows and columns, max row, max column, longest row}
+    int* mm = nullptr;
+    int rc = f4j_dev_alloc(ctx, 16, (void**)&mm);
+    if (rc) return rc;
+    const int mm0[4] = {INT32_MAX, INT32_MIN, INT32_MIN, 0};
+    F4J_CUDA(cudaMemcpyAsync(mm, mm0, 16, cudaMemcpyHostToDevice, ctx->stream));
+    k_coo_minmax<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, c, mm);
+    ctx->launches++;
+    int hm[4];
+    F4J_CUDA(cudaMemcpyAsync(hm, mm, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hm[0] < 0) {
+        f4j_dev_free(ctx, mm);
+        return coo_sort_radix(ctx, nnz, r, c, v, 32, 32, true);
+    }
+    const int64_t rows = (int64_t)hm[1] + 1;
+    if (rows > 4 * nnz + 4096) {  // row offsets would outweigh the triplets
+        f4j_dev_free(ctx, mm);
+        int rb = 0, cb = 0;
+        while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
+        while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
+        return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false);
+    }
+
+    // row offsets and the longest row
+    int *rp = nullptr, *cur = nullptr;
+    rc = f4j_dev_alloc(ctx, (size_t)(rows + 1) * 4, (void**)&rp);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)rows * 4, (void**)&cur);
+    if (!rc) {
+        F4J_CUDA(cudaMemsetAsync(rp, 0, (size_t)(rows + 1) * 4, ctx->stream));
+        k_count_rows<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, rp + 1);
+        k_max_int<<<(unsigned)std::min<int64_t>(grid1(rows), (int64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+            rows, rp + 1, mm + 3);
+        ctx->launches += 2;
+        rc = scan_inclusive(ctx, rp + 1, rows);
+    }
+    if (!rc) {
+        F4J_CUDA(cudaMemcpyAsync(&hm[3], mm + 3, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (hm[3] > SEG_CAP) {
+            f4j_dev_free(ctx, rp);
+            f4j_dev_free(ctx, cur);
+            f4j_dev_free(ctx, mm);
+            int rb = 0, cb = 0;
+            while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
+            while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
+            return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false);
+        }
+    }
+    unsigned long long* key = nullptr;
+    double* vin = nullptr;
+    int* longlist = nullptr;
+    const int64_t maxlong = std::min<int64_t>(rows, nnz / 33 + 1);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&key);
+    if (!rc && v) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&vin);
+    if (!rc) rc = f4j_dev_alloc(ctx, (size_t)maxlong * 4, (void**)&longlist);
+    if (!rc) {
+        F4J_CUDA(cudaMemsetAsync(cur, 0, (size_t)rows * 4, ctx->stream));
+        F4J_CUDA(cudaMemsetAsync(mm, 0, 4, ctx->stream));  // mm[0]: count of listed long rows
+        if (v) F4J_CUDA(cudaMemcpyAsync(vin, v, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+        k_coo_bucket<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, c, rp, cur, key);
+        k_coo_seg_warp<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, rp, key, r, c, vin, v,
+                                                                                   longlist, mm);
+        k_coo_seg_block<<<(unsigned)ctx->sm_count * 2, 512, 0, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v);
+        ctx->launches += 3;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
+    }
+    f4j_dev_free(ctx, key);
+    f4j_dev_free(ctx, vin);
+    f4j_dev_free(ctx, longlist);
+    f4j_dev_free(ctx, rp);
+    f4j_dev_free(ctx, cur);
+    f4j_dev_free(ctx, mm);
     return rc;
 }
 

@@ -188,6 +188,69 @@ def test_coo_sort_stable_bit_exact(f4j, oracle):
     assert np.array_equal(coo.data, ev)
 
 
+def _coo_sort_abi(f4j, r, c, v):
+    """f4j_coo_sort through the C ABI (no shape validation: negative indices reach it)."""
+    ctx = f4j.default_context()
+    r, c = np.ascontiguousarray(r, np.int32), np.ascontiguousarray(c, np.int32)
+    R, C = ctx.from_numpy(r), ctx.from_numpy(c)
+    V = ctx.from_numpy(np.ascontiguousarray(v, np.float64)) if v is not None else None
+    assert ctx.lib.f4j_coo_sort(ctx.handle, len(r), R.handle, C.handle, V.handle if V else None) == 0
+    ro, co = np.empty_like(r), np.empty_like(c)
+    R.download(ro)
+    C.download(co)
+    vo = None
+    if V is not None:
+        vo = np.empty(len(r))
+        V.download(vo)
+    return ro, co, vo
+
+
+def _shuffled_coo(rng, lens, cols, dup=0):
+    r = np.repeat(np.arange(len(lens)), lens)
+    c = np.concatenate([rng.choice(cols, n, replace=False) for n in lens]) if len(r) else np.zeros(0, int)
+    if dup:
+        k = rng.choice(len(r), dup, replace=False)
+        r, c = np.concatenate([r, r[k]]), np.concatenate([c, c[k]])
+    p = rng.permutation(len(r))
+    return r[p], c[p], rng.standard_normal(len(r))
+
+
+@pytest.mark.parametrize("case", ["segments", "beyond_segment_cap", "no_values"])
+def test_coo_sort_row_lengths_and_paths(f4j, oracle, case):
+    """Rows of 0..32 entries (ranked in a warp), 33..4096 (sorted in shared
+    memory) and beyond 4096 (the radix path), duplicates included."""
+    rng = np.random.default_rng(len(case))
+    lens = rng.integers(0, 40, 3000)
+    if case == "beyond_segment_cap":
+        lens[[10, 2000]] = [5000, 4097]
+    else:
+        lens[[5, 6, 700, 1500, 2999]] = [33, 64, 1000, 4096, 100]
+    r, c, v = _shuffled_coo(rng, lens, 6000, dup=700)
+    er, ec, ev, _ = oracle.coo_sort(r, c, v)
+    ro, co, vo = _coo_sort_abi(f4j, r, c, None if case == "no_values" else v)
+    assert np.array_equal(ro, er) and np.array_equal(co, ec)
+    if vo is not None:
+        assert np.array_equal(vo, ev)
+
+
+def test_coo_sort_negative_and_sparse_index_ranges(f4j, oracle):
+    rng = np.random.default_rng(8)
+    # negative indices sort first, as Flag4j's int comparison orders them
+    r = rng.integers(-50, 50, 4000)
+    c = rng.integers(-1000, 1000, 4000)
+    v = rng.standard_normal(4000)
+    er, ec, ev, _ = oracle.coo_sort(r, c, v)
+    ro, co, vo = _coo_sort_abi(f4j, r, c, v)
+    assert np.array_equal(ro, er) and np.array_equal(co, ec) and np.array_equal(vo, ev)
+    # a row range far larger than nnz
+    r = rng.integers(0, 1 << 30, 3000)
+    r[:40] = r[40]  # one row repeated
+    c = rng.integers(0, 1 << 30, 3000)
+    er, ec, ev, _ = oracle.coo_sort(r, c, v[:3000])
+    ro, co, vo = _coo_sort_abi(f4j, r, c, v[:3000])
+    assert np.array_equal(ro, er) and np.array_equal(co, ec) and np.array_equal(vo, ev)
+
+
 def test_transpose_and_permutation_bit_exact(f4j, oracle):
     from flag4j_gb300 import synth
     rows, cols = 9000, 5000
