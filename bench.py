@@ -421,6 +421,28 @@ def sparse_section(E, full, steps=20):
                 "sddmm64_ms": t_sddmm, "sddmm64_gbs_compulsory": b_sddmm / t_sddmm / 1e6,
                 "sddmm64_gflops": 2.0 * 64 * nnz / t_sddmm / 1e6})
     del X64, dC64, Y64, dS, S
+
+    # ---- CSR x CSR with a CSR result (CsrMatrix.mult2Csr): G G, G of rows/4 rows, Poisson(8)
+    g_rows = rows // 4
+    grp, gci, gv = synth.csr_poisson(g_rows, g_rows, lam=8.0, seed=77)
+    G = E.f.CsrMatrix((g_rows, g_rows), gv, grp, gci)
+    hG = G.handle(E.ctx)
+    nnz_out = []
+
+    def spgemm():
+        h = ctypes.c_void_p()
+        E.check(E.lib.f4j_csr_mult_csr(E.ctx.handle, hG, hG, ctypes.byref(h), None))
+        if not nnz_out:
+            nz = ctypes.c_int64()
+            E.check(E.lib.f4j_csr_info(h, None, None, ctypes.byref(nz)))
+            nnz_out.append(nz.value)
+        E.lib.f4j_csr_free(E.ctx.handle, h)
+    t_spgemm = E.timed(spgemm, max(3, steps // 4), 2)
+    products = int(np.diff(grp)[gci].sum())
+    res["spgemm_csr"] = {"rows": g_rows, "nnz_a": len(gv), "products": products, "nnz_c": nnz_out[0],
+                         "ms": t_spgemm, "gproducts_per_s": products / t_spgemm / 1e6,
+                         "note": "includes the result's device allocation and two host reads of sizes"}
+    del G
     return res
 
 

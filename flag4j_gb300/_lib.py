@@ -81,6 +81,8 @@ SIGNATURES = {
     "f4j_csr_info": (_i, [_v, _pi64, _pi64, _pi64]),
     "f4j_csr_buffers": (_i, [_v, _pv, _pv, _pv]),
     "f4j_csr_transpose": (_i, [_v, _v, _pv]),
+    "f4j_csr_mult_dense": (_i, [_v, _v, _v, _v, _rep]),
+    "f4j_csr_mult_csr": (_i, [_v, _v, _v, _pv, _rep]),
     "f4j_csr_transpose_perm": (_i, [_v, _v, _v]),
     "f4j_spmv": (_i, [_v, _v, _v, _v, _rep]),
     "f4j_spmv_ex": (_i, [_v, _v, _v, _v, _i, _rep]),

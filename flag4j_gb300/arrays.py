@@ -450,11 +450,37 @@ class CsrMatrix:
                                       ctypes.byref(rep)))
             out = (CVector._from_device(Shape(self.numRows), y, ctx) if vec
                    else CMatrix._from_device(Shape(self.numRows, nc), y, ctx))
+        elif isinstance(b, CsrMatrix) and not isinstance(b, CsrCMatrix):
+            # CsrMatrix.mult(CsrMatrix) -> RealCsrMatMult.standard (RealCsrMatMult.java:53-75): dense result
+            ensure_mat_mult_shapes(self.shape, b.shape)
+            ctx = self._ctx or b._ctx or default_context()
+            y = ctx.alloc(max(8 * self.numRows * b.numCols, 8))
+            check(ctx.lib.f4j_csr_mult_dense(ctx.handle, self.handle(ctx), b.handle(ctx), y.handle,
+                                             ctypes.byref(rep)))
+            out = Matrix._from_device(Shape(self.numRows, b.numCols), y, ctx)
         else:
             raise NotImplementedError("CsrMatrix.mult(%s) is not on this engine's path" % type(b).__name__)
         if report is not None:
             report.update(rep.as_dict())
         return out
+
+    def mult2Csr(self, b):
+        """CsrMatrix.mult2Csr(CsrMatrix) -> RealCsrMatMult.standardAsSparse (RealCsrMatMult.java:92-131):
+        the product as CSR, every touched column stored (explicit zeros too), bit-identical."""
+        ensure_mat_mult_shapes(self.shape, b.shape)
+        ctx = self._ctx or b._ctx or default_context()
+        h = ctypes.c_void_p()
+        check(ctx.lib.f4j_csr_mult_csr(ctx.handle, self.handle(ctx), b.handle(ctx), ctypes.byref(h), None))
+        nnz = ctypes.c_int64()
+        check(ctx.lib.f4j_csr_info(h, None, None, ctypes.byref(nnz)))
+        return CsrMatrix._from_handle((self.numRows, b.numCols), nnz.value, h, None, ctx)
+
+    def multTranspose(self, b):
+        """CsrMatrix.multTranspose(CsrMatrix) -> RealCsrMatMult.standard(this, b.T()) (CsrMatrix.java:809-810)."""
+        if not isinstance(b, CsrMatrix) or isinstance(b, CsrCMatrix):
+            raise NotImplementedError("CsrMatrix.multTranspose(%s) is not on this engine's path" % type(b).__name__)
+        ensure_mat_mult_shapes(self.shape, Shape(b.numCols, b.numRows))
+        return self.mult(b.T())
 
     def multTransposeLeft(self, b):
         """S^T * b without forming S^T (cached transpose permutation)."""

@@ -548,13 +548,14 @@ __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const u
     if (lane < len) coo_emit(q0 + rank, (int)row, k, ro, co, vin, vo);
 }
 
-// a block per listed row (33 .. SEG_CAP entries): bitonic sort in shared memory
+// a block per listed row (33 .. pmax entries, pmax a power of two up to
+// SEG_CAP): bitonic sort in shared memory (pmax keys)
 __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ longlist, const int* __restrict__ nlong,
                                                        const int* __restrict__ rp,
                                                        const unsigned long long* __restrict__ key,
                                                        int* __restrict__ ro, int* __restrict__ co,
                                                        const double* __restrict__ vin, double* __restrict__ vo) {
-    __shared__ unsigned long long sk[SEG_CAP];
+    extern __shared__ unsigned long long sk[];
     const int nl = *nlong;
     for (int b = blockIdx.x; b < nl; b += gridDim.x) {
         const int row = longlist[b];
@@ -581,6 +582,99 @@ __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ l
         for (int i = threadIdx.x; i < len; i += blockDim.x) coo_emit(q0 + i, row, sk[i], ro, co, vin, vo);
         __syncthreads();
     }
+}
+
+// ---------------- CSR x CSR (RealCsrMatMult, src/main/java/org/flag4j/linalg/
+// ops/sparse/csr/real/RealCsrMatMult.java)
+// Dense result (standard, :53-75): a warp per row i of A walks the row's
+// nonzeros in storage order; for each, the lanes add a * B[k, :] into the
+// dense row i of C (zeroed), each product and sum rounded.  A row of B holds
+// distinct columns, so the lanes of one step touch distinct entries; the
+// __syncwarp orders successive steps.
+__global__ void k_spgemm_dense(int64_t rows, int64_t n2, const int* __restrict__ arp, const int* __restrict__ aci,
+                               const double* __restrict__ av, const int* __restrict__ brp,
+                               const int* __restrict__ bci, const double* __restrict__ bv, double* __restrict__ C) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= rows) return;
+    double* Cr = C + row * n2;
+    const int q1 = __ldg(&arp[row + 1]);
+    for (int q = __ldg(&arp[row]); q < q1; q++) {
+        const int k = __ldg(&aci[q]);
+        const double a = __ldg(&av[q]);
+        const int t1 = __ldg(&brp[k + 1]);
+        for (int t = __ldg(&brp[k]) + lane; t < t1; t += 32) {
+            const int j = __ldg(&bci[t]);
+            Cr[j] = __dadd_rn(Cr[j], __dmul_rn(a, __ldg(&bv[t])));
+        }
+        __syncwarp();
+    }
+}
+
+// CSR result (standardAsSparse, :92-131), expand-sort-compress: every product
+// b * a is written out in the reference's loop order (rows of A, a row's
+// nonzeros, then the nonzeros of B's row), stably sorted by (row, column),
+// and each run of one (row, column) summed in order starting from its first
+// product, as HashMap.merge(col, b * a, Double::sum) does.
+__global__ void k_spgemm_len(int64_t annz, const int* __restrict__ aci, const int* __restrict__ brp,
+                             int* __restrict__ len, unsigned long long* __restrict__ total) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long l = 0;
+    if (q < annz) {
+        const int k = __ldg(&aci[q]);
+        l = (unsigned long long)(__ldg(&brp[k + 1]) - __ldg(&brp[k]));
+        len[q] = (int)l;
+    }
+    for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if (threadIdx.x % 32 == 0 && l) atomicAdd(total, l);
+}
+
+// off: inclusive scan of the expansion lengths, one per nonzero of A
+__global__ void k_spgemm_expand(int64_t rows, const int* __restrict__ arp, const int* __restrict__ aci,
+                                const double* __restrict__ av, const int* __restrict__ brp,
+                                const int* __restrict__ bci, const double* __restrict__ bv,
+                                const int* __restrict__ off, int* __restrict__ er, int* __restrict__ ec,
+                                double* __restrict__ ev) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= rows) return;
+    const int q1 = __ldg(&arp[row + 1]);
+    for (int q = __ldg(&arp[row]); q < q1; q++) {
+        const int k = __ldg(&aci[q]);
+        const double a = __ldg(&av[q]);
+        const int t0 = __ldg(&brp[k]), t1 = __ldg(&brp[k + 1]);
+        const int base = (q ? __ldg(&off[q - 1]) : 0) - t0;
+        for (int t = t0 + lane; t < t1; t += 32) {
+            er[base + t] = (int)row;
+            ec[base + t] = __ldg(&bci[t]);
+            ev[base + t] = __dmul_rn(__ldg(&bv[t]), a);
+        }
+    }
+}
+
+// fs: inclusive scan of the run-start flags of the sorted expansion
+__global__ void k_run_flags(int64_t n, const int* __restrict__ r, const int* __restrict__ c, int* __restrict__ f) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) f[e] = (e == 0 || r[e] != r[e - 1] || c[e] != c[e - 1]) ? 1 : 0;
+}
+
+__global__ void k_run_starts(int64_t n, const int* __restrict__ fs, int* __restrict__ starts) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n && (e == 0 || fs[e] != fs[e - 1])) starts[fs[e] - 1] = (int)e;
+}
+
+__global__ void k_run_sum(int64_t runs, int64_t n, const int* __restrict__ starts, const int* __restrict__ r,
+                          const int* __restrict__ c, const double* __restrict__ v, int* __restrict__ oc,
+                          double* __restrict__ ov, int* __restrict__ rowcnt) {
+    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= runs) return;
+    const int s0 = starts[u];
+    const int64_t s1 = u + 1 < runs ? starts[u + 1] : n;
+    double acc = v[s0];
+    for (int64_t e = s0 + 1; e < s1; e++) acc = __dadd_rn(acc, v[e]);
+    oc[u] = c[s0];
+    ov[u] = acc;
+    atomicAdd(&rowcnt[r[s0]], 1);
 }
 
 }  // namespace
@@ -940,17 +1034,9 @@ static int coo_sort_radix(f4j_ctx* ctx, int64_t nnz, int* rowidx, int* colidx, d
     return rc;
 }
 
-extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
-    F4J_CHECK_CTX(ctx);
-    if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
-    if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
-    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || (vals && vals->bytes < (size_t)nnz * 8))
-        return f4j_fail(F4J_ERR_ARG, "COO buffers shorter than nnz");
+// Stable sort of n device triplets by (row, col), in place (v may be null).
+static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
     if (nnz <= 1) return F4J_OK;
-    F4J_CUDA(cudaSetDevice(ctx->device));
-    int* r = (int*)rowidx->ptr;
-    int* c = (int*)colidx->ptr;
-    double* v = vals ? (double*)vals->ptr : nullptr;
     const unsigned red_grid = (unsigned)std::min<int64_t>(grid1(nnz), (int64_t)ctx->sm_count * 8);
 
     // index range: mm = {min of rows and columns, max row, max column, longest row}
@@ -1016,7 +1102,12 @@ extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf c
         k_coo_bucket<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, c, rp, cur, key);
         k_coo_seg_warp<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, rp, key, r, c, vin, v,
                                                                                    longlist, mm);
-        k_coo_seg_block<<<(unsigned)ctx->sm_count * 2, 512, 0, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v);
+        // block path sized to the longest row: pmax keys of shared memory, pmax / 2 threads
+        int pmax = 64;
+        while (pmax < hm[3]) pmax <<= 1;
+        const int bthreads = pmax / 2 < 512 ? pmax / 2 : 512;
+        const unsigned bgrid = (unsigned)std::min<int64_t>(maxlong, (int64_t)ctx->sm_count * 32);
+        k_coo_seg_block<<<bgrid, bthreads, (size_t)pmax * 8, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v);
         ctx->launches += 3;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
@@ -1028,6 +1119,133 @@ extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf c
     f4j_dev_free(ctx, cur);
     f4j_dev_free(ctx, mm);
     return rc;
+}
+
+extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
+    F4J_CHECK_CTX(ctx);
+    if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
+    if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
+    if (rowidx->bytes < (size_t)nnz * 4 || colidx->bytes < (size_t)nnz * 4 || (vals && vals->bytes < (size_t)nnz * 8))
+        return f4j_fail(F4J_ERR_ARG, "COO buffers shorter than nnz");
+    if (nnz <= 1) return F4J_OK;
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    return coo_sort_dev(ctx, nnz, (int*)rowidx->ptr, (int*)colidx->ptr, vals ? (double*)vals->ptr : nullptr);
+}
+
+// ------------------------------------------------------------------ CSR x CSR
+extern "C" int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null argument");
+    if (A->cols != B->rows) return f4j_shape_error(A->rows, A->cols, B->rows, B->cols);
+    if (C->bytes < (size_t)(A->rows * B->cols) * 8) return f4j_fail(F4J_ERR_ARG, "C buffer too small");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    if (A->rows * B->cols > 0) {
+        F4J_CUDA(cudaMemsetAsync(C->ptr, 0, (size_t)(A->rows * B->cols) * 8, ctx->stream));
+        f4j_prof_begin(ctx);
+        k_spgemm_dense<<<(unsigned)f4j_cdiv(A->rows * 32, 256), 256, 0, ctx->stream>>>(
+            A->rows, B->cols, (const int*)A->rowptr->ptr, (const int*)A->colidx->ptr, (const double*)A->vals->ptr,
+            (const int*)B->rowptr->ptr, (const int*)B->colidx->ptr, (const double*)B->vals->ptr, (double*)C->ptr);
+        f4j_prof_end(ctx);
+        F4J_LAUNCHED(ctx);
+    }
+    if (rep) {
+        *rep = f4j_report{};
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
+}
+
+extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!A || !B || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (A->cols != B->rows) return f4j_shape_error(A->rows, A->cols, B->rows, B->cols);
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    int64_t l0 = ctx->launches;
+    const int64_t annz = A->nnz, rows = A->rows;
+    const int *arp = (const int*)A->rowptr->ptr, *aci = (const int*)A->colidx->ptr;
+    const int *brp = (const int*)B->rowptr->ptr, *bci = (const int*)B->colidx->ptr;
+    const double *av = (const double*)A->vals->ptr, *bv = (const double*)B->vals->ptr;
+
+    // expansion size
+    int* len = nullptr;
+    unsigned long long* total = nullptr;
+    unsigned long long E = 0;
+    int rc = f4j_dev_alloc(ctx, (size_t)(annz > 0 ? annz : 1) * 4, (void**)&len);
+    if (!rc) rc = f4j_dev_alloc(ctx, 8, (void**)&total);
+    if (!rc && annz > 0) {
+        F4J_CUDA(cudaMemsetAsync(total, 0, 8, ctx->stream));
+        k_spgemm_len<<<(unsigned)f4j_cdiv(annz, 256), 256, 0, ctx->stream>>>(annz, aci, brp, len, total);
+        ctx->launches++;
+        F4J_CUDA(cudaMemcpyAsync(&E, total, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (E > (unsigned long long)INT32_MAX)
+            rc = f4j_fail(F4J_ERR_UNSUPPORTED, "CSR product expands to %llu products, over 2^31 - 1", E);
+    }
+    int *er = nullptr, *ec = nullptr, *fs = nullptr, *starts = nullptr;
+    double* ev = nullptr;
+    int64_t runs = 0;
+    if (!rc && E > 0) {
+        rc = scan_inclusive(ctx, len, annz);
+        if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&er);
+        if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&ec);
+        if (!rc) rc = f4j_dev_alloc(ctx, E * 8, (void**)&ev);
+        if (!rc) {
+            k_spgemm_expand<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, arp, aci, av, brp, bci,
+                                                                                       bv, len, er, ec, ev);
+            ctx->launches++;
+            rc = coo_sort_dev(ctx, (int64_t)E, er, ec, ev);
+        }
+        if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&fs);
+        if (!rc) {
+            k_run_flags<<<(unsigned)f4j_cdiv(E, 256), 256, 0, ctx->stream>>>((int64_t)E, er, ec, fs);
+            ctx->launches++;
+            rc = scan_inclusive(ctx, fs, (int64_t)E);
+        }
+        if (!rc) {
+            int last = 0;
+            F4J_CUDA(cudaMemcpyAsync(&last, fs + E - 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+            runs = last;
+            rc = f4j_dev_alloc(ctx, (size_t)runs * 4, (void**)&starts);
+        }
+        if (!rc) {
+            k_run_starts<<<(unsigned)f4j_cdiv(E, 256), 256, 0, ctx->stream>>>((int64_t)E, fs, starts);
+            ctx->launches++;
+        }
+    }
+    f4j_csr T = nullptr;
+    if (!rc) rc = alloc_owned_csr(ctx, rows, B->cols, runs, &T);
+    if (!rc) {
+        int* trp = (int*)T->rowptr->ptr;
+        F4J_CUDA(cudaMemsetAsync(trp, 0, (size_t)(rows + 1) * 4, ctx->stream));
+        if (runs > 0) {
+            k_run_sum<<<(unsigned)f4j_cdiv(runs, 256), 256, 0, ctx->stream>>>(
+                runs, (int64_t)E, starts, er, ec, ev, (int*)T->colidx->ptr, (double*)T->vals->ptr, trp + 1);
+            ctx->launches++;
+            rc = scan_inclusive(ctx, trp + 1, rows);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (!rc && e != cudaSuccess) rc = f4j_cuda_fail(e, "CSR x CSR");
+    }
+    f4j_dev_free(ctx, len);
+    f4j_dev_free(ctx, total);
+    f4j_dev_free(ctx, er);
+    f4j_dev_free(ctx, ec);
+    f4j_dev_free(ctx, ev);
+    f4j_dev_free(ctx, fs);
+    f4j_dev_free(ctx, starts);
+    if (rc) {
+        if (T) f4j_csr_free(ctx, T);
+        return rc;
+    }
+    *out = T;
+    if (rep) {
+        *rep = f4j_report{};
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    return F4J_OK;
 }
 
 extern "C" int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out) {

@@ -204,6 +204,22 @@ int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out);
 /* Copy out the cached transpose permutation (int32[nnz]: for each position of
  * S^T in RealCsrOps.transpose order, the source nnz index of S). */
 int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out);
+/* CSR x CSR with a dense result, CsrMatrix.mult(CsrMatrix) ->
+ *   RealCsrMatMult.standard (CsrMatrix.java:748-749,
+ *   src/main/java/org/flag4j/linalg/ops/sparse/csr/real/RealCsrMatMult.java:53-75):
+ *   C (A.rows x B.cols, row-major, overwritten) accumulates a * b over A's row
+ *   nonzeros in storage order, each product and sum rounded; bit-identical.
+ *   CsrMatrix.multTranspose(CsrMatrix) (CsrMatrix.java:809-810) is this with
+ *   f4j_csr_transpose(B).  F4J_ERR_SHAPE when A.cols != B.rows. */
+int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report* report);
+/* CSR x CSR with a CSR result (owned by *out), CsrMatrix.mult2Csr(CsrMatrix) ->
+ *   RealCsrMatMult.standardAsSparse (CsrMatrix.java:778-779,
+ *   RealCsrMatMult.java:92-131): every column a row's products touch is
+ *   stored, ascending, even where the products cancel; per entry the products
+ *   are summed in the reference's loop order starting from the first
+ *   (HashMap.merge).  Bit-identical.  F4J_ERR_UNSUPPORTED when the product
+ *   count (sum over A's nonzeros of the length of B's row) exceeds 2^31 - 1. */
+int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* report);
 
 /* y = S x.  Replaces CsrMatrix.mult(Vector) -> RealCsrDenseMatMult.standardVector
  *   (CsrMatrix.java:1170-1171, src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/

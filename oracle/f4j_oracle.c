@@ -386,6 +386,81 @@ static int orc_key_less(const int32_t* r, const int32_t* c, int64_t a, int64_t b
     return c[a] < c[b];
 }
 
+/* CSR x CSR, dense result: RealCsrMatMult.standard                      */
+/* (src/main/java/org/flag4j/linalg/ops/sparse/csr/real/                  */
+/* RealCsrMatMult.java:53-75): destEntries[i*n2 + bCol] += aVal*bVal over */
+/* row i's nonzeros in storage order, then the nonzeros of B's row aCol;  */
+/* each product and sum rounded (no contraction).                        */
+void orc_spgemm_dense(int64_t rows, int64_t n2, const int32_t* arp, const int32_t* aci, const double* av,
+                      const int32_t* brp, const int32_t* bci, const double* bv, double* C) {
+    for (int64_t i = 0; i < rows * n2; i++) C[i] = 0.0;
+    for (int64_t i = 0; i < rows; i++) {
+        double* d = C + i * n2;
+        for (int32_t q = arp[i]; q < arp[i + 1]; q++) {
+            const int32_t k = aci[q];
+            const double a = av[q];
+            for (int32_t t = brp[k]; t < brp[k + 1]; t++) {
+                const double prod = a * bv[t];
+                d[bci[t]] = d[bci[t]] + prod;
+            }
+        }
+    }
+}
+
+static int orc_cmp_i32(const void* x, const void* y) {
+    const int32_t a = *(const int32_t*)x, b = *(const int32_t*)y;
+    return (a > b) - (a < b);
+}
+
+/* CSR x CSR, CSR result: RealCsrMatMult.standardAsSparse (:92-131).  Per  */
+/* row, tempMap.merge(bCol, bVal*aVal, Double::sum) in the same loop order */
+/* (:107-118): the first product of a column is stored as is, later ones  */
+/* are added to it (old + new); then the row's columns ascending          */
+/* (:121-127), every touched column kept.  Fills out_rp (rows + 1) and,   */
+/* when out_ci / out_v are non-null, the entries; returns the nnz.        */
+int64_t orc_spgemm_csr(int64_t rows, int64_t n2, const int32_t* arp, const int32_t* aci, const double* av,
+                       const int32_t* brp, const int32_t* bci, const double* bv, int32_t* out_rp,
+                       int32_t* out_ci, double* out_v) {
+    double* acc = (double*)calloc(n2 > 0 ? n2 : 1, sizeof(double));
+    unsigned char* seen = (unsigned char*)calloc(n2 > 0 ? n2 : 1, 1);
+    int32_t* list = (int32_t*)malloc(sizeof(int32_t) * (n2 > 0 ? n2 : 1));
+    int64_t nnz = 0;
+    out_rp[0] = 0;
+    for (int64_t i = 0; i < rows; i++) {
+        int64_t nl = 0;
+        for (int32_t q = arp[i]; q < arp[i + 1]; q++) {
+            const int32_t k = aci[q];
+            const double a = av[q];
+            for (int32_t t = brp[k]; t < brp[k + 1]; t++) {
+                const int32_t j = bci[t];
+                const double prod = bv[t] * a;
+                if (!seen[j]) {
+                    seen[j] = 1;
+                    acc[j] = prod;
+                    list[nl++] = j;
+                } else {
+                    acc[j] = acc[j] + prod;
+                }
+            }
+        }
+        qsort(list, (size_t)nl, sizeof(int32_t), orc_cmp_i32);
+        for (int64_t u = 0; u < nl; u++) {
+            const int32_t j = list[u];
+            if (out_ci) {
+                out_ci[nnz] = j;
+                out_v[nnz] = acc[j];
+            }
+            nnz++;
+            seen[j] = 0;
+        }
+        out_rp[i + 1] = (int32_t)nnz;
+    }
+    free(acc);
+    free(seen);
+    free(list);
+    return nnz;
+}
+
 void orc_coo_sort(int64_t nnz, int32_t* rowidx, int32_t* colidx, double* vals, int64_t* perm_out) {
     int64_t* p = (int64_t*)malloc(sizeof(int64_t) * (nnz > 0 ? nnz : 1));
     int64_t* t = (int64_t*)malloc(sizeof(int64_t) * (nnz > 0 ? nnz : 1));

@@ -55,11 +55,14 @@ def lib():
                 "orc_sddmm": [i64, i64, p, p, p, p, p],
                 "orc_truth_sampled": [i64, p, i64, i32, p, i64, i32, i32, i64, p, p, p, p, p],
                 "orc_absgemm": [i64, i64, i64, p, p, p, i32],
+                "orc_spgemm_dense": [i64, i64, p, p, p, p, p, p, p],
+                "orc_spgemm_csr": [i64, i64, p, p, p, p, p, p, p, p, p],
             }
             for name, args in sig.items():
                 f = getattr(L, name)
                 f.argtypes = args
                 f.restype = None
+            L.orc_spgemm_csr.restype = ctypes.c_int64
             _lib = L
     return _lib
 
@@ -194,6 +197,26 @@ def spmm(rowptr, colidx, vals, X, threads=1):
     Y = np.empty((rows, nc), np.float64)
     lib().orc_spmm(rows, nc, _p(rowptr), _p(colidx), _p(vals), _p(X), _p(Y), threads)
     return Y
+
+
+def spgemm_dense(arp, aci, av, brp, bci, bv, n2):
+    """CsrMatrix.mult(CsrMatrix): RealCsrMatMult.standard, dense (rows of A) x n2 result."""
+    arp, aci, av, brp, bci, bv = _i32(arp), _i32(aci), _f64(av), _i32(brp), _i32(bci), _f64(bv)
+    rows = len(arp) - 1
+    C = np.empty((rows, n2), np.float64)
+    lib().orc_spgemm_dense(rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(C))
+    return C
+
+
+def spgemm_csr(arp, aci, av, brp, bci, bv, n2):
+    """CsrMatrix.mult2Csr(CsrMatrix): RealCsrMatMult.standardAsSparse -> (rowptr, colidx, vals)."""
+    arp, aci, av, brp, bci, bv = _i32(arp), _i32(aci), _f64(av), _i32(brp), _i32(bci), _f64(bv)
+    rows = len(arp) - 1
+    rp = np.empty(rows + 1, np.int32)
+    nnz = lib().orc_spgemm_csr(rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rp), None, None)
+    ci, v = np.empty(max(nnz, 1), np.int32), np.empty(max(nnz, 1), np.float64)
+    lib().orc_spgemm_csr(rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rp), _p(ci), _p(v))
+    return rp, ci[:nnz], v[:nnz]
 
 
 def spmm_rz(rowptr, colidx, vals, X, threads=1):

@@ -13,6 +13,7 @@ Files read (paths within the Flag4j project):
   src/test/java/org/flag4j/arrays/dense/matrix/MatrixVectorTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java
+  src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java
 
 Usage:  python tests/golden/make_golden.py [/path/to/flag4j]
 The fixture is committed; the GPU machine never needs the reference tree.
@@ -33,6 +34,7 @@ FILES = {
     "matrix_vector": T + "arrays/dense/matrix/MatrixVectorTests.java",
     "csr_dense": T + "arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java",
     "csr_transpose": T + "arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java",
+    "csr_csr": T + "arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java",
 }
 
 # ---------------------------------------------------------------- parsing

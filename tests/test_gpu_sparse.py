@@ -1,6 +1,7 @@
 """CSR products and sparse structure on the GPU: bit-identical to the oracle's
-restatement of Flag4j's loops (RealCsrDenseMatMult, CooMatrix.toCsr,
-CooDataSorter, RealCsrOps.transpose); SDDMM within 2 k u sum|a||b|."""
+restatement of Flag4j's loops (RealCsrDenseMatMult, RealCsrMatMult,
+CooMatrix.toCsr, CooDataSorter, RealCsrOps.transpose); the FMA mode and SDDMM
+within 2 k u sum|a||b|."""
 import ctypes
 import math
 
@@ -353,3 +354,85 @@ def test_device_csr_validation_messages(f4j):
         _wrap(f4j, 3, 3, [0, 1, 2, 2], [0, 1, 2], [1.0, 2.0, 3.0])
     with pytest.raises(f4j.IllegalArgumentException, match="Invalid index"):
         f4j.CooMatrix((3, 3), [1.0, 2.0], [0, 3], [0, 1]).toCsr()
+
+
+# ------------------------------------------------------------------ CSR x CSR
+def _bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.int64)
+
+
+def test_golden_csr_csr_products(f4j, golden):
+    # RealCsrCsrMatMultTests.java:34-189: A.mult(B) equals aDense.mult(bDense),
+    # A.mult2Csr(B) equals that product's toCsr(); shape mismatches throw
+    for c in golden["csr_csr"]:
+        a, b = np.array(c["vars"]["aEntries"]), np.array(c["vars"]["bEntries"])
+        A, B = f4j.Matrix(a).toCsr(), f4j.Matrix(b).toCsr()
+        if c["call"] == "assertThrows":
+            with pytest.raises(f4j.LinearAlgebraException):
+                A.mult(B) if c["method"] == "multTests" else A.mult2Csr(B)
+            continue
+        if c["call"] != "assertEquals":
+            continue
+        exp = f4j.Matrix(a).mult(f4j.Matrix(b), mode="exact")
+        if c["method"] == "multTests":
+            assert A.mult(B) == exp
+        else:
+            got, e = A.mult2Csr(B), exp.toCsr()
+            assert np.array_equal(got.rowPointers, e.rowPointers) and np.array_equal(got.colIndices, e.colIndices)
+            assert np.array_equal(got.data, e.data)
+
+
+@pytest.mark.parametrize("m,k,n,la,lb", [(1, 1, 1, 1.0, 1.0), (2000, 1500, 1800, 8.0, 6.0), (700, 300, 5000, 40.0, 30.0)])
+def test_csr_csr_bit_identical(f4j, oracle, m, k, n, la, lb):
+    from flag4j_gb300 import synth
+    arp, aci, av = synth.csr_poisson(m, k, lam=la, hi=min(k, 256), seed=m + 1)
+    brp, bci, bv = synth.csr_poisson(k, n, lam=lb, hi=min(n, 256), seed=k + 2)
+    A, B = f4j.CsrMatrix((m, k), av, arp, aci), f4j.CsrMatrix((k, n), bv, brp, bci)
+    assert np.array_equal(_bits(A.mult(B).toNumpy()), _bits(oracle.spgemm_dense(arp, aci, av, brp, bci, bv, n)))
+    rp, ci, v = oracle.spgemm_csr(arp, aci, av, brp, bci, bv, n)
+    S = A.mult2Csr(B)
+    assert S.shape == (m, n) and S.nnz == len(v)
+    assert np.array_equal(S.rowPointers, rp) and np.array_equal(S.colIndices, ci)
+    assert np.array_equal(_bits(S.data), _bits(v))
+
+
+def test_csr_csr_cancellations_signed_zeros_and_empty(f4j, oracle):
+    # explicit zeros in B, products that cancel, -0.0 first products, empty rows
+    rng = np.random.default_rng(12)
+    m, k, n = 400, 300, 200
+    a = np.where(rng.random((m, k)) < 0.03, rng.choice([-1.0, 1.0, 2.0], (m, k)), 0.0)
+    a[50:60] = 0.0
+    b = np.where(rng.random((k, n)) < 0.05, rng.choice([-2.0, 2.0, 0.5], (k, n)), 0.0)
+    arp, aci, av = _csr_of(a)
+    brp, bci, bv = _csr_of(b)
+    bv[::7] = 0.0  # stored zeros: products of -0.0 and +0.0
+    A, B = f4j.CsrMatrix((m, k), av, arp, aci), f4j.CsrMatrix((k, n), bv, brp, bci)
+    assert np.array_equal(_bits(A.mult(B).toNumpy()), _bits(oracle.spgemm_dense(arp, aci, av, brp, bci, bv, n)))
+    rp, ci, v = oracle.spgemm_csr(arp, aci, av, brp, bci, bv, n)
+    S = A.mult2Csr(B)
+    assert np.count_nonzero(v == 0.0) > 0 and np.count_nonzero(np.signbit(v) & (v == 0.0)) > 0
+    assert np.array_equal(S.rowPointers, rp) and np.array_equal(S.colIndices, ci)
+    assert np.array_equal(_bits(S.data), _bits(v))
+    Z = f4j.CsrMatrix((m, k), np.zeros(0), np.zeros(m + 1, np.int32), np.zeros(0, np.int32))
+    assert not Z.mult(B).toNumpy().any()
+    E = Z.mult2Csr(B)
+    assert E.nnz == 0 and not E.rowPointers.any()
+
+
+def test_csr_csr_mult_transpose(f4j, oracle):
+    from flag4j_gb300 import synth
+    arp, aci, av = synth.csr_poisson(900, 700, lam=10.0, seed=3)
+    brp, bci, bv = synth.csr_poisson(500, 700, lam=12.0, seed=4)
+    A, B = f4j.CsrMatrix((900, 700), av, arp, aci), f4j.CsrMatrix((500, 700), bv, brp, bci)
+    trp, tci, tv, _ = oracle.csr_transpose(500, 700, brp, bci, bv)
+    exp = oracle.spgemm_dense(arp, aci, av, trp, tci, tv, 500)
+    assert np.array_equal(_bits(A.multTranspose(B).toNumpy()), _bits(exp))
+    with pytest.raises(f4j.LinearAlgebraException):
+        A.multTranspose(f4j.CsrMatrix((5, 6), np.ones(1), np.array([0, 1, 1, 1, 1, 1]), np.array([2])))
+
+
+def _csr_of(a):
+    r, c = np.nonzero(a != 0.0)
+    rp = np.zeros(a.shape[0] + 1, np.int32)
+    np.cumsum(np.bincount(r, minlength=a.shape[0]), out=rp[1:])
+    return rp, c.astype(np.int32), a[r, c].copy()

@@ -92,6 +92,39 @@ def test_csr_transpose_matches_dense_transpose(oracle, golden):
         assert np.array_equal(v[perm], tv)
 
 
+def test_csr_csr_products_equal_dense(oracle, golden):
+    # RealCsrCsrMatMultTests.java:34-92: A.mult(B) equals aDense.mult(bDense);
+    # :94-189: A.mult2Csr(B) equals aDense.mult(bDense).toCsr()
+    mult = [c for c in golden["csr_csr"] if c["call"] == "assertEquals"]
+    assert [c["method"] for c in mult] == ["multTests", "multTests", "multAsCsrTests", "multAsCsrTests"]
+    for c in mult:
+        a, b = np.array(c["vars"]["aEntries"]), np.array(c["vars"]["bEntries"])
+        (arp, aci, av), (brp, bci, bv) = _csr_of_dense(a), _csr_of_dense(b)
+        exp = oracle.dgemm(a, b)
+        if c["method"] == "multTests":
+            assert np.array_equal(oracle.spgemm_dense(arp, aci, av, brp, bci, bv, b.shape[1]), exp)
+        else:
+            rp, ci, v = oracle.spgemm_csr(arp, aci, av, brp, bci, bv, b.shape[1])
+            erp, eci, ev = _csr_of_dense(exp)
+            assert np.array_equal(rp, erp) and np.array_equal(ci, eci) and np.array_equal(v, ev)
+    # the shape-mismatch cases keep a.shape[1] != b.shape[0]
+    for c in [c for c in golden["csr_csr"] if c["call"] == "assertThrows"]:
+        assert np.array(c["vars"]["aEntries"]).shape[1] != np.array(c["vars"]["bEntries"]).shape[0]
+
+
+def test_csr_csr_sparse_result_keeps_cancellations(oracle):
+    # standardAsSparse stores every touched column: 1*x + 1*(-x) is an explicit 0.0,
+    # and a lone product -1 * 0.0 stays -0.0 (HashMap.merge keeps the first value as is)
+    arp, aci, av = np.array([0, 2, 3]), np.array([0, 1, 0]), np.array([1.0, 1.0, -1.0])
+    brp, bci, bv = np.array([0, 2, 3]), np.array([0, 2, 0]), np.array([2.5, 0.0, -2.5])
+    rp, ci, v = oracle.spgemm_csr(arp, aci, av, brp, bci, bv, 3)
+    assert list(rp) == [0, 2, 4] and list(ci) == [0, 2, 0, 2]
+    assert v[0] == 0.0 and np.signbit(v[3]) and v[3] == 0.0 and not np.signbit(v[1])
+    # the dense result starts from +0.0: 0.0 + -0.0 is +0.0
+    C = oracle.spgemm_dense(arp, aci, av, brp, bci, bv, 3)
+    assert not np.signbit(C[1, 2])
+
+
 def test_coo_sort_is_stable_lexicographic(oracle):
     rng = np.random.default_rng(3)
     r = rng.integers(0, 5, 400).astype(np.int32)
