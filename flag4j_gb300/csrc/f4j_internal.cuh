@@ -27,6 +27,8 @@ struct f4j_csr_s {
     void* t_rowptr;
     void* t_perm;
     void* t_rowidx;
+    // Row of each nonzero (int32[nnz]), built on first use by f4j_sddmm.
+    void* rowidx;
 };
 
 struct f4j_ctx {

@@ -243,51 +243,39 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// SDDMM with 64 columns: warp per row of S; eight lanes per nonzero, up to
-// 4 * SDDMM_GROUPS nonzeros in flight per warp; a lane holds its eight
-// columns of A's row in registers and loads B's row with 16-byte loads, then
-// an 8-lane tree sum.  Gathering B rows is latency-bound, so the width of the
-// gather in flight sets the speed.
-constexpr int SDDMM_GROUPS = 2;  // 4 measured 18 % slower at Poisson(16) rows
+// SDDMM with 64 columns, flat over the nonzeros: a warp takes 8 consecutive
+// nonzeros whatever their rows, a group of 4 lanes one nonzero, a lane 16
+// columns of the row of A and of the row of B (16-byte loads), 16 FMAs and a
+// 2-step tree sum: 18 FP64 warp instructions per 8 nonzeros, and no partly
+// filled groups at the ends of rows.  rowidx: the row of each nonzero.
 __global__ void __launch_bounds__(256)
-    k_sddmm64(int64_t rows, const int* __restrict__ rowptr, const int* __restrict__ colidx,
-              const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ out) {
-    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x % 32, g = lane / 8, l8 = lane % 8;
-    if (row >= rows) return;
-    const int q0 = rowptr[row], q1 = rowptr[row + 1];
-    const double2* arow = reinterpret_cast<const double2*>(A + row * 64) + l8 * 4;
-    double2 a[4];
+    k_sddmm64f(int64_t nnz, const int* __restrict__ rowidx, const int* __restrict__ colidx,
+               const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ out) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 4;
+    const int l4 = threadIdx.x % 4;
+    double2 a[8], b[8];
+    if (q < nnz) {
+        const double2* arow = reinterpret_cast<const double2*>(A + (int64_t)__ldg(&rowidx[q]) * 64) + l4 * 8;
+        const double2* brow = reinterpret_cast<const double2*>(B + (int64_t)__ldg(&colidx[q]) * 64) + l4 * 8;
 #pragma unroll
-    for (int u = 0; u < 4; u++) a[u] = __ldg(arow + u);
-    for (int qb = q0; qb < q1; qb += 4 * SDDMM_GROUPS) {
-        double s[SDDMM_GROUPS];
-        double2 b[SDDMM_GROUPS][4];
-#pragma unroll
-        for (int h = 0; h < SDDMM_GROUPS; h++) {
-            const int q = qb + 4 * h + g;
-            if (q < q1) {
-                const double2* brow = reinterpret_cast<const double2*>(B + (int64_t)__ldg(&colidx[q]) * 64) + l8 * 4;
-#pragma unroll
-                for (int u = 0; u < 4; u++) b[h][u] = __ldg(brow + u);
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; u++) b[h][u] = make_double2(0.0, 0.0);
-            }
+        for (int u = 0; u < 8; u++) {
+            a[u] = __ldg(arow + u);
+            b[u] = __ldg(brow + u);
         }
+    } else {
 #pragma unroll
-        for (int h = 0; h < SDDMM_GROUPS; h++) {
-            s[h] = 0.0;
-#pragma unroll
-            for (int u = 0; u < 4; u++) s[h] = fma(a[u].y, b[h][u].y, fma(a[u].x, b[h][u].x, s[h]));
-        }
-#pragma unroll
-        for (int h = 0; h < SDDMM_GROUPS; h++) {
-            for (int off = 4; off; off >>= 1) s[h] += __shfl_xor_sync(0xffffffffu, s[h], off);
-            const int q = qb + 4 * h + g;
-            if (q < q1 && l8 == 0) out[q] = s[h];
-        }
+        for (int u = 0; u < 8; u++) a[u] = b[u] = make_double2(0.0, 0.0);
     }
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; u += 2) {
+        s0 = fma(a[u].y, b[u].y, fma(a[u].x, b[u].x, s0));
+        s1 = fma(a[u + 1].y, b[u + 1].y, fma(a[u + 1].x, b[u + 1].x, s1));
+    }
+    double s = s0 + s1;
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    if (q < nnz && l4 == 0) out[q] = s;
 }
 
 // ------------------------------------------------------------------ structure
@@ -796,6 +784,18 @@ fail:
     return rc;
 }
 
+// Row of each nonzero, cached in the handle.
+static int ensure_rowidx(f4j_ctx* ctx, f4j_csr S) {
+    if (S->rowidx || S->nnz == 0) return F4J_OK;
+    int* ri = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)S->nnz * 4, (void**)&ri);
+    if (rc) return rc;
+    k_expand_rows<<<grid1(S->rows * 32), 256, 0, ctx->stream>>>(S->rows, (const int*)S->rowptr->ptr, ri);
+    F4J_LAUNCHED(ctx);
+    S->rowidx = ri;
+    return F4J_OK;
+}
+
 static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp, const int* ci, const double* v,
                        const int* perm, const double* X, double* Y, bool fused = false) {
     if (rows == 0 || ncols == 0) return F4J_OK;
@@ -883,7 +883,7 @@ extern "C" int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nn
             return f4j_fail(F4J_ERR_CSR, "rowIndices specifies %lld elements but nnz=%lld. These values must be equal.",
                             (long long)((int64_t)first_last[1] - first_last[0]), (long long)nnz);
     }
-    *out = new f4j_csr_s{rows, cols, nnz, rowptr, colidx, vals, false, nullptr, nullptr, nullptr};
+    *out = new f4j_csr_s{rows, cols, nnz, rowptr, colidx, vals, false, nullptr, nullptr, nullptr, nullptr};
     return F4J_OK;
 }
 
@@ -894,6 +894,7 @@ extern "C" int f4j_csr_free(f4j_ctx* ctx, f4j_csr S) {
     cudaFree(S->t_rowptr);
     cudaFree(S->t_perm);
     cudaFree(S->t_rowidx);
+    cudaFree(S->rowidx);
     if (S->owns) {
         f4j_buf_free(ctx, S->rowptr);
         f4j_buf_free(ctx, S->colidx);
@@ -930,7 +931,7 @@ static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz
         f4j_buf_free(ctx, v);
         return rc;
     }
-    *out = new f4j_csr_s{rows, cols, nnz, rp, ci, v, true, nullptr, nullptr, nullptr};
+    *out = new f4j_csr_s{rows, cols, nnz, rp, ci, v, true, nullptr, nullptr, nullptr, nullptr};
     return F4J_OK;
 }
 
@@ -1415,11 +1416,13 @@ extern "C" int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t 
     int64_t l0 = ctx->launches;
     if (S->rows && S->nnz) {
         f4j_prof_begin(ctx);
-        if (ncols == 64 && ((reinterpret_cast<uintptr_t>(A->ptr) | reinterpret_cast<uintptr_t>(B->ptr)) & 15) == 0)
-            k_sddmm64<<<(unsigned)f4j_cdiv(S->rows * 32, 256), 256, 0, ctx->stream>>>(
-                S->rows, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)A->ptr,
+        if (ncols == 64 && ((reinterpret_cast<uintptr_t>(A->ptr) | reinterpret_cast<uintptr_t>(B->ptr)) & 15) == 0) {
+            int rc = ensure_rowidx(ctx, S);
+            if (rc) return rc;
+            k_sddmm64f<<<(unsigned)f4j_cdiv(S->nnz * 4, 256), 256, 0, ctx->stream>>>(
+                S->nnz, (const int*)S->rowidx, (const int*)S->colidx->ptr, (const double*)A->ptr,
                 (const double*)B->ptr, (double*)out->ptr);
-        else
+        } else
             k_sddmm<<<(unsigned)f4j_cdiv(S->rows * 32, 256), 256, 0, ctx->stream>>>(
                 S->rows, ncols, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)A->ptr,
                 (const double*)B->ptr, (double*)out->ptr);
