@@ -9,7 +9,9 @@ line carries the plain DMMA path, errors against the double-double check for
 phi in {0, 8, 32}, the Complex128 4096^3 product, CSR SpMV/SpMM GB/s at 2^20
 rows (Poisson(16) row lengths), the dense adjoint step ratio, the roofline of
 the slice GEMM kernel, the CPU baseline and an end-to-end number through the
-host-buffer API (host<->device copies inside the timed region).
+host-buffer API (host<->device copies inside the timed region).  After all GPU
+timing, the oracle's restatements of the reference's loops are timed on this
+host beside the sparse, complex and adjoint rows (their cpu_baseline keys).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --case small        # 2048^3 / 2^16-row variant (profiling)
@@ -290,6 +292,38 @@ def cpu_baseline(n, k, seconds_target=15.0):
                       "(gcc -O3 -ffp-contract=off), %d pthreads, %.1f s" % (rows, n, n, threads, dt)}
 
 
+def dense_cpu_baselines(nz, ma, ka, seconds=1.5):
+    """Complex nz^3 (DenseSemiringMatMult over Complex128) and the C4 adjoint step
+    (A B forward; W.multTranspose(B) and A.T().mult(W) backward) as the oracle's
+    restatements of the reference's loops, on all host cores, each over a row
+    sample of about `seconds` scaled to the full product by rows."""
+    from oracle import oracle as O
+    from flag4j_gb300 import synth
+    O.build()
+    threads = os.cpu_count() or 1
+
+    def sampled(fn, full_rows):
+        r = threads
+        t = _wall(lambda: fn(r))
+        r = min(full_rows, max(threads, int(r * seconds / max(t, 1e-4)) // threads * threads))
+        t = _wall(lambda: fn(r))
+        return t * full_rows / r, r
+
+    Bz = synth.scaled(nz, nz, 8, 4, "col", cplx=True)
+    tz, rz = sampled(lambda r: O.zgemm(synth.scaled(r, nz, 8, 3, "row", cplx=True), Bz, threads=threads), nz)
+    del Bz
+    A, B, W = synth.normal(ma, ka, 5), synth.normal(ka, ma, 6), synth.normal(ma, ma, 7)
+    tf, rf = sampled(lambda r: O.dgemm(A[:r], B, threads=threads), ma)
+    ta, ra = sampled(lambda r: O.dgemm_abt(W[:r], B, threads=threads), ma)
+    At = np.ascontiguousarray(A.T)
+    tb, rb = sampled(lambda r: O.dgemm(At[:r], W, threads=threads), ka)
+    return {"complex": {"value": 8.0 * nz ** 3 / tz / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                        "sample": "%d of %d rows, scaled" % (rz, nz)},
+            "adjoint": {"forward_ms": 1e3 * tf, "fwd_bwd_ms": 1e3 * (tf + ta + tb), "ratio": (tf + ta + tb) / tf,
+                        "cores": threads, "kind": "port",
+                        "sample": "row samples of A B (%d rows), W B^T (%d rows), A^T W (%d rows), scaled" % (rf, ra, rb)}}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -334,9 +368,66 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- sparse products
-def sparse_section(E, full, steps=20):
+def _wall(fn):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
+def sparse_cpu_baselines(rp, ci, v, g):
+    """The oracle's restatements of the reference's sparse loops on this host,
+    single-threaded as Flag4j runs them (RealCsrDenseMatMult, CooMatrix.toCsr,
+    CooDataSorter, RealCsrOps.transpose + standard, RealCsrMatMult), each on a
+    bounded sample of the bench's own workload and scaled to it as stated."""
+    from oracle import oracle as O
+    from flag4j_gb300 import synth
+    O.build()
+    rows, nnz = len(rp) - 1, len(v)
+    out = {"kind": "port", "cores": 1}
+    x = synth.normal(rows, 1, 5).ravel()
+    t = _wall(lambda: O.spmv(rp, ci, v, x))
+    out["spmv_ms"] = 1e3 * t
+    # row samples: the first r rows, all of X (their columns span the whole range)
+    r = max(1, rows // 16)
+    rps, q = rp[:r + 1], int(rp[r])
+    X = synth.normal(rows, 32, 6)
+    t = _wall(lambda: O.spmm(rps, ci[:q], v[:q], X))
+    out["spmm_ms"] = 1e3 * t * nnz / max(q, 1)
+    del X
+    X64 = synth.normal(rows, 64, 8)
+    dC64 = synth.normal(rows, 64, 9)
+    t = _wall(lambda: O.sddmm(rps, ci[:q], dC64, X64))
+    out["sddmm64_ms"] = 1e3 * t * nnz / max(q, 1)
+    # S^T dC as the reference does it: S.T() then standard(S^T, dC)
+    t1 = _wall(lambda: O.csr_transpose(rows, rows, rp, ci, v))
+    trp, tci, tv, _ = O.csr_transpose(rows, rows, rp, ci, v)
+    qt = int(trp[r])
+    t2 = _wall(lambda: O.spmm(trp[:r + 1], tci[:qt], tv[:qt], dC64))
+    out["spmm_t64_ms"] = 1e3 * (t1 + t2 * nnz / max(qt, 1))
+    del X64, dC64
+    rs, cs, vs = synth.coo_shuffled(rp, ci, v, seed=7)
+    m = min(nnz, 1 << 20)
+    t = _wall(lambda: O.coo_sort(rs[:m], cs[:m], vs[:m]))
+    out["coo_sort_ms"] = 1e3 * t * (nnz * math.log2(nnz)) / (m * math.log2(max(m, 2)))
+    rsorted = np.repeat(np.arange(rows, dtype=np.int32), np.diff(rp))
+    out["coo_to_csr_ms"] = 1e3 * _wall(lambda: O.coo_to_csr(rows, rsorted))
+    grp, gci, gv = g
+    gr = max(1, (len(grp) - 1) // 8)
+    gq = int(grp[gr])
+    t = _wall(lambda: O.spgemm_csr(grp[:gr + 1], gci[:gq], gv[:gq], grp, gci, gv, len(grp) - 1))
+    products = int(np.diff(grp)[gci].sum())
+    products_s = int(np.diff(grp)[gci[:gq]].sum())
+    out["spgemm_csr_ms"] = 1e3 * t * products / max(products_s, 1)
+    out["sample"] = ("SpMV and COO -> CSR on the whole matrix; SpMM, SDDMM, S^T dC and CSR x CSR on the first "
+                     "1/16 (1/8 for CSR x CSR) of the rows, scaled by nonzeros (products); COO sort on 2^20 of the "
+                     "shuffled triplets, scaled by n log n; S^T dC includes the full transpose")
+    return out
+
+
+def sparse_section(E, full, steps=20, cpu=False):
     """CSR SpMV / SpMM (32 and 64 columns), S^T dC and SDDMM (64 columns), COO sort and COO -> CSR,
-    at 2^20 rows with Poisson(16) row lengths."""
+    at 2^20 rows with Poisson(16) row lengths; CSR x CSR into CSR at rows / 4.  With cpu, the
+    oracle's single-threaded restatements timed beside each (cpu_baseline)."""
     from flag4j_gb300 import synth
     rows = (1 << 20) if full else (1 << 16)
     rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
@@ -443,7 +534,24 @@ def sparse_section(E, full, steps=20):
                          "ms": t_spgemm, "gproducts_per_s": products / t_spgemm / 1e6,
                          "note": "includes the result's device allocation and two host reads of sizes"}
     del G
+    if cpu:
+        attach_sparse_cpu(res, full)
     return res
+
+
+def attach_sparse_cpu(res, full):
+    """Adds the single-threaded CPU baselines beside the sparse section's GPU times
+    (inputs regenerated from the same seeds)."""
+    from flag4j_gb300 import synth
+    rows = (1 << 20) if full else (1 << 16)
+    rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
+    g = synth.csr_poisson(rows // 4, rows // 4, lam=8.0, seed=77)
+    cb = sparse_cpu_baselines(rp, ci, v, g)
+    gpu_ms = {"spmv_ms": res["spmv_ms"], "spmm_ms": res["spmm_ms"], "sddmm64_ms": res["sddmm64_ms"],
+              "spmm_t64_ms": res["spmm_t64_ms"], "coo_sort_ms": res["coo_sort_ms"],
+              "coo_to_csr_ms": res["coo_to_csr_ms"], "spgemm_csr_ms": res["spgemm_csr"]["ms"]}
+    cb["gpu_speedup"] = {k: cb[k] / gpu_ms[k] for k in gpu_ms}
+    res["cpu_baseline"] = cb
 
 
 def run_sparse_only(args):
@@ -451,7 +559,7 @@ def run_sparse_only(args):
     from flag4j_gb300 import build
     build.build()
     E = Eng(dist_env()[2])
-    print(json.dumps(sparse_section(E, args.case == "full", steps=args.steps)))
+    print(json.dumps(sparse_section(E, args.case == "full", steps=args.steps, cpu=True)))
 
 
 # ---------------------------------------------------------------- our arm
@@ -607,6 +715,12 @@ def run_ours(args):
         from oracle import oracle as O
         O.build()
         cb = cpu_baseline(n, n, seconds_target=15.0 if full else 3.0)
+        # CPU baselines of the other rows, after every GPU measurement
+        if not args.skip_extras:
+            attach_sparse_cpu(out["spmm"], full)
+            dcb = dense_cpu_baselines(n // 2, n // 2, n // 4)
+            out["complex"]["cpu_baseline"] = dcb["complex"]
+            out["adjoint"]["cpu_baseline"] = dcb["adjoint"]
 
     dist.close()
     if rank != 0:
