@@ -94,6 +94,14 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
         cudaEventDestroy(ctx->ev_fork);
         cudaEventDestroy(ctx->ev_join);
     }
+    if (ctx->parts_init) {
+        for (int i = 0; i < F4J_HOST_PARTS_MAX; i++) {
+            cudaStreamSynchronize(ctx->part_stream[i]);
+            cudaStreamDestroy(ctx->part_stream[i]);
+            cudaEventDestroy(ctx->part_ev[i]);
+        }
+        cudaEventDestroy(ctx->ev_prep);
+    }
     for (int i = 0; i < 8; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
     if (ctx->d_status) cudaFree(ctx->d_status);

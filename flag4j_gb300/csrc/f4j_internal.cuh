@@ -31,16 +31,27 @@ struct f4j_csr_s {
     void* rowidx;
 };
 
+// Row parts of a host-buffer GEMM (C's download overlaps the later parts'
+// products): F4J_HOST_PARTS by default, up to F4J_HOST_PARTS_MAX through the
+// F4J_HOST_PARTS environment variable.
+#define F4J_HOST_PARTS 4
+#define F4J_HOST_PARTS_MAX 8
+
 struct f4j_ctx {
     int device;
     int sm_count;
     cudaStream_t stream;
     bool own_stream;
     void* ws[8];       // grow-only workspaces (slot ws_base + 0: split bulk, ws_base + 1: split
-    size_t ws_bytes[8];  // small/stats; 2-3: sparse; 4-5: the second product of an adjoint)
+    size_t ws_bytes[8];  // small/stats; 2: sparse; 4-5: the second product of an adjoint;
+                         // 3, 6, 7: A, B, C of f4j_dgemm_host)
     int ws_base;       // first split workspace slot (0, or 4 while an adjoint's second product is queued)
     cudaStream_t aux_stream;  // second stream of an adjoint (created on first use)
     cudaEvent_t ev_fork, ev_join;
+    // Streams of the row parts of a host-buffer GEMM (f4j_dgemm_host), created on first use.
+    cudaStream_t part_stream[F4J_HOST_PARTS_MAX];
+    cudaEvent_t part_ev[F4J_HOST_PARTS_MAX], ev_prep;
+    bool parts_init;
     int* d_status;     // device status words (bounded-wait timeouts, validation)
     cudaEvent_t ev[16];
     bool ev_init[16];

@@ -127,6 +127,7 @@ struct SplitGemmParams {
     double* C;
     int* status;
     const SplitPlan* plan;
+    int tm0, tm1;           // the launch covers tile rows [tm0, tm1) of C
 };
 
 // ------------------------------------------------------------------ stats
@@ -560,7 +561,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int nrounds = plan->nrounds;
     // persistent: CTA b takes tiles b, b + grid, ...; see tile_origin for the order
-    const int tiles_n = (p.N + BN - 1) / BN, tiles_m = (p.M + BM - 1) / BM;
+    const int tiles_n = (p.N + BN - 1) / BN, tiles_m = p.tm1 - p.tm0;
     const int ntiles = tiles_n * tiles_m;
 
     const int ngroups = plan->ngroups;
@@ -639,6 +640,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
                 int m0, n0;
                 tile_origin(tile, tiles_m, tiles_n, m0, n0);
+        m0 += p.tm0 * BM;
                 for (int kc = 0; kc < nkb && ok; kc += kcb) {
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
                     for (int g = 0; g < ngroups && ok; g++) {
@@ -769,6 +771,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         int m0, n0;
         tile_origin(tile, tiles_m, tiles_n, m0, n0);
+        m0 += p.tm0 * BM;
         const int row = m0 + 32 * q + lane;
         long long acc[EPI_COLS];
 #pragma unroll
@@ -883,6 +886,12 @@ static int env_slices() {
 }
 
 // Levels per band in the slice GEMM's schedule (F4J_SPLIT_BAND, 1..4; default 4).
+static int env_host_parts() {
+    const char* e = getenv("F4J_HOST_PARTS");
+    const int v = e ? atoi(e) : F4J_HOST_PARTS;
+    return v < 1 ? 1 : (v > F4J_HOST_PARTS_MAX ? F4J_HOST_PARTS_MAX : v);
+}
+
 static int env_band() {
     const char* env = getenv("F4J_SPLIT_BAND");
     const int b = env ? atoi(env) : 0;
@@ -896,9 +905,17 @@ static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 // receives the device flag that is non-zero when the plan stood down (NaN/Inf
 // input); the caller then runs the gated plain kernel.  With a report the
 // call waits for the plan to fill in slices / spread.
-int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
-                   const double* B, int opB, double* C, int slices_req, f4j_report* rep, const int** gate) {
-    *gate = nullptr;
+// Everything of one split GEMM but the slice GEMM launch: statistics, plan,
+// slicing, tensor maps and kernel parameters (the launch covers all tile rows
+// until split_launch narrows it).
+struct SplitLaunch {
+    CUtensorMap ta, tb;
+    SplitGemmParams prm;
+    int tiles_m, tiles_n;
+};
+
+static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                         const double* B, int opB, double* C, int slices_req, SplitLaunch* L) {
     const int64_t M = m, N = cplx ? 2 * n : n;
     const int64_t Kh = f4j_cdiv(k, BKB) * BKB;  // K of one real part, padded to whole stages
     const int64_t Kp = cplx ? 2 * Kh : Kh;      // cat K: [re | im], zero padded in between
@@ -975,13 +992,13 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     }
     f4j_prof_end(ctx);
 
-    CUtensorMap ta{}, tb{};
-    rc = make_slice_map(&ta, slA, Kp, M, S_MAX);
+    rc = make_slice_map(&L->ta, slA, Kp, M, S_MAX);
     if (rc) return rc;
-    rc = make_slice_map(&tb, slB, Kp, N, S_MAX);
+    rc = make_slice_map(&L->tb, slB, Kp, N, S_MAX);
     if (rc) return rc;
 
-    SplitGemmParams prm{};
+    SplitGemmParams& prm = L->prm;
+    prm = SplitGemmParams{};
     prm.M = (int)M;
     prm.N = (int)N;
     prm.Kp = (int)Kp;
@@ -992,15 +1009,29 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
     prm.C = C;
     prm.status = ctx->d_status + F4J_ST_TIMEOUT;
     prm.plan = plan;
+    prm.tm0 = 0;
+    prm.tm1 = (int)f4j_cdiv(M, BM);
+    L->tiles_m = prm.tm1;
+    L->tiles_n = (int)f4j_cdiv(N, BN);
+    return F4J_OK;
+}
 
+// The slice GEMM over tile rows [tm0, tm1) of C on `stream`.
+static int split_launch(f4j_ctx* ctx, const SplitLaunch& L, cudaStream_t stream, int tm0, int tm1) {
+    SplitGemmParams prm = L.prm;
+    prm.tm0 = tm0;
+    prm.tm1 = tm1;
     const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
-    const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);
+    const int64_t ntiles = (int64_t)L.tiles_n * (tm1 - tm0);
     const unsigned grid = (unsigned)(ntiles < ctx->sm_count ? ntiles : ctx->sm_count);
+    const cudaStream_t saved = ctx->stream;
+    ctx->stream = stream;
     f4j_prof_begin(ctx);
-    k_split_gemm<<<grid, GEMM_THREADS, smem, ctx->stream>>>(ta, tb, prm);
+    k_split_gemm<<<grid, GEMM_THREADS, smem, stream>>>(L.ta, L.tb, prm);
     f4j_prof_end(ctx);
+    ctx->stream = saved;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         cudaFuncAttributes fa{};
@@ -1012,20 +1043,128 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
                         fa.localSizeBytes, fa.maxDynamicSharedSizeBytes, smem, sizeof(SplitGemmParams));
     }
     ctx->launches++;
-    *gate = &plan->nonfinite;
-
-    if (rep) {
-        int hp[5];
-        F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, ctx->stream));
-        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-        float spread;
-        memcpy(&spread, &hp[4], 4);
-        rep->slices = hp[0];
-        rep->frac_bits = 4 + 5 * (hp[0] - 1);
-        rep->exp_spread = spread;
-        if (hp[3]) rep->slices = 0;
-    }
     return F4J_OK;
+}
+
+// Plan header (s, nrounds, ubits, nonfinite, spread) into a report.
+static int split_report(f4j_ctx* ctx, const SplitPlan* plan, f4j_report* rep) {
+    int hp[5];
+    F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, ctx->stream));
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    float spread;
+    memcpy(&spread, &hp[4], 4);
+    rep->slices = hp[0];
+    rep->frac_bits = 4 + 5 * (hp[0] - 1);
+    rep->exp_spread = spread;
+    if (hp[3]) rep->slices = 0;
+    return F4J_OK;
+}
+
+int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                   const double* B, int opB, double* C, int slices_req, f4j_report* rep, const int** gate) {
+    *gate = nullptr;
+    SplitLaunch L;
+    int rc = split_prepare(ctx, cplx, m, n, k, A, opA, B, opB, C, slices_req, &L);
+    if (rc) return rc;
+    rc = split_launch(ctx, L, ctx->stream, 0, L.tiles_m);
+    if (rc) return rc;
+    *gate = &L.prm.plan->nonfinite;
+    if (rep) return split_report(ctx, L.prm.plan, rep);
+    return F4J_OK;
+}
+
+// ------------------------------------------------------------------ host buffers
+// C = op(A) op(B) from and to host memory (pinned for full copy speed).  For
+// a split product with op(A) = N and at least two tile rows, the slice GEMM
+// runs as F4J_HOST_PARTS launches over row parts of C on their own streams,
+// each followed by its part's gated DMMA fallback and download, so C's
+// download overlaps the later parts' products and each launch's CTAs fill the
+// previous launch's last wave.  Other products upload, multiply and download
+// in turn.  Returns when C is in host memory.
+extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                              const double* B, int opB, double* C, int mode, f4j_report* rep) {
+    F4J_CHECK_CTX(ctx);
+    if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null host pointer");
+    if (m < 0 || n < 0 || k < 0) return f4j_fail(F4J_ERR_ARG, "negative dimension");
+    if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX)
+        return f4j_fail(F4J_ERR_ARG, "dimension exceeds Flag4j's int range");
+    if (opA < F4J_OP_N || opA > F4J_OP_C || opB < F4J_OP_N || opB > F4J_OP_C) return f4j_fail(F4J_ERR_ARG, "bad op");
+    if (mode < F4J_MODE_PLAIN || mode > F4J_MODE_EXACT) return f4j_fail(F4J_ERR_ARG, "bad mode %d", mode);
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    if (rep) *rep = f4j_report{};
+    if (m == 0 || n == 0) return F4J_OK;
+    if (opA == F4J_OP_C) opA = F4J_OP_T;  // real data
+    if (opB == F4J_OP_C) opB = F4J_OP_T;
+    const size_t ab = (size_t)m * k * 8, bb = (size_t)k * n * 8, cb = (size_t)m * n * 8;
+    void *dA, *dB, *dC;
+    int rc = f4j_workspace(ctx, 3, ab, &dA);
+    if (!rc) rc = f4j_workspace(ctx, 6, bb, &dB);
+    if (!rc) rc = f4j_workspace(ctx, 7, cb, &dC);
+    if (rc) return rc;
+    if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
+    if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
+    const double work = 2.0 * (double)m * (double)n * (double)k;
+    const bool split = k > 0 && (mode == F4J_MODE_SPLIT || (mode == F4J_MODE_AUTO && work > (double)(1 << 24)));
+    const int tiles_m = (int)f4j_cdiv(m, BM);
+    const int want = env_host_parts();
+    const int parts = tiles_m < want ? tiles_m : want;
+    if (!split || opA != F4J_OP_N || parts < 2) {
+        rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,
+                           rep);
+        if (rc) return rc;
+        F4J_CUDA(cudaMemcpyAsync(C, dC, cb, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        return F4J_OK;
+    }
+    const int64_t l0 = ctx->launches;
+    SplitLaunch L;
+    rc = split_prepare(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, 0, &L);
+    if (rc) return rc;
+    if (!ctx->parts_init) {
+        for (int i = 0; i < F4J_HOST_PARTS_MAX; i++) {
+            F4J_CUDA(cudaStreamCreateWithFlags(&ctx->part_stream[i], cudaStreamNonBlocking));
+            F4J_CUDA(cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming));
+        }
+        F4J_CUDA(cudaEventCreateWithFlags(&ctx->ev_prep, cudaEventDisableTiming));
+        ctx->parts_init = true;
+    }
+    F4J_CUDA(cudaEventRecord(ctx->ev_prep, ctx->stream));
+    const int* gate = &L.prm.plan->nonfinite;
+    int launched = 0;
+    for (int p = 0; p < parts && !rc; p++) {
+        const int tm0 = (int)((int64_t)tiles_m * p / parts), tm1 = (int)((int64_t)tiles_m * (p + 1) / parts);
+        const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
+        const cudaStream_t st = ctx->part_stream[p];
+        F4J_CUDA(cudaStreamWaitEvent(st, ctx->ev_prep, 0));
+        launched = p + 1;
+        rc = split_launch(ctx, L, st, tm0, tm1);
+        if (!rc) {
+            const cudaStream_t saved = ctx->stream;
+            ctx->stream = st;
+            rc = f4j_gemm_dmma(ctx, false, r1 - r0, n, k, (const double*)dA + r0 * k, F4J_OP_N, (const double*)dB,
+                               opB, (double*)dC + r0 * n, gate);
+            ctx->stream = saved;
+        }
+        if (!rc) {
+            F4J_CUDA(cudaMemcpyAsync(C + r0 * n, (const double*)dC + r0 * n, (size_t)(r1 - r0) * n * 8,
+                                     cudaMemcpyDeviceToHost, st));
+            F4J_CUDA(cudaEventRecord(ctx->part_ev[p], st));
+            F4J_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->part_ev[p], 0));
+        }
+    }
+    if (rc) {
+        for (int p = 0; p < launched; p++) cudaStreamSynchronize(ctx->part_stream[p]);
+        return rc;
+    }
+    if (rep) {
+        rep->flops = work;
+        rep->mode_used = F4J_MODE_SPLIT;
+        rc = split_report(ctx, L.prm.plan, rep);
+        if (rep->slices == 0) rep->mode_used = F4J_MODE_PLAIN;
+        rep->launches = (int32_t)(ctx->launches - l0);
+    }
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    return rc;
 }
 
 // ------------------------------------------------------------------ no-allocation variant
@@ -1154,6 +1293,8 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.C = C;
     prm.status = misc + 8;
     prm.plan = plan;
+    prm.tm0 = 0;
+    prm.tm1 = (int)f4j_cdiv(M, BM);
     const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);

@@ -130,6 +130,15 @@ int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out);
  * A is stored m x k (opA N) or k x m (opA T); B k x n (N) or n x k (T). */
 int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA, f4j_buf B,
               int opB, f4j_buf C, int mode, f4j_report* report);
+/* f4j_dgemm from and to host memory: A, B, C are host pointers (row-major,
+ * pinned with f4j_host_register for full copy speed; pageable works), and the
+ * call returns when C is in host memory.  A split product with opA = N runs
+ * as row parts of C on their own streams so that C's download overlaps the
+ * later parts' products; the result is bitwise the f4j_dgemm result.  This is
+ * the entry a JVM binding calls with its arrays' native copies; Flag4j's
+ * Matrix.mult(Matrix) has the same arguments and result. */
+int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
+                   int opB, double* C, int mode, f4j_report* report);
 
 /* Complex128 C = op(A) * op(B), interleaved (re, im); op may be N, T or C.
  * Replaces CMatrix.mult -> Cm128DeMatMultDispatcher.dispatch

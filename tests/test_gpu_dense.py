@@ -383,3 +383,63 @@ def test_wrap_rejects_misaligned_and_null(f4j):
         check(ctx.lib.f4j_buf_wrap(ctx.handle, ctypes.c_void_p(buf.ctypes.data + 8), 64, ctypes.byref(h)))
     with pytest.raises(IllegalArgumentException):
         check(ctx.lib.f4j_buf_wrap(ctx.handle, None, 64, ctypes.byref(h)))
+
+
+@pytest.mark.parametrize("m,n,k,mode,opA,pinned", [
+    (1000, 700, 900, "split", 0, True),     # 8 tile rows: four row parts
+    (300, 260, 520, "split", 0, False),     # 3 tile rows: three parts, pageable host memory
+    (130, 200, 300, "split", 0, True),      # 2 tile rows, the last ragged
+    (100, 90, 80, "split", 0, True),        # one tile row: no parts
+    (600, 500, 400, "split", 1, True),      # op(A) = T: uploaded, multiplied, downloaded in turn
+    (500, 300, 200, "plain", 0, True),
+    (64, 48, 40, "exact", 0, True),
+])
+def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, pinned):
+    """f4j_dgemm_host is bitwise f4j_dgemm on the same operands."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    A = synth.scaled(m, k, 4, 21, "row") if opA == 0 else synth.scaled(k, m, 4, 21, "col")
+    B = synth.scaled(k, n, 4, 22, "col")
+    dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(8 * m * n)
+    check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, 0, dC.handle, _lib.MODES[mode], None))
+    ref = dC.to_numpy(np.float64, m * n).reshape(m, n)
+    C = np.full((m, n), np.nan)
+    arrays = (A, B, C)
+    if pinned:
+        for a in arrays:
+            check(ctx.lib.f4j_host_register(a.ctypes.data, a.nbytes))
+    try:
+        rep = _lib.f4j_report()
+        check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, opA, B.ctypes.data, 0, C.ctypes.data,
+                                     _lib.MODES[mode], ctypes.byref(rep)))
+        assert np.array_equal(C, ref)
+        if mode == "split":
+            assert rep.slices > 0 and rep.mode_used == _lib.MODE_SPLIT
+    finally:
+        if pinned:
+            for a in arrays:
+                check(ctx.lib.f4j_host_unregister(a.ctypes.data))
+
+
+def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
+    """NaN / Inf in A: every row part falls back to DMMA, which propagates them
+    like the reference; finite rows stay within the bound."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    m, n, k = 700, 300, 256
+    A = synth.normal(m, k, 31)
+    B = synth.normal(k, n, 32)
+    A[5, 7] = np.nan
+    A[650, 3] = np.inf
+    C = np.zeros((m, n))
+    rep = _lib.f4j_report()
+    check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, 0, B.ctypes.data, 0, C.ctypes.data,
+                                 _lib.MODE_SPLIT, ctypes.byref(rep)))
+    assert rep.slices == 0 and rep.mode_used == _lib.MODE_PLAIN
+    assert np.isnan(C[5]).all() and not np.isfinite(C[650]).any()
+    fin = np.isfinite(A).all(axis=1)
+    ref = oracle.dgemm(A[fin], B)
+    bound = 2 * k * U * oracle.absgemm(A[fin], B)
+    assert np.all(np.abs(C[fin] - ref) <= bound)
