@@ -634,6 +634,16 @@ def run_ours(args):
             del Ap, Bp
         out["errors_by_phi"] = errs
         del A, B
+        # ---- matrix-vector product n x n (Matrix.mult(Vector) in AUTO mode: one FP64 FMA dot product per
+        # row, A read once; A is 512 MiB at 8192, larger than L2)
+        Av, xv, yv = E.dev(synth.normal(n, n, 51)), E.dev(synth.normal(n, 1, 52)), E.ctx.alloc(8 * n)
+        mrep = E.gemm(Av, xv, yv, n, 1, n, L.MODE_AUTO, report=True)
+        t_mv = E.timed(lambda: E.gemm(Av, xv, yv, n, 1, n, L.MODE_AUTO), 20, 3)
+        hbm_peak, _ = measured_peaks()
+        out["matvec"] = {"n": n, "ms": t_mv, "gbs": 8.0 * n * n / t_mv / 1e6,
+                         "frac_hbm": 8.0 * n * n / t_mv / 1e6 / hbm_peak, "gflops": 2.0 * n * n / t_mv / 1e6,
+                         "mode_used": mrep.mode_used, "basis": "A's 8 n^2 bytes read once per product"}
+        del Av, xv, yv
         # ---- Complex128 n/2 ^3 (8mnk basis)
         nz = n // 2
         Az = synth.scaled(nz, nz, 8, 3, "row", cplx=True)

@@ -409,6 +409,11 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
         F4J_CUDA(cudaMemsetAsync(C, 0, (size_t)m * n * (cplx ? 16 : 8), ctx->stream));
     } else if (mode == F4J_MODE_EXACT) {
         rc = f4j_gemm_exact(ctx, cplx, m, n, k, A, opA, B, opB, C);
+    } else if (n == 1) {
+        // a matrix-vector product: one FP64 FMA dot product per row reads A once,
+        // where slicing A and a GEMM with one column would waste the tiles
+        rc = f4j_gemv(ctx, cplx, m, k, A, opA, B, opB == F4J_OP_C, C);
+        used = F4J_MODE_PLAIN;
     } else if (mode == F4J_MODE_PLAIN) {
         rc = f4j_gemm_dmma(ctx, cplx, m, n, k, A, opA, B, opB, C);
     } else {

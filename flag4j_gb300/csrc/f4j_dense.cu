@@ -425,6 +425,92 @@ __global__ void k_gemm_check(int64_t m, int64_t n, int64_t k, const double* __re
     }
 }
 
+// ------------------------------------------------------------------ GEMV
+// y = op(A) x (n == 1) for the non-exact modes: FP64 FMA dot products, error
+// within k u |A||x| (the plain DMMA path's class).  W = 2 for interleaved
+// complex; sa / sx = -1 conjugate A / x (an exact sign flip).
+// op(A) = N: A stored m x k, a warp per row, lanes stride the row, warp sum.
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_gemv_rows(int64_t m, int64_t k, const double* __restrict__ A,
+                                                   const double* __restrict__ x, double sx, double* __restrict__ y) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= m) return;
+    double re = 0.0, im = 0.0;
+    if (!CPLX) {
+        const double* a = A + row * k;
+        double r1 = 0.0;
+        int64_t j = lane;
+        for (; j + 32 < k; j += 64) {
+            re = fma(__ldg(&a[j]), __ldg(&x[j]), re);
+            r1 = fma(__ldg(&a[j + 32]), __ldg(&x[j + 32]), r1);
+        }
+        if (j < k) re = fma(__ldg(&a[j]), __ldg(&x[j]), re);
+        re += r1;
+    } else {
+        const double2* a = reinterpret_cast<const double2*>(A) + row * k;
+        const double2* xv = reinterpret_cast<const double2*>(x);
+        for (int64_t j = lane; j < k; j += 32) {
+            const double2 av = __ldg(&a[j]), xx = __ldg(&xv[j]);
+            const double xi = sx * xx.y;
+            re = fma(av.x, xx.x, re);
+            re = fma(-av.y, xi, re);
+            im = fma(av.x, xi, im);
+            im = fma(av.y, xx.x, im);
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        if (CPLX) im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+        if (CPLX) {
+            y[2 * row] = re;
+            y[2 * row + 1] = im;
+        } else {
+            y[row] = re;
+        }
+    }
+}
+
+// op(A) = T / C: A stored k x m; a thread per output element and K chunk
+// (coalesced along the stored rows), partial sums part[chunk][m * W].
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_gemv_cols(int64_t m, int64_t k, int64_t kchunk, const double* __restrict__ A,
+                                                   double sa, const double* __restrict__ x, double sx,
+                                                   double* __restrict__ part) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int64_t k0 = (int64_t)blockIdx.y * kchunk, k1 = k0 + kchunk < k ? k0 + kchunk : k;
+    if (!CPLX) {
+        double s = 0.0;
+        for (int64_t kk = k0; kk < k1; kk++) s = fma(__ldg(&A[kk * m + i]), __ldg(&x[kk]), s);
+        part[blockIdx.y * m + i] = s;
+    } else {
+        const double2* a = reinterpret_cast<const double2*>(A);
+        const double2* xv = reinterpret_cast<const double2*>(x);
+        double re = 0.0, im = 0.0;
+        for (int64_t kk = k0; kk < k1; kk++) {
+            const double2 av = __ldg(&a[kk * m + i]), xx = __ldg(&xv[kk]);
+            const double ai = sa * av.y, xi = sx * xx.y;
+            re = fma(av.x, xx.x, re);
+            re = fma(-ai, xi, re);
+            im = fma(av.x, xi, im);
+            im = fma(ai, xx.x, im);
+        }
+        part[(blockIdx.y * m + i) * 2] = re;
+        part[(blockIdx.y * m + i) * 2 + 1] = im;
+    }
+}
+
+__global__ void k_gemv_sum(int64_t len, int64_t nchunk, const double* __restrict__ part, double* __restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    double s = 0.0;
+    for (int64_t c = 0; c < nchunk; c++) s += part[c * len + i];
+    y[i] = s;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host side
@@ -544,4 +630,40 @@ extern "C" int f4j_gemm_check(f4j_ctx* ctx, int cplx, int64_t m, int64_t n, int6
     memcpy(max_abs, &h[0], 8);
     memcpy(max_rel, &h[1], 8);
     return F4J_OK;
+}
+
+int f4j_gemv(f4j_ctx* ctx, bool cplx, int64_t m, int64_t k, const double* A, int opA, const double* x, bool conj_x,
+             double* y) {
+    const double sx = conj_x ? -1.0 : 1.0;
+    if (opA == F4J_OP_N) {
+        const unsigned blocks = (unsigned)f4j_cdiv(m * 32, 256);
+        f4j_prof_begin(ctx);
+        if (cplx) k_gemv_rows<true><<<blocks, 256, 0, ctx->stream>>>(m, k, A, x, sx, y);
+        else k_gemv_rows<false><<<blocks, 256, 0, ctx->stream>>>(m, k, A, x, sx, y);
+        f4j_prof_end(ctx);
+        F4J_LAUNCHED(ctx);
+        return F4J_OK;
+    }
+    // K split so that about 2048 threads per SM are busy; partials summed in chunk order
+    int64_t nchunk = f4j_cdiv((int64_t)ctx->sm_count * 2048, m);
+    if (nchunk > k) nchunk = k;
+    if (nchunk > 65535) nchunk = 65535;
+    if (nchunk < 1) nchunk = 1;
+    const int64_t kchunk = f4j_cdiv(k, nchunk);
+    nchunk = f4j_cdiv(k, kchunk);
+    const int64_t len = m * (cplx ? 2 : 1);
+    double* part = nullptr;
+    int rc = f4j_dev_alloc(ctx, (size_t)(nchunk * len) * 8, (void**)&part);
+    if (rc) return rc;
+    const double sa = (opA == F4J_OP_C) ? -1.0 : 1.0;
+    const dim3 grid((unsigned)f4j_cdiv(m, 256), (unsigned)nchunk);
+    f4j_prof_begin(ctx);
+    if (cplx) k_gemv_cols<true><<<grid, 256, 0, ctx->stream>>>(m, k, kchunk, A, sa, x, sx, part);
+    else k_gemv_cols<false><<<grid, 256, 0, ctx->stream>>>(m, k, kchunk, A, sa, x, sx, part);
+    k_gemv_sum<<<(unsigned)f4j_cdiv(len, 256), 256, 0, ctx->stream>>>(len, nchunk, part, y);
+    f4j_prof_end(ctx);
+    ctx->launches += 2;
+    f4j_dev_free(ctx, part);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? F4J_OK : f4j_cuda_fail(e, "gemv");
 }

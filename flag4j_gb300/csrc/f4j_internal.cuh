@@ -131,6 +131,10 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
                   const int** gate_out = nullptr);
 // `gate` (device int, may be null): the DMMA kernel computes only when *gate
 // is non-zero -- the split path's NaN/Inf fallback, decided on the device.
+// y = op(A) x with FP64 FMA dot products (n == 1 in the non-exact modes); x
+// conjugated when conj_x.  A, x, y interleaved when cplx.
+int f4j_gemv(f4j_ctx* ctx, bool cplx, int64_t m, int64_t k, const double* A, int opA, const double* x, bool conj_x,
+             double* y);
 int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                   int opA, const double* B, int opB, double* C, const int* gate = nullptr);
 int f4j_gemm_exact(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,

@@ -171,8 +171,52 @@ def test_fast_modes_within_bound(f4j, oracle, mode, m, n, k, cp):
         B = B + 1j * synth.normal(k, n, 14)
     C, rep = run_gemm(f4j, A, B, mode=mode)
     check_bound(C, *ref_bound(oracle, A, B, cp), k, mode)
-    if mode == "split":
+    if mode == "split" and n == 1:
+        # one column: the FP64 FMA matrix-vector product (plain arithmetic)
+        assert rep.mode_used == 0 and rep.slices == 0
+    elif mode == "split":
         assert rep.mode_used == 1 and 2 <= rep.slices <= 14
+
+
+@pytest.mark.parametrize("mode", ["plain", "split", "auto"])
+@pytest.mark.parametrize("opA", [0, 1, 2])
+@pytest.mark.parametrize("cp", [False, True])
+@pytest.mark.parametrize("m,k", [(1, 1), (37, 1001), (3000, 257), (5, 40000), (8192, 8192)])
+def test_matrix_vector_products(f4j, oracle, mode, opA, cp, m, k):
+    """Matrix.mult(Vector) and its transposed / conjugated forms in the fast
+    modes: one FP64 FMA dot product per row (warp per row for op(A) = N, a
+    K-split column pass for T / C), within 2 k u |A||x|."""
+    if opA == 2 and not cp:
+        pytest.skip("conjugation is the identity for real data")
+    from flag4j_gb300 import synth
+    rng = np.random.default_rng(m + k)
+    Ast = synth.normal(m, k, 41) if opA == 0 else synth.normal(k, m, 41)
+    x = rng.standard_normal((k, 1))
+    if cp:
+        Ast = Ast + 1j * (synth.normal(m, k, 42) if opA == 0 else synth.normal(k, m, 42))
+        x = x + 1j * rng.standard_normal((k, 1))
+    C, rep = run_gemm(f4j, Ast, x, opA=opA, mode=mode)
+    Aop = opx(Ast, opA)
+    ref, ab = ref_bound(oracle, np.ascontiguousarray(Aop), x, cp)
+    check_bound(C, ref, ab, k, "gemv")
+    if not (mode == "auto" and 2 * m * k * (4 if cp else 1) <= (1 << 24)):
+        assert rep.mode_used == 0
+
+
+def test_matrix_vector_conjugated_vector_and_nonfinite(f4j, oracle):
+    rng = np.random.default_rng(3)
+    m, k = 300, 500
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    xt = rng.standard_normal((1, k)) + 1j * rng.standard_normal((1, k))  # stored 1 x k, op C -> conj column
+    C, _ = run_gemm(f4j, A, xt, opB=2, mode="plain")
+    ref, ab = ref_bound(oracle, A, np.ascontiguousarray(xt.conj().T), True)
+    check_bound(C, ref, ab, k, "gemv conj x")
+    Ar = rng.standard_normal((m, k))
+    Ar[7, 3] = np.nan
+    Ar[9, 0] = np.inf
+    C, _ = run_gemm(f4j, Ar, rng.standard_normal((k, 1)), mode="split")
+    assert np.isnan(C[7, 0]) and not np.isfinite(C[9, 0])
+    assert np.isfinite(np.delete(C, [7, 9], axis=0)).all()
 
 
 @pytest.mark.parametrize("mode", ["exact", "plain", "split"])
