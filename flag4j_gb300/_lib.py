@@ -84,6 +84,8 @@ SIGNATURES = {
     "f4j_csr_transpose": (_i, [_v, _v, _pv]),
     "f4j_csr_mult_dense": (_i, [_v, _v, _v, _v, _rep]),
     "f4j_csr_mult_csr": (_i, [_v, _v, _v, _pv, _rep]),
+    "f4j_csr_mult_dense_ex": (_i, [_v, _v, _i, _v, _i, _v, _rep]),
+    "f4j_csr_mult_csr_ex": (_i, [_v, _v, _i, _v, _i, _pv, _rep]),
     "f4j_csr_transpose_perm": (_i, [_v, _v, _v]),
     "f4j_spmv": (_i, [_v, _v, _v, _v, _rep]),
     "f4j_spmv_ex": (_i, [_v, _v, _v, _v, _i, _rep]),

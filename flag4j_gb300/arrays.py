@@ -248,6 +248,14 @@ class CMatrix(_Dense):
     def H(self):
         return CMatrix(self.toNumpy().conj().T.copy())
 
+    def toCsr(self):
+        """CMatrix.toCsr: the nonzero entries in row-major order as a CsrCMatrix."""
+        a = self.toNumpy()
+        r, c = np.nonzero(a != 0)
+        rp = np.zeros(self.numRows + 1, np.int32)
+        np.cumsum(np.bincount(r, minlength=self.numRows), out=rp[1:])
+        return CsrCMatrix(self.shape, a[r, c], rp, c.astype(np.int32))
+
     def mult(self, b, mode=None, report=None):
         """CMatrix.mult(CMatrix / CVector / Matrix / Vector) on the GPU.
 
@@ -450,34 +458,48 @@ class CsrMatrix:
                                       ctypes.byref(rep)))
             out = (CVector._from_device(Shape(self.numRows), y, ctx) if vec
                    else CMatrix._from_device(Shape(self.numRows, nc), y, ctx))
-        elif isinstance(b, CsrMatrix) and not isinstance(b, CsrCMatrix):
-            # CsrMatrix.mult(CsrMatrix) -> RealCsrMatMult.standard (RealCsrMatMult.java:53-75): dense result
-            ensure_mat_mult_shapes(self.shape, b.shape)
-            ctx = self._ctx or b._ctx or default_context()
-            y = ctx.alloc(max(8 * self.numRows * b.numCols, 8))
-            check(ctx.lib.f4j_csr_mult_dense(ctx.handle, self.handle(ctx), b.handle(ctx), y.handle,
-                                             ctypes.byref(rep)))
-            out = Matrix._from_device(Shape(self.numRows, b.numCols), y, ctx)
+        elif isinstance(b, CsrMatrix):
+            out = self._csr_mult_dense(b, rep)
         else:
             raise NotImplementedError("CsrMatrix.mult(%s) is not on this engine's path" % type(b).__name__)
         if report is not None:
             report.update(rep.as_dict())
         return out
 
-    def mult2Csr(self, b):
-        """CsrMatrix.mult2Csr(CsrMatrix) -> RealCsrMatMult.standardAsSparse (RealCsrMatMult.java:92-131):
-        the product as CSR, every touched column stored (explicit zeros too), bit-identical."""
+    def _csr_mult_dense(self, b, rep=None):
+        """CSR x CSR with a dense result (RealCsrMatMult.standard, RealComplexCsrMatMult.standard,
+        SemiringCsrMatMult.standard by the operands' value types), bit-identical."""
         ensure_mat_mult_shapes(self.shape, b.shape)
+        ac, bc = isinstance(self, CsrCMatrix), isinstance(b, CsrCMatrix)
+        w = 2 if (ac or bc) else 1
+        ctx = self._ctx or b._ctx or default_context()
+        y = ctx.alloc(max(8 * w * self.numRows * b.numCols, 8))
+        check(ctx.lib.f4j_csr_mult_dense_ex(ctx.handle, self.handle(ctx), int(ac), b.handle(ctx), int(bc), y.handle,
+                                            ctypes.byref(rep) if rep is not None else None))
+        cls = CMatrix if w == 2 else Matrix
+        return cls._from_device(Shape(self.numRows, b.numCols), y, ctx)
+
+    def mult2Csr(self, b):
+        """CsrMatrix.mult2Csr(CsrMatrix | CsrCMatrix) -> RealCsrMatMult.standardAsSparse
+        (RealCsrMatMult.java:92-131) / RealComplexCsrMatMult.standardAsSparse (:133-181); for a
+        CsrCMatrix receiver its own variants: the product as CSR, every touched column stored (explicit
+        zeros too), bit-identical."""
+        if not isinstance(b, CsrMatrix):
+            raise NotImplementedError("mult2Csr(%s) is not on this engine's path" % type(b).__name__)
+        ensure_mat_mult_shapes(self.shape, b.shape)
+        ac, bc = isinstance(self, CsrCMatrix), isinstance(b, CsrCMatrix)
         ctx = self._ctx or b._ctx or default_context()
         h = ctypes.c_void_p()
-        check(ctx.lib.f4j_csr_mult_csr(ctx.handle, self.handle(ctx), b.handle(ctx), ctypes.byref(h), None))
+        check(ctx.lib.f4j_csr_mult_csr_ex(ctx.handle, self.handle(ctx), int(ac), b.handle(ctx), int(bc),
+                                          ctypes.byref(h), None))
         nnz = ctypes.c_int64()
         check(ctx.lib.f4j_csr_info(h, None, None, ctypes.byref(nnz)))
-        return CsrMatrix._from_handle((self.numRows, b.numCols), nnz.value, h, None, ctx)
+        cls = CsrCMatrix if (ac or bc) else CsrMatrix
+        return cls._from_handle((self.numRows, b.numCols), nnz.value, h, None, ctx)
 
     def multTranspose(self, b):
         """CsrMatrix.multTranspose(CsrMatrix) -> RealCsrMatMult.standard(this, b.T()) (CsrMatrix.java:809-810)."""
-        if not isinstance(b, CsrMatrix) or isinstance(b, CsrCMatrix):
+        if not isinstance(b, CsrMatrix) or isinstance(b, CsrCMatrix) or isinstance(self, CsrCMatrix):
             raise NotImplementedError("CsrMatrix.multTranspose(%s) is not on this engine's path" % type(b).__name__)
         ensure_mat_mult_shapes(self.shape, Shape(b.numCols, b.numRows))
         return self.mult(b.T())
@@ -538,6 +560,10 @@ class CsrCMatrix(CsrMatrix):
     def mult(self, b, report=None):
         """CsrCMatrix.mult(CMatrix / CVector) -> DenseCsrSemiringMatMult.standard / standardVector
         (DenseCsrSemiringMatMult.java:59-98, :140-160), bit-identical."""
+        if isinstance(b, CsrMatrix):
+            # CsrCMatrix.mult(CsrMatrix) -> RealComplexCsrMatMult.standard (RealComplexCsrMatMult.java:93-118);
+            # CsrCMatrix.mult(CsrCMatrix) -> SemiringCsrMatMult.standard (SemiringCsrMatMult.java:58-87)
+            return self._csr_mult_dense(b)
         if not isinstance(b, (CMatrix, CVector)):
             raise NotImplementedError("CsrCMatrix.mult(%s) is not on this engine's path" % type(b).__name__)
         vec = isinstance(b, CVector)

@@ -511,17 +511,19 @@ __global__ void k_coo_bucket(int64_t n, const int* __restrict__ r, const int* __
 // writes one sorted entry: row, column, and the value of its input index
 __device__ __forceinline__ void coo_emit(int64_t pos, int row, unsigned long long k, int* __restrict__ ro,
                                          int* __restrict__ co, const double* __restrict__ vin,
-                                         double* __restrict__ vo) {
+                                         double* __restrict__ vo, int* __restrict__ po) {
     ro[pos] = row;
     co[pos] = (int)(k >> 32);
     if (vo) vo[pos] = __ldg(&vin[(unsigned)k]);
+    if (po) po[pos] = (int)(unsigned)k;
 }
 
 // a warp per row; rows of up to 32 entries are ranked in registers (keys are
 // unique), longer ones are listed for k_coo_seg_block
 __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const unsigned long long* __restrict__ key,
                                int* __restrict__ ro, int* __restrict__ co, const double* __restrict__ vin,
-                               double* __restrict__ vo, int* __restrict__ longlist, int* __restrict__ nlong) {
+                               double* __restrict__ vo, int* __restrict__ po, int* __restrict__ longlist,
+                               int* __restrict__ nlong) {
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
     if (row >= rows) return;
@@ -533,7 +535,7 @@ __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const u
     const unsigned long long k = lane < len ? key[q0 + lane] : ~0ull;
     int rank = 0;
     for (int j = 0; j < len; j++) rank += __shfl_sync(0xffffffffu, k, j) < k;
-    if (lane < len) coo_emit(q0 + rank, (int)row, k, ro, co, vin, vo);
+    if (lane < len) coo_emit(q0 + rank, (int)row, k, ro, co, vin, vo, po);
 }
 
 // a block per listed row (33 .. pmax entries, pmax a power of two up to
@@ -542,7 +544,8 @@ __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ l
                                                        const int* __restrict__ rp,
                                                        const unsigned long long* __restrict__ key,
                                                        int* __restrict__ ro, int* __restrict__ co,
-                                                       const double* __restrict__ vin, double* __restrict__ vo) {
+                                                       const double* __restrict__ vin, double* __restrict__ vo,
+                                                       int* __restrict__ po) {
     extern __shared__ unsigned long long sk[];
     const int nl = *nlong;
     for (int b = blockIdx.x; b < nl; b += gridDim.x) {
@@ -567,7 +570,7 @@ __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ l
                 __syncthreads();
             }
         }
-        for (int i = threadIdx.x; i < len; i += blockDim.x) coo_emit(q0 + i, row, sk[i], ro, co, vin, vo);
+        for (int i = threadIdx.x; i < len; i += blockDim.x) coo_emit(q0 + i, row, sk[i], ro, co, vin, vo, po);
         __syncthreads();
     }
 }
@@ -579,21 +582,49 @@ __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ l
 // dense row i of C (zeroed), each product and sum rounded.  A row of B holds
 // distinct columns, so the lanes of one step touch distinct entries; the
 // __syncwarp orders successive steps.
+template <int AK, int BK>
+__device__ __forceinline__ double2 spgemm_prod(const double* __restrict__ av, int64_t q,
+                                               const double* __restrict__ bv, int64_t t) {
+    // the product each variant adds: real b*a; bVal.mult(aVal) with a real
+    // (RealComplexCsrMatMult.java:78) or complex a (SemiringCsrMatMult.java:81,
+    // Complex128.java:336-341: b.re a.re - b.im a.im, b.re a.im + b.im a.re);
+    // aVal.mult(bVal) with b real (RealComplexCsrMatMult.java:113)
+    if (!AK && !BK) return make_double2(__dmul_rn(__ldg(&av[q]), __ldg(&bv[t])), 0.0);
+    if (!AK) {
+        const double a = __ldg(&av[q]);
+        const double2 b = __ldg(reinterpret_cast<const double2*>(bv) + t);
+        return make_double2(__dmul_rn(b.x, a), __dmul_rn(b.y, a));
+    }
+    const double2 a = __ldg(reinterpret_cast<const double2*>(av) + q);
+    if (!BK) {
+        const double b = __ldg(&bv[t]);
+        return make_double2(__dmul_rn(a.x, b), __dmul_rn(a.y, b));
+    }
+    const double2 b = __ldg(reinterpret_cast<const double2*>(bv) + t);
+    return make_double2(__dsub_rn(__dmul_rn(b.x, a.x), __dmul_rn(b.y, a.y)),
+                        __dadd_rn(__dmul_rn(b.x, a.y), __dmul_rn(b.y, a.x)));
+}
+
+// AK / BK: 1 when A's / B's values are complex (interleaved); C is complex
+// (interleaved) when either is.
+template <int AK, int BK>
 __global__ void k_spgemm_dense(int64_t rows, int64_t n2, const int* __restrict__ arp, const int* __restrict__ aci,
                                const double* __restrict__ av, const int* __restrict__ brp,
                                const int* __restrict__ bci, const double* __restrict__ bv, double* __restrict__ C) {
+    constexpr int W = (AK || BK) ? 2 : 1;
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
     if (row >= rows) return;
-    double* Cr = C + row * n2;
+    double* Cr = C + row * n2 * W;
     const int q1 = __ldg(&arp[row + 1]);
     for (int q = __ldg(&arp[row]); q < q1; q++) {
         const int k = __ldg(&aci[q]);
-        const double a = __ldg(&av[q]);
         const int t1 = __ldg(&brp[k + 1]);
         for (int t = __ldg(&brp[k]) + lane; t < t1; t += 32) {
-            const int j = __ldg(&bci[t]);
-            Cr[j] = __dadd_rn(Cr[j], __dmul_rn(a, __ldg(&bv[t])));
+            const int64_t j = __ldg(&bci[t]);
+            const double2 p = spgemm_prod<AK, BK>(av, q, bv, t);
+            Cr[W * j] = __dadd_rn(Cr[W * j], p.x);
+            if (W == 2) Cr[W * j + 1] = __dadd_rn(Cr[W * j + 1], p.y);
         }
         __syncwarp();
     }
@@ -617,27 +648,38 @@ __global__ void k_spgemm_len(int64_t annz, const int* __restrict__ aci, const in
     if (threadIdx.x % 32 == 0 && l) atomicAdd(total, l);
 }
 
-// off: inclusive scan of the expansion lengths, one per nonzero of A
+// off: inclusive scan of the expansion lengths, one per nonzero of A; ev
+// holds W values per product (interleaved when complex)
+template <int AK, int BK>
 __global__ void k_spgemm_expand(int64_t rows, const int* __restrict__ arp, const int* __restrict__ aci,
                                 const double* __restrict__ av, const int* __restrict__ brp,
                                 const int* __restrict__ bci, const double* __restrict__ bv,
                                 const int* __restrict__ off, int* __restrict__ er, int* __restrict__ ec,
                                 double* __restrict__ ev) {
+    constexpr int W = (AK || BK) ? 2 : 1;
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
     if (row >= rows) return;
     const int q1 = __ldg(&arp[row + 1]);
     for (int q = __ldg(&arp[row]); q < q1; q++) {
         const int k = __ldg(&aci[q]);
-        const double a = __ldg(&av[q]);
         const int t0 = __ldg(&brp[k]), t1 = __ldg(&brp[k + 1]);
-        const int base = (q ? __ldg(&off[q - 1]) : 0) - t0;
+        const int64_t base = (int64_t)(q ? __ldg(&off[q - 1]) : 0) - t0;
         for (int t = t0 + lane; t < t1; t += 32) {
             er[base + t] = (int)row;
             ec[base + t] = __ldg(&bci[t]);
-            ev[base + t] = __dmul_rn(__ldg(&bv[t]), a);
+            const double2 p = spgemm_prod<AK, BK>(av, q, bv, t);
+            ev[W * (base + t)] = p.x;
+            if (W == 2) ev[W * (base + t) + 1] = p.y;
         }
     }
+}
+
+// complex products gathered into sorted order: dst[i] = src[perm[i]]
+__global__ void k_gather_z(int64_t n, const int* __restrict__ perm, const double2* __restrict__ src,
+                           double2* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[perm[i]];
 }
 
 // fs: inclusive scan of the run-start flags of the sorted expansion
@@ -651,6 +693,7 @@ __global__ void k_run_starts(int64_t n, const int* __restrict__ fs, int* __restr
     if (e < n && (e == 0 || fs[e] != fs[e - 1])) starts[fs[e] - 1] = (int)e;
 }
 
+template <int W>
 __global__ void k_run_sum(int64_t runs, int64_t n, const int* __restrict__ starts, const int* __restrict__ r,
                           const int* __restrict__ c, const double* __restrict__ v, int* __restrict__ oc,
                           double* __restrict__ ov, int* __restrict__ rowcnt) {
@@ -658,10 +701,14 @@ __global__ void k_run_sum(int64_t runs, int64_t n, const int* __restrict__ start
     if (u >= runs) return;
     const int s0 = starts[u];
     const int64_t s1 = u + 1 < runs ? starts[u + 1] : n;
-    double acc = v[s0];
-    for (int64_t e = s0 + 1; e < s1; e++) acc = __dadd_rn(acc, v[e]);
+    double acc0 = v[W * (int64_t)s0], acc1 = W == 2 ? v[W * (int64_t)s0 + 1] : 0.0;
+    for (int64_t e = s0 + 1; e < s1; e++) {
+        acc0 = __dadd_rn(acc0, v[W * e]);
+        if (W == 2) acc1 = __dadd_rn(acc1, v[W * e + 1]);
+    }
     oc[u] = c[s0];
-    ov[u] = acc;
+    ov[W * u] = acc0;
+    if (W == 2) ov[W * u + 1] = acc1;
     atomicAdd(&rowcnt[r[s0]], 1);
 }
 
@@ -920,11 +967,11 @@ extern "C" int f4j_csr_buffers(f4j_csr S, f4j_buf* rowptr, f4j_buf* colidx, f4j_
     return F4J_OK;
 }
 
-static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_csr* out) {
+static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_csr* out, int vw = 1) {
     f4j_buf rp = nullptr, ci = nullptr, v = nullptr;
     int rc = f4j_buf_alloc(ctx, (size_t)(rows + 1) * 4, &rp);
     if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 4, &ci);
-    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 8, &v);
+    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 8 * vw, &v);
     if (rc) {
         f4j_buf_free(ctx, rp);
         f4j_buf_free(ctx, ci);
@@ -996,7 +1043,7 @@ extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_
 // keys' significant bits (all 32 with a sign flip when an index is negative,
 // so negative indices order first as the reference's int comparison has them).
 static int coo_sort_radix(f4j_ctx* ctx, int64_t nnz, int* rowidx, int* colidx, double* vals, int rbits, int cbits,
-                          bool flip) {
+                          bool flip, int* perm_out) {
     unsigned* keys = nullptr;
     int *perm = nullptr, *tmp = nullptr;
     double* vtmp = nullptr;
@@ -1025,6 +1072,7 @@ static int coo_sort_radix(f4j_ctx* ctx, int64_t nnz, int* rowidx, int* colidx, d
             cudaMemcpyAsync(vals, vtmp, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream);
         }
         ctx->launches += vals ? 3 : 2;
+        if (perm_out) cudaMemcpyAsync(perm_out, perm, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
     }
@@ -1035,9 +1083,13 @@ static int coo_sort_radix(f4j_ctx* ctx, int64_t nnz, int* rowidx, int* colidx, d
     return rc;
 }
 
-// Stable sort of n device triplets by (row, col), in place (v may be null).
-static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
-    if (nnz <= 1) return F4J_OK;
+// Stable sort of n device triplets by (row, col), in place (v may be null);
+// perm_out (may be null) receives the input index of every sorted position.
+static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, int* perm_out = nullptr) {
+    if (nnz <= 1) {
+        if (nnz == 1 && perm_out) F4J_CUDA(cudaMemsetAsync(perm_out, 0, 4, ctx->stream));
+        return F4J_OK;
+    }
     const unsigned red_grid = (unsigned)std::min<int64_t>(grid1(nnz), (int64_t)ctx->sm_count * 8);
 
     // index range: mm = {min of rows and columns, max row, max column, longest row}
@@ -1053,7 +1105,7 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     if (hm[0] < 0) {
         f4j_dev_free(ctx, mm);
-        return coo_sort_radix(ctx, nnz, r, c, v, 32, 32, true);
+        return coo_sort_radix(ctx, nnz, r, c, v, 32, 32, true, perm_out);
     }
     const int64_t rows = (int64_t)hm[1] + 1;
     if (rows > 4 * nnz + 4096) {  // row offsets would outweigh the triplets
@@ -1061,7 +1113,7 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
         int rb = 0, cb = 0;
         while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
         while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
-        return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false);
+        return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false, perm_out);
     }
 
     // row offsets and the longest row
@@ -1086,7 +1138,7 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
             int rb = 0, cb = 0;
             while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
             while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
-            return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false);
+            return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false, perm_out);
         }
     }
     unsigned long long* key = nullptr;
@@ -1102,13 +1154,14 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v) {
         if (v) F4J_CUDA(cudaMemcpyAsync(vin, v, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
         k_coo_bucket<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, c, rp, cur, key);
         k_coo_seg_warp<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, rp, key, r, c, vin, v,
-                                                                                   longlist, mm);
+                                                                                   perm_out, longlist, mm);
         // block path sized to the longest row: pmax keys of shared memory, pmax / 2 threads
         int pmax = 64;
         while (pmax < hm[3]) pmax <<= 1;
         const int bthreads = pmax / 2 < 512 ? pmax / 2 : 512;
         const unsigned bgrid = (unsigned)std::min<int64_t>(maxlong, (int64_t)ctx->sm_count * 32);
-        k_coo_seg_block<<<bgrid, bthreads, (size_t)pmax * 8, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v);
+        k_coo_seg_block<<<bgrid, bthreads, (size_t)pmax * 8, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v,
+                                                                            perm_out);
         ctx->launches += 3;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
@@ -1134,19 +1187,42 @@ extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf c
 }
 
 // ------------------------------------------------------------------ CSR x CSR
-extern "C" int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report* rep) {
+// The value kinds of A and B select the variant: real x real (RealCsrMatMult),
+// real x complex and complex x real (RealComplexCsrMatMult), complex x complex
+// (SemiringCsrMatMult over Complex128).
+static int check_csr_values(f4j_csr S, int cplx) {
+    if (cplx && (S->vals->bytes < (size_t)S->nnz * 16 || !f4j_aligned16(S->vals->ptr)))
+        return f4j_fail(F4J_ERR_ARG, "complex CSR values need 16 * nnz bytes, 16-byte aligned");
+    return F4J_OK;
+}
+
+template <int AK, int BK>
+static void launch_spgemm_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, double* C) {
+    k_spgemm_dense<AK, BK><<<(unsigned)f4j_cdiv(A->rows * 32, 256), 256, 0, ctx->stream>>>(
+        A->rows, B->cols, (const int*)A->rowptr->ptr, (const int*)A->colidx->ptr, (const double*)A->vals->ptr,
+        (const int*)B->rowptr->ptr, (const int*)B->colidx->ptr, (const double*)B->vals->ptr, C);
+}
+
+extern "C" int f4j_csr_mult_dense_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_buf C,
+                                     f4j_report* rep) {
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (A->cols != B->rows) return f4j_shape_error(A->rows, A->cols, B->rows, B->cols);
-    if (C->bytes < (size_t)(A->rows * B->cols) * 8) return f4j_fail(F4J_ERR_ARG, "C buffer too small");
+    int rc = check_csr_values(A, a_complex);
+    if (!rc) rc = check_csr_values(B, b_complex);
+    if (rc) return rc;
+    const int W = (a_complex || b_complex) ? 2 : 1;
+    if (C->bytes < (size_t)(A->rows * B->cols) * 8 * W) return f4j_fail(F4J_ERR_ARG, "C buffer too small");
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     if (A->rows * B->cols > 0) {
-        F4J_CUDA(cudaMemsetAsync(C->ptr, 0, (size_t)(A->rows * B->cols) * 8, ctx->stream));
+        F4J_CUDA(cudaMemsetAsync(C->ptr, 0, (size_t)(A->rows * B->cols) * 8 * W, ctx->stream));
+        double* Cp = (double*)C->ptr;
         f4j_prof_begin(ctx);
-        k_spgemm_dense<<<(unsigned)f4j_cdiv(A->rows * 32, 256), 256, 0, ctx->stream>>>(
-            A->rows, B->cols, (const int*)A->rowptr->ptr, (const int*)A->colidx->ptr, (const double*)A->vals->ptr,
-            (const int*)B->rowptr->ptr, (const int*)B->colidx->ptr, (const double*)B->vals->ptr, (double*)C->ptr);
+        if (a_complex && b_complex) launch_spgemm_dense<1, 1>(ctx, A, B, Cp);
+        else if (a_complex) launch_spgemm_dense<1, 0>(ctx, A, B, Cp);
+        else if (b_complex) launch_spgemm_dense<0, 1>(ctx, A, B, Cp);
+        else launch_spgemm_dense<0, 0>(ctx, A, B, Cp);
         f4j_prof_end(ctx);
         F4J_LAUNCHED(ctx);
     }
@@ -1157,23 +1233,38 @@ extern "C" int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C,
     return F4J_OK;
 }
 
-extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* rep) {
+extern "C" int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report* rep) {
+    return f4j_csr_mult_dense_ex(ctx, A, 0, B, 0, C, rep);
+}
+
+template <int AK, int BK>
+static void launch_spgemm_expand(f4j_ctx* ctx, f4j_csr A, f4j_csr B, const int* off, int* er, int* ec, double* ev) {
+    k_spgemm_expand<AK, BK><<<(unsigned)f4j_cdiv(A->rows * 32, 256), 256, 0, ctx->stream>>>(
+        A->rows, (const int*)A->rowptr->ptr, (const int*)A->colidx->ptr, (const double*)A->vals->ptr,
+        (const int*)B->rowptr->ptr, (const int*)B->colidx->ptr, (const double*)B->vals->ptr, off, er, ec, ev);
+}
+
+extern "C" int f4j_csr_mult_csr_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_csr* out,
+                                   f4j_report* rep) {
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
     *out = nullptr;
     if (A->cols != B->rows) return f4j_shape_error(A->rows, A->cols, B->rows, B->cols);
+    int rc = check_csr_values(A, a_complex);
+    if (!rc) rc = check_csr_values(B, b_complex);
+    if (rc) return rc;
+    const int W = (a_complex || b_complex) ? 2 : 1;
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     const int64_t annz = A->nnz, rows = A->rows;
-    const int *arp = (const int*)A->rowptr->ptr, *aci = (const int*)A->colidx->ptr;
-    const int *brp = (const int*)B->rowptr->ptr, *bci = (const int*)B->colidx->ptr;
-    const double *av = (const double*)A->vals->ptr, *bv = (const double*)B->vals->ptr;
+    const int* aci = (const int*)A->colidx->ptr;
+    const int* brp = (const int*)B->rowptr->ptr;
 
     // expansion size
     int* len = nullptr;
     unsigned long long* total = nullptr;
     unsigned long long E = 0;
-    int rc = f4j_dev_alloc(ctx, (size_t)(annz > 0 ? annz : 1) * 4, (void**)&len);
+    rc = f4j_dev_alloc(ctx, (size_t)(annz > 0 ? annz : 1) * 4, (void**)&len);
     if (!rc) rc = f4j_dev_alloc(ctx, 8, (void**)&total);
     if (!rc && annz > 0) {
         F4J_CUDA(cudaMemsetAsync(total, 0, 8, ctx->stream));
@@ -1184,19 +1275,36 @@ extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out
         if (E > (unsigned long long)INT32_MAX)
             rc = f4j_fail(F4J_ERR_UNSUPPORTED, "CSR product expands to %llu products, over 2^31 - 1", E);
     }
-    int *er = nullptr, *ec = nullptr, *fs = nullptr, *starts = nullptr;
-    double* ev = nullptr;
+    int *er = nullptr, *ec = nullptr, *fs = nullptr, *starts = nullptr, *perm = nullptr;
+    double *ev = nullptr, *evs = nullptr;
     int64_t runs = 0;
     if (!rc && E > 0) {
         rc = scan_inclusive(ctx, len, annz);
         if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&er);
         if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&ec);
-        if (!rc) rc = f4j_dev_alloc(ctx, E * 8, (void**)&ev);
+        if (!rc) rc = f4j_dev_alloc(ctx, E * 8 * W, (void**)&ev);
         if (!rc) {
-            k_spgemm_expand<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, arp, aci, av, brp, bci,
-                                                                                       bv, len, er, ec, ev);
+            if (a_complex && b_complex) launch_spgemm_expand<1, 1>(ctx, A, B, len, er, ec, ev);
+            else if (a_complex) launch_spgemm_expand<1, 0>(ctx, A, B, len, er, ec, ev);
+            else if (b_complex) launch_spgemm_expand<0, 1>(ctx, A, B, len, er, ec, ev);
+            else launch_spgemm_expand<0, 0>(ctx, A, B, len, er, ec, ev);
             ctx->launches++;
-            rc = coo_sort_dev(ctx, (int64_t)E, er, ec, ev);
+            if (W == 1) {
+                rc = coo_sort_dev(ctx, (int64_t)E, er, ec, ev);
+            } else {
+                // complex products follow the sort through its permutation
+                rc = f4j_dev_alloc(ctx, E * 4, (void**)&perm);
+                if (!rc) rc = coo_sort_dev(ctx, (int64_t)E, er, ec, nullptr, perm);
+                if (!rc) rc = f4j_dev_alloc(ctx, E * 16, (void**)&evs);
+                if (!rc) {
+                    k_gather_z<<<(unsigned)f4j_cdiv(E, 256), 256, 0, ctx->stream>>>(
+                        (int64_t)E, perm, (const double2*)ev, (double2*)evs);
+                    ctx->launches++;
+                    double* t = ev;
+                    ev = evs;
+                    evs = t;
+                }
+            }
         }
         if (!rc) rc = f4j_dev_alloc(ctx, E * 4, (void**)&fs);
         if (!rc) {
@@ -1217,13 +1325,18 @@ extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out
         }
     }
     f4j_csr T = nullptr;
-    if (!rc) rc = alloc_owned_csr(ctx, rows, B->cols, runs, &T);
+    if (!rc) rc = alloc_owned_csr(ctx, rows, B->cols, runs, &T, W);
     if (!rc) {
         int* trp = (int*)T->rowptr->ptr;
         F4J_CUDA(cudaMemsetAsync(trp, 0, (size_t)(rows + 1) * 4, ctx->stream));
         if (runs > 0) {
-            k_run_sum<<<(unsigned)f4j_cdiv(runs, 256), 256, 0, ctx->stream>>>(
-                runs, (int64_t)E, starts, er, ec, ev, (int*)T->colidx->ptr, (double*)T->vals->ptr, trp + 1);
+            const unsigned g = (unsigned)f4j_cdiv(runs, 256);
+            if (W == 2)
+                k_run_sum<2><<<g, 256, 0, ctx->stream>>>(runs, (int64_t)E, starts, er, ec, ev, (int*)T->colidx->ptr,
+                                                         (double*)T->vals->ptr, trp + 1);
+            else
+                k_run_sum<1><<<g, 256, 0, ctx->stream>>>(runs, (int64_t)E, starts, er, ec, ev, (int*)T->colidx->ptr,
+                                                         (double*)T->vals->ptr, trp + 1);
             ctx->launches++;
             rc = scan_inclusive(ctx, trp + 1, rows);
         }
@@ -1235,6 +1348,8 @@ extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out
     f4j_dev_free(ctx, er);
     f4j_dev_free(ctx, ec);
     f4j_dev_free(ctx, ev);
+    f4j_dev_free(ctx, evs);
+    f4j_dev_free(ctx, perm);
     f4j_dev_free(ctx, fs);
     f4j_dev_free(ctx, starts);
     if (rc) {
@@ -1247,6 +1362,10 @@ extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out
         rep->launches = (int32_t)(ctx->launches - l0);
     }
     return F4J_OK;
+}
+
+extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* rep) {
+    return f4j_csr_mult_csr_ex(ctx, A, 0, B, 0, out, rep);
 }
 
 extern "C" int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out) {

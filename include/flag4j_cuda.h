@@ -229,6 +229,24 @@ int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report
  *   (HashMap.merge).  Bit-identical.  F4J_ERR_UNSUPPORTED when the product
  *   count (sum over A's nonzeros of the length of B's row) exceeds 2^31 - 1. */
 int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* report);
+/* The same two products for complex operands: a_complex / b_complex say
+ * whether A's / B's values are complex (interleaved, 16 * nnz bytes); the
+ * result (C, or *out's values) is complex when either is.
+ *   real x complex  CsrMatrix.mult(CsrCMatrix) / mult2Csr(CsrCMatrix) ->
+ *     RealComplexCsrMatMult.standard / standardAsSparse
+ *     (src/main/java/org/flag4j/linalg/ops/sparse/csr/real_complex/
+ *      RealComplexCsrMatMult.java:58-83, :133-181): per part b * a
+ *   complex x real  CsrCMatrix.mult(CsrMatrix) / mult2Csr(CsrMatrix)
+ *     (same file :93-118, :190-238): per part a * b
+ *   complex x complex  CsrCMatrix.mult(CsrCMatrix) / mult2Csr(CsrCMatrix) ->
+ *     SemiringCsrMatMult.standard / standardToSparse
+ *     (…/semiring_ops/SemiringCsrMatMult.java:58-87, :109-158) with
+ *     Complex128.mult(b, a) (Complex128.java:336-341)
+ * each product and sum rounded as there; bit-identical. */
+int f4j_csr_mult_dense_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_buf C,
+                          f4j_report* report);
+int f4j_csr_mult_csr_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_csr* out,
+                        f4j_report* report);
 
 /* y = S x.  Replaces CsrMatrix.mult(Vector) -> RealCsrDenseMatMult.standardVector
  *   (CsrMatrix.java:1170-1171, src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/

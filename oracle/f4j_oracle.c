@@ -461,6 +461,108 @@ int64_t orc_spgemm_csr(int64_t rows, int64_t n2, const int32_t* arp, const int32
     return nnz;
 }
 
+/* The product one entry of a CSR x CSR product adds, by the operands'     */
+/* value kinds (ak / bk 1 = complex, interleaved):                         */
+/*   real x real: aVal*bVal (RealCsrMatMult.java:70)                       */
+/*   real x complex: bVal.mult(aVal) = (b.re*a, b.im*a)                    */
+/*     (RealComplexCsrMatMult.java:78; Complex128.mult(double))            */
+/*   complex x real: aVal.mult(bVal) = (a.re*b, a.im*b) (:113)             */
+/*   complex x complex: bVal.mult(aVal) (SemiringCsrMatMult.java:81,       */
+/*     Complex128.java:336-341): (b.re*a.re - b.im*a.im, b.re*a.im + b.im*a.re) */
+static void orc_csr_prod(int ak, int bk, const double* av, int64_t q, const double* bv, int64_t t, double* pr,
+                         double* pi) {
+    if (!ak && !bk) {
+        *pr = av[q] * bv[t];
+        *pi = 0.0;
+    } else if (!ak) {
+        const double a = av[q];
+        *pr = bv[2 * t] * a;
+        *pi = bv[2 * t + 1] * a;
+    } else if (!bk) {
+        const double b = bv[t];
+        *pr = av[2 * q] * b;
+        *pi = av[2 * q + 1] * b;
+    } else {
+        const double ar = av[2 * q], ai = av[2 * q + 1], br = bv[2 * t], bi = bv[2 * t + 1];
+        const double rr = br * ar, ii = bi * ai, ri = br * ai, ir = bi * ar;
+        *pr = rr - ii;
+        *pi = ri + ir;
+    }
+}
+
+/* Dense result of the complex variants (RealComplexCsrMatMult.standard,  */
+/* :58-83 and :93-118; SemiringCsrMatMult.standard, :58-87): C (rows x n2 */
+/* complex, interleaved) starts at Complex128.ZERO and adds each product  */
+/* per part in the loop order of orc_spgemm_dense.                        */
+void orc_spgemm_dense_z(int ak, int bk, int64_t rows, int64_t n2, const int32_t* arp, const int32_t* aci,
+                        const double* av, const int32_t* brp, const int32_t* bci, const double* bv, double* C) {
+    for (int64_t i = 0; i < 2 * rows * n2; i++) C[i] = 0.0;
+    for (int64_t i = 0; i < rows; i++) {
+        double* d = C + 2 * i * n2;
+        for (int32_t q = arp[i]; q < arp[i + 1]; q++) {
+            const int32_t k = aci[q];
+            for (int32_t t = brp[k]; t < brp[k + 1]; t++) {
+                double pr, pi;
+                orc_csr_prod(ak, bk, av, q, bv, t, &pr, &pi);
+                const int64_t j = bci[t];
+                d[2 * j] = d[2 * j] + pr;
+                d[2 * j + 1] = d[2 * j + 1] + pi;
+            }
+        }
+    }
+}
+
+/* CSR result of the complex variants (RealComplexCsrMatMult.standardAs-  */
+/* Sparse :133-181 and :190-238; SemiringCsrMatMult.standardToSparse      */
+/* :109-158): tempMap.merge(bCol, product, add) per row, columns sorted;  */
+/* as orc_spgemm_csr with complex values (out_v interleaved).             */
+int64_t orc_spgemm_csr_z(int ak, int bk, int64_t rows, int64_t n2, const int32_t* arp, const int32_t* aci,
+                         const double* av, const int32_t* brp, const int32_t* bci, const double* bv,
+                         int32_t* out_rp, int32_t* out_ci, double* out_v) {
+    double* acc = (double*)calloc(2 * (n2 > 0 ? n2 : 1), sizeof(double));
+    unsigned char* seen = (unsigned char*)calloc(n2 > 0 ? n2 : 1, 1);
+    int32_t* list = (int32_t*)malloc(sizeof(int32_t) * (n2 > 0 ? n2 : 1));
+    int64_t nnz = 0;
+    out_rp[0] = 0;
+    for (int64_t i = 0; i < rows; i++) {
+        int64_t nl = 0;
+        for (int32_t q = arp[i]; q < arp[i + 1]; q++) {
+            const int32_t k = aci[q];
+            for (int32_t t = brp[k]; t < brp[k + 1]; t++) {
+                const int32_t j = bci[t];
+                double pr, pi;
+                orc_csr_prod(ak, bk, av, q, bv, t, &pr, &pi);
+                if (!seen[j]) {
+                    seen[j] = 1;
+                    acc[2 * j] = pr;
+                    acc[2 * j + 1] = pi;
+                    list[nl++] = j;
+                } else {
+                    acc[2 * j] = acc[2 * j] + pr;
+                    acc[2 * j + 1] = acc[2 * j + 1] + pi;
+                }
+            }
+        }
+        qsort(list, (size_t)nl, sizeof(int32_t), orc_cmp_i32);
+        for (int64_t u = 0; u < nl; u++) {
+            const int32_t j = list[u];
+            if (out_ci) {
+                out_ci[nnz] = j;
+                out_v[2 * nnz] = acc[2 * j];
+                out_v[2 * nnz + 1] = acc[2 * j + 1];
+            }
+            nnz++;
+            seen[j] = 0;
+        }
+        out_rp[i + 1] = (int32_t)nnz;
+    }
+    free(acc);
+    free(seen);
+    free(list);
+    return nnz;
+}
+
+
 void orc_coo_sort(int64_t nnz, int32_t* rowidx, int32_t* colidx, double* vals, int64_t* perm_out) {
     int64_t* p = (int64_t*)malloc(sizeof(int64_t) * (nnz > 0 ? nnz : 1));
     int64_t* t = (int64_t*)malloc(sizeof(int64_t) * (nnz > 0 ? nnz : 1));

@@ -57,12 +57,15 @@ def lib():
                 "orc_absgemm": [i64, i64, i64, p, p, p, i32],
                 "orc_spgemm_dense": [i64, i64, p, p, p, p, p, p, p],
                 "orc_spgemm_csr": [i64, i64, p, p, p, p, p, p, p, p, p],
+                "orc_spgemm_dense_z": [i32, i32, i64, i64, p, p, p, p, p, p, p],
+                "orc_spgemm_csr_z": [i32, i32, i64, i64, p, p, p, p, p, p, p, p, p],
             }
             for name, args in sig.items():
                 f = getattr(L, name)
                 f.argtypes = args
                 f.restype = None
             L.orc_spgemm_csr.restype = ctypes.c_int64
+            L.orc_spgemm_csr_z.restype = ctypes.c_int64
             _lib = L
     return _lib
 
@@ -216,6 +219,44 @@ def spgemm_csr(arp, aci, av, brp, bci, bv, n2):
     nnz = lib().orc_spgemm_csr(rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rp), None, None)
     ci, v = np.empty(max(nnz, 1), np.int32), np.empty(max(nnz, 1), np.float64)
     lib().orc_spgemm_csr(rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rp), _p(ci), _p(v))
+    return rp, ci[:nnz], v[:nnz]
+
+
+def _csr_vals(v):
+    """(kind, float64 storage): complex values interleaved."""
+    v = np.asarray(v)
+    if np.iscomplexobj(v):
+        return 1, np.ascontiguousarray(v, np.complex128).view(np.float64)
+    return 0, _f64(v)
+
+
+def spgemm_dense_any(arp, aci, av, brp, bci, bv, n2):
+    """CSR x CSR with a dense result for any mix of real / complex values (the complex variants
+    RealComplexCsrMatMult.standard, SemiringCsrMatMult.standard; real x real as spgemm_dense)."""
+    ak, av = _csr_vals(av)
+    bk, bv = _csr_vals(bv)
+    if not ak and not bk:
+        return spgemm_dense(arp, aci, av, brp, bci, bv, n2)
+    arp, aci, brp, bci = _i32(arp), _i32(aci), _i32(brp), _i32(bci)
+    rows = len(arp) - 1
+    C = np.empty((rows, n2), np.complex128)
+    lib().orc_spgemm_dense_z(ak, bk, rows, n2, _p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(C))
+    return C
+
+
+def spgemm_csr_any(arp, aci, av, brp, bci, bv, n2):
+    """CSR x CSR with a CSR result for any mix of real / complex values -> (rowptr, colidx, vals)."""
+    ak, av = _csr_vals(av)
+    bk, bv = _csr_vals(bv)
+    if not ak and not bk:
+        return spgemm_csr(arp, aci, av, brp, bci, bv, n2)
+    arp, aci, brp, bci = _i32(arp), _i32(aci), _i32(brp), _i32(bci)
+    rows = len(arp) - 1
+    rp = np.empty(rows + 1, np.int32)
+    args = (_p(arp), _p(aci), _p(av), _p(brp), _p(bci), _p(bv), _p(rp))
+    nnz = lib().orc_spgemm_csr_z(ak, bk, rows, n2, *args, None, None)
+    ci, v = np.empty(max(nnz, 1), np.int32), np.empty(max(nnz, 1), np.complex128)
+    lib().orc_spgemm_csr_z(ak, bk, rows, n2, *args, _p(ci), _p(v))
     return rp, ci[:nnz], v[:nnz]
 
 

@@ -14,6 +14,7 @@ Files read (paths within the Flag4j project):
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java
+  src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealComplexCsrCsrMatMultTests.java
 
 Usage:  python tests/golden/make_golden.py [/path/to/flag4j]
 The fixture is committed; the GPU machine never needs the reference tree.
@@ -35,6 +36,7 @@ FILES = {
     "csr_dense": T + "arrays/sparse/csr_matrix/RealCsrDenseMatMultTests.java",
     "csr_transpose": T + "arrays/sparse/csr_matrix/CsrMatrixTransposeTests.java",
     "csr_csr": T + "arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java",
+    "csr_csr_rz": T + "arrays/sparse/csr_matrix/RealComplexCsrCsrMatMultTests.java",
 }
 
 # ---------------------------------------------------------------- parsing

@@ -436,3 +436,62 @@ def _csr_of(a):
     rp = np.zeros(a.shape[0] + 1, np.int32)
     np.cumsum(np.bincount(r, minlength=a.shape[0]), out=rp[1:])
     return rp, c.astype(np.int32), a[r, c].copy()
+
+
+def _cplx(a):
+    a = np.asarray(a, dtype=np.float64)
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def test_golden_real_complex_csr_products(f4j, golden):
+    # RealComplexCsrCsrMatMultTests.java:37-162: CsrMatrix.mult(CsrCMatrix) equals aDense.mult(bDense),
+    # mult2Csr its toCsr(); shape mismatches throw
+    for c in golden["csr_csr_rz"]:
+        a, b = np.array(c["vars"]["aEntries"]), _cplx(c["vars"]["bEntries"])
+        A = f4j.Matrix(a).toCsr()
+        B = f4j.CMatrix(b).toCsr()
+        if c["call"] == "assertThrows":
+            with pytest.raises(f4j.LinearAlgebraException):
+                A.mult(B) if c["method"] == "multTests" else A.mult2Csr(B)
+            continue
+        if c["call"] != "assertEquals":
+            continue
+        exp = f4j.Matrix(a).mult(f4j.CMatrix(b), mode="exact").toNumpy()
+        if c["method"] == "multTests":
+            assert np.array_equal(A.mult(B).toNumpy(), exp)
+        else:
+            got = A.mult2Csr(B)
+            assert isinstance(got, f4j.CsrCMatrix)
+            r, cc = np.nonzero(exp != 0)
+            assert np.array_equal(got.colIndices, cc) and np.array_equal(got.data, exp[r, cc])
+
+
+def _csr_any(rng, rows, cols, dens, cplx):
+    a = np.where(rng.random((rows, cols)) < dens, rng.standard_normal((rows, cols)), 0.0)
+    if cplx:
+        a = a + 1j * np.where(a != 0, rng.standard_normal((rows, cols)), 0.0)
+    r, c = np.nonzero(a != 0)
+    rp = np.zeros(rows + 1, np.int32)
+    np.cumsum(np.bincount(r, minlength=rows), out=rp[1:])
+    return rp, c.astype(np.int32), a[r, c].copy()
+
+
+@pytest.mark.parametrize("ak,bk", [(0, 1), (1, 0), (1, 1)])
+def test_complex_csr_csr_bit_identical(f4j, oracle, ak, bk):
+    rng = np.random.default_rng(10 * ak + bk)
+    m, k, n = 700, 500, 900
+    arp, aci, av = _csr_any(rng, m, k, 0.02, ak)
+    brp, bci, bv = _csr_any(rng, k, n, 0.02, bk)
+    bv[::9] = 0.0  # stored zeros: signed-zero products
+    A = (f4j.CsrCMatrix if ak else f4j.CsrMatrix)((m, k), av, arp, aci)
+    B = (f4j.CsrCMatrix if bk else f4j.CsrMatrix)((k, n), bv, brp, bci)
+    got = A.mult(B).toNumpy()
+    assert np.array_equal(_bits(got.view(np.float64)),
+                          _bits(oracle.spgemm_dense_any(arp, aci, av, brp, bci, bv, n).view(np.float64)))
+    rp, ci, v = oracle.spgemm_csr_any(arp, aci, av, brp, bci, bv, n)
+    S = A.mult2Csr(B)
+    assert isinstance(S, f4j.CsrCMatrix) and S.nnz == len(v)
+    assert np.array_equal(S.rowPointers, rp) and np.array_equal(S.colIndices, ci)
+    assert np.array_equal(_bits(S.data.view(np.float64)), _bits(v.view(np.float64)))
+    with pytest.raises(f4j.LinearAlgebraException):
+        A.mult(A)

@@ -112,6 +112,46 @@ def test_csr_csr_products_equal_dense(oracle, golden):
         assert np.array(c["vars"]["aEntries"]).shape[1] != np.array(c["vars"]["bEntries"]).shape[0]
 
 
+def _cplx(a):
+    a = np.asarray(a, dtype=np.float64)
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def test_real_complex_csr_products_equal_dense(oracle, golden):
+    # RealComplexCsrCsrMatMultTests.java:37-162: CsrMatrix.mult(CsrCMatrix) equals
+    # aDense.mult(bDense); mult2Csr equals that product's toCsr()
+    cases = [c for c in golden["csr_csr_rz"] if c["call"] == "assertEquals"]
+    assert [c["method"] for c in cases] == ["multTests", "multTests", "mult2CsrTests", "mult2CsrTests"]
+    for c in cases:
+        a, b = np.array(c["vars"]["aEntries"]), _cplx(c["vars"]["bEntries"])
+        (arp, aci, av), (brp, bci, bv) = _csr_of_dense(a), _csr_of_dense(b)
+        exp = oracle.rzgemm(a, b)
+        if c["method"] == "multTests":
+            assert np.array_equal(oracle.spgemm_dense_any(arp, aci, av, brp, bci, bv, b.shape[1]), exp)
+        else:
+            rp, ci, v = oracle.spgemm_csr_any(arp, aci, av, brp, bci, bv, b.shape[1])
+            erp, eci, ev = _csr_of_dense(exp)
+            assert np.array_equal(rp, erp) and np.array_equal(ci, eci) and np.array_equal(v, ev)
+
+
+def test_complex_csr_restatements_agree_with_dense(oracle):
+    # the three complex variants against dense products of the same matrices
+    rng = np.random.default_rng(4)
+    a = np.where(rng.random((30, 20)) < 0.2, rng.standard_normal((30, 20)), 0.0)
+    b = np.where(rng.random((20, 25)) < 0.2, rng.standard_normal((20, 25)), 0.0)
+    az = a * (1 + 0.5j)
+    bz = b * (0.25 - 1j)
+    for A, B in ((a, bz), (az, b), (az, bz)):
+        (arp, aci, av), (brp, bci, bv) = _csr_of_dense(A), _csr_of_dense(B)
+        C = oracle.spgemm_dense_any(arp, aci, av, brp, bci, bv, B.shape[1])
+        assert np.allclose(C, A @ B, rtol=1e-13, atol=1e-13)
+        rp, ci, v = oracle.spgemm_csr_any(arp, aci, av, brp, bci, bv, B.shape[1])
+        D = np.zeros(C.shape, complex)
+        for i in range(C.shape[0]):
+            D[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        assert np.array_equal(D, C)
+
+
 def test_csr_csr_sparse_result_keeps_cancellations(oracle):
     # standardAsSparse stores every touched column: 1*x + 1*(-x) is an explicit 0.0,
     # and a lone product -1 * 0.0 stays -0.0 (HashMap.merge keeps the first value as is)
