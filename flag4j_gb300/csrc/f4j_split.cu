@@ -479,16 +479,19 @@ __global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int
             float f[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                int d;
+                // with t = x + 16 the balanced digit is (t & 31) - 16 and the
+                // rest (x - digit) / 32 is t >> 5; the -16 is folded into the
+                // float conversion's constant
+                int t;
                 if (c < 6) {
-                    d = ((L[j] + 16) & 31) - 16;
-                    L[j] = (L[j] - d) >> 5;
+                    t = L[j] + 16;
+                    L[j] = t >> 5;
                     if (c == 5) H[j] += L[j];  // carry out of the low 30 bits: 0 or 1
                 } else {
-                    d = ((H[j] + 16) & 31) - 16;
-                    H[j] = (H[j] - d) >> 5;
+                    t = H[j] + 16;
+                    H[j] = t >> 5;
                 }
-                f[j] = float_of_small_int(d);
+                f[j] = float_of_small_int((t & 31) - 16);
             }
             store_e4m3x8(base + (int64_t)(s - 1 - c) * rows_out * Kp, f);
         }
