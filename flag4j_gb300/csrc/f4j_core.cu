@@ -82,6 +82,7 @@ extern "C" int f4j_create(int device, f4j_ctx** out) {
 
 extern "C" int f4j_destroy(f4j_ctx* ctx) {
     F4J_CHECK_CTX(ctx);
+    std::unique_lock<std::recursive_mutex> lock(ctx->mu);  // waits for a call in flight on another thread
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (int i = 0; i < 16; i++)
@@ -106,11 +107,13 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    lock.unlock();
     delete ctx;
     return F4J_OK;
 }
 
 extern "C" int f4j_sync(f4j_ctx* ctx) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     int t = 0;
@@ -121,6 +124,7 @@ extern "C" int f4j_sync(f4j_ctx* ctx) {
 }
 
 extern "C" int f4j_set_stream(f4j_ctx* ctx, void* s) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -138,6 +142,7 @@ extern "C" void* f4j_get_stream(f4j_ctx* ctx) { return ctx ? (void*)ctx->stream 
 extern "C" int64_t f4j_launch_count(f4j_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
 extern "C" int f4j_timer_record(f4j_ctx* ctx, int slot) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (slot < 0 || slot >= 16) return f4j_fail(F4J_ERR_ARG, "timer slot %d out of range", slot);
     if (!ctx->ev_init[slot]) {
@@ -149,6 +154,7 @@ extern "C" int f4j_timer_record(f4j_ctx* ctx, int slot) {
 }
 
 extern "C" int f4j_timer_elapsed(f4j_ctx* ctx, int a, int b, float* ms) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (a < 0 || a >= 16 || b < 0 || b >= 16 || !ctx->ev_init[a] || !ctx->ev_init[b] || !ms)
         return f4j_fail(F4J_ERR_ARG, "timer slots not recorded");
@@ -170,6 +176,7 @@ void f4j_prof_end(f4j_ctx* ctx) {
 }
 
 extern "C" int f4j_set_profiling(f4j_ctx* ctx, int on) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (on && !ctx->prof_init) {
         for (int i = 0; i < 1024; i++) F4J_CUDA(cudaEventCreate(&ctx->prof_ev[i]));
@@ -181,6 +188,7 @@ extern "C" int f4j_set_profiling(f4j_ctx* ctx, int on) {
 }
 
 extern "C" int f4j_profile_read(f4j_ctx* ctx, int tag, double* total_ms, int64_t* count) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!total_ms || !count) return f4j_fail(F4J_ERR_ARG, "null output");
     double t = 0;
@@ -199,6 +207,7 @@ extern "C" int f4j_profile_read(f4j_ctx* ctx, int tag, double* total_ms, int64_t
 }
 
 extern "C" int f4j_profile_reset(f4j_ctx* ctx) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->prof_n = 0;
@@ -250,6 +259,7 @@ void f4j_dev_free(f4j_ctx* ctx, void* p) {
 
 // ------------------------------------------------------------------ buffers
 extern "C" int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
     *out = nullptr;
@@ -264,6 +274,7 @@ extern "C" int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out) {
 }
 
 extern "C" int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
     *out = nullptr;
@@ -296,6 +307,7 @@ extern "C" int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out)
 }
 
 extern "C" int f4j_buf_free(f4j_ctx* ctx, f4j_buf b) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!b) return F4J_OK;
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -318,6 +330,7 @@ static int copy_check(f4j_ctx* ctx, f4j_buf b, const void* host, size_t bytes, s
 }
 
 extern "C" int f4j_buf_upload_async(f4j_ctx* ctx, f4j_buf b, const void* host, size_t bytes, size_t off) {
+    F4J_LOCK(ctx);
     int rc = copy_check(ctx, b, host, bytes, off);
     if (rc) return rc;
     if (bytes)
@@ -326,6 +339,7 @@ extern "C" int f4j_buf_upload_async(f4j_ctx* ctx, f4j_buf b, const void* host, s
 }
 
 extern "C" int f4j_buf_download_async(f4j_ctx* ctx, f4j_buf b, void* host, size_t bytes, size_t off) {
+    F4J_LOCK(ctx);
     int rc = copy_check(ctx, b, host, bytes, off);
     if (rc) return rc;
     if (bytes)
@@ -334,6 +348,7 @@ extern "C" int f4j_buf_download_async(f4j_ctx* ctx, f4j_buf b, void* host, size_
 }
 
 extern "C" int f4j_buf_upload(f4j_ctx* ctx, f4j_buf b, const void* host, size_t bytes, size_t off) {
+    F4J_LOCK(ctx);
     int rc = f4j_buf_upload_async(ctx, b, host, bytes, off);
     if (rc) return rc;
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -341,6 +356,7 @@ extern "C" int f4j_buf_upload(f4j_ctx* ctx, f4j_buf b, const void* host, size_t 
 }
 
 extern "C" int f4j_buf_download(f4j_ctx* ctx, f4j_buf b, void* host, size_t bytes, size_t off) {
+    F4J_LOCK(ctx);
     int rc = f4j_buf_download_async(ctx, b, host, bytes, off);
     if (rc) return rc;
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -348,6 +364,7 @@ extern "C" int f4j_buf_download(f4j_ctx* ctx, f4j_buf b, void* host, size_t byte
 }
 
 extern "C" int f4j_buf_zero(f4j_ctx* ctx, f4j_buf b) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!b) return f4j_fail(F4J_ERR_ARG, "null buffer");
     F4J_CUDA(cudaMemsetAsync(b->ptr, 0, b->bytes, ctx->stream));
@@ -436,6 +453,7 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
 
 extern "C" int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                          f4j_buf B, int opB, f4j_buf C, int mode, f4j_report* rep) {
+    F4J_LOCK(ctx);
     int rc = check_gemm_args(ctx, false, m, n, k, A, opA, B, opB, C, mode);
     if (rc) return rc;
     F4J_CUDA(cudaSetDevice(ctx->device));
@@ -445,6 +463,7 @@ extern "C" int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf 
 
 extern "C" int f4j_zgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                          f4j_buf B, int opB, f4j_buf C, int mode, f4j_report* rep) {
+    F4J_LOCK(ctx);
     int rc = check_gemm_args(ctx, true, m, n, k, A, opA, B, opB, C, mode);
     if (rc) return rc;
     F4J_CUDA(cudaSetDevice(ctx->device));
@@ -548,11 +567,13 @@ static int adjoint(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j
 extern "C" int f4j_dgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A,
                                  f4j_buf B, f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode,
                                  f4j_report* rep) {
+    F4J_LOCK(ctx);
     return adjoint(ctx, false, m, n, k, A, B, dC, dA, dB, mode, rep);
 }
 
 extern "C" int f4j_zgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A,
                                  f4j_buf B, f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode,
                                  f4j_report* rep) {
+    F4J_LOCK(ctx);
     return adjoint(ctx, true, m, n, k, A, B, dC, dA, dB, mode, rep);
 }

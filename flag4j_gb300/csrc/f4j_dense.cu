@@ -595,6 +595,7 @@ int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
 extern "C" int f4j_gemm_check(f4j_ctx* ctx, int cplx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                               f4j_buf B, int opB, f4j_buf C, int64_t samples, uint64_t seed,
                               double* max_abs, double* max_rel) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !C || !max_abs || !max_rel) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (m <= 0 || n <= 0 || k < 0 || samples <= 0) return f4j_fail(F4J_ERR_ARG, "bad sizes");

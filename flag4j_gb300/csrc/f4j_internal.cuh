@@ -6,6 +6,7 @@
 
 #include <cstdarg>
 #include <cstdint>
+#include <mutex>
 #include <cstdio>
 #include <string>
 
@@ -38,6 +39,7 @@ struct f4j_csr_s {
 #define F4J_HOST_PARTS_MAX 8
 
 struct f4j_ctx {
+    std::recursive_mutex mu;  // held by every C-ABI call on this context (F4J_LOCK)
     int device;
     int sm_count;
     cudaStream_t stream;
@@ -92,6 +94,14 @@ int f4j_cuda_fail(cudaError_t e, const char* what);
 
 #define F4J_CHECK_CTX(ctx) \
     do { if (!(ctx)) return f4j_fail(F4J_ERR_ARG, "null context"); } while (0)
+
+// First statement of every C-ABI entry that takes a context: the null check,
+// then the context's lock until the entry returns (entries that call other
+// entries take it again: the mutex is recursive).  Calls from several threads
+// on one context therefore run one at a time, in a consistent state.
+#define F4J_LOCK(ctx) \
+    if (!(ctx)) return f4j_fail(F4J_ERR_ARG, "null context"); \
+    std::lock_guard<std::recursive_mutex> f4j_ctx_lock_((ctx)->mu)
 
 // Workspace slot of at least `bytes` (stream-ordered reuse; growing syncs the
 // stream and discards the slot's previous contents).

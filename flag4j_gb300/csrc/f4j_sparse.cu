@@ -875,6 +875,7 @@ static int launch_spmm(f4j_ctx* ctx, int64_t rows, int64_t ncols, const int* rp,
 // ------------------------------------------------------------------ C ABI
 extern "C" int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowptr, f4j_buf colidx,
                             f4j_buf vals, int validate, f4j_csr* out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
     *out = nullptr;
@@ -935,6 +936,7 @@ extern "C" int f4j_csr_wrap(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nn
 }
 
 extern "C" int f4j_csr_free(f4j_ctx* ctx, f4j_csr S) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S) return F4J_OK;
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -984,6 +986,7 @@ static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz
 
 extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_buf rowidx, f4j_buf colidx,
                                 f4j_buf vals, f4j_csr* out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
     *out = nullptr;
@@ -1176,6 +1179,7 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, in
 }
 
 extern "C" int f4j_coo_sort(f4j_ctx* ctx, int64_t nnz, f4j_buf rowidx, f4j_buf colidx, f4j_buf vals) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!rowidx || !colidx) return f4j_fail(F4J_ERR_ARG, "null COO buffer");
     if (nnz < 0 || nnz > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "bad nnz");
@@ -1205,6 +1209,7 @@ static void launch_spgemm_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, double* C) {
 
 extern "C" int f4j_csr_mult_dense_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_buf C,
                                      f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (A->cols != B->rows) return f4j_shape_error(A->rows, A->cols, B->rows, B->cols);
@@ -1234,6 +1239,7 @@ extern "C" int f4j_csr_mult_dense_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j
 }
 
 extern "C" int f4j_csr_mult_dense(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_buf C, f4j_report* rep) {
+    F4J_LOCK(ctx);
     return f4j_csr_mult_dense_ex(ctx, A, 0, B, 0, C, rep);
 }
 
@@ -1246,6 +1252,7 @@ static void launch_spgemm_expand(f4j_ctx* ctx, f4j_csr A, f4j_csr B, const int* 
 
 extern "C" int f4j_csr_mult_csr_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_csr B, int b_complex, f4j_csr* out,
                                    f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
     *out = nullptr;
@@ -1365,10 +1372,12 @@ extern "C" int f4j_csr_mult_csr_ex(f4j_ctx* ctx, f4j_csr A, int a_complex, f4j_c
 }
 
 extern "C" int f4j_csr_mult_csr(f4j_ctx* ctx, f4j_csr A, f4j_csr B, f4j_csr* out, f4j_report* rep) {
+    F4J_LOCK(ctx);
     return f4j_csr_mult_csr_ex(ctx, A, 0, B, 0, out, rep);
 }
 
 extern "C" int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
     F4J_CUDA(cudaSetDevice(ctx->device));
@@ -1390,6 +1399,7 @@ extern "C" int f4j_csr_transpose(f4j_ctx* ctx, f4j_csr S, f4j_csr* out) {
 }
 
 extern "C" int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S || !perm_out) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (perm_out->bytes < (size_t)S->nnz * 4) return f4j_fail(F4J_ERR_ARG, "perm buffer too small");
@@ -1401,6 +1411,7 @@ extern "C" int f4j_csr_transpose_perm(f4j_ctx* ctx, f4j_csr S, f4j_buf perm_out)
 }
 
 extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mode, f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (mode != F4J_SPARSE_EXACT && mode != F4J_SPARSE_FMA) return f4j_fail(F4J_ERR_ARG, "unknown sparse mode %d", mode);
     if (!S || !x || !y) return f4j_fail(F4J_ERR_ARG, "null argument");
@@ -1439,11 +1450,13 @@ extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mo
 }
 
 extern "C" int f4j_spmv(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, f4j_report* rep) {
+    F4J_LOCK(ctx);
     return f4j_spmv_ex(ctx, S, x, y, F4J_SPARSE_EXACT, rep);
 }
 
 extern "C" int f4j_spmm_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, int mode,
                            f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (mode != F4J_SPARSE_EXACT && mode != F4J_SPARSE_FMA) return f4j_fail(F4J_ERR_ARG, "unknown sparse mode %d", mode);
     if (!S || !X || !Y) return f4j_fail(F4J_ERR_ARG, "null argument");
@@ -1467,10 +1480,12 @@ extern "C" int f4j_spmm_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4
 }
 
 extern "C" int f4j_spmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+    F4J_LOCK(ctx);
     return f4j_spmm_ex(ctx, S, X, ncols, Y, F4J_SPARSE_EXACT, rep);
 }
 
 extern "C" int f4j_zspmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_buf Y, f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S || !X || !Y) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
@@ -1502,6 +1517,7 @@ extern "C" int f4j_zspmm(f4j_ctx* ctx, f4j_csr S, f4j_buf X, int64_t ncols, f4j_
 }
 
 extern "C" int f4j_spmm_t(f4j_ctx* ctx, f4j_csr S, f4j_buf dC, int64_t ncols, f4j_buf dX, f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S || !dC || !dX) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");
@@ -1525,6 +1541,7 @@ extern "C" int f4j_spmm_t(f4j_ctx* ctx, f4j_csr S, f4j_buf dC, int64_t ncols, f4
 
 extern "C" int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t ncols, f4j_buf out,
                          f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!S || !A || !B || !out) return f4j_fail(F4J_ERR_ARG, "null argument");
     if (ncols < 0) return f4j_fail(F4J_ERR_ARG, "negative column count");

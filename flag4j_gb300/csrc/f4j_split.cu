@@ -1086,6 +1086,7 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 // in turn.  Returns when C is in host memory.
 extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                               const double* B, int opB, double* C, int mode, f4j_report* rep) {
+    F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null host pointer");
     if (m < 0 || n < 0 || k < 0) return f4j_fail(F4J_ERR_ARG, "negative dimension");

@@ -17,8 +17,10 @@
  *    on the GPU across calls.  Inputs are never modified; outputs are written.
  *  - All work of a context runs in order on that context's CUDA stream; calls
  *    return once the work is queued (use f4j_sync or a download to wait).
- *    Separate contexts are independent.  A context must not be used from two
- *    threads at once.
+ *    Separate contexts are independent.  A context may be shared by threads:
+ *    every call on it holds the context's lock until it returns, so calls
+ *    from several threads run one at a time (the reference's dispatcher
+ *    cache, BiTensorOpDispatcher.java:68-84, is not thread-safe; this layer is).
  *  - No CPU fallback: every product runs as CUDA kernels on the context's GPU.
  */
 #ifndef FLAG4J_CUDA_H

@@ -487,3 +487,46 @@ def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
     ref = oracle.dgemm(A[fin], B)
     bound = 2 * k * U * oracle.absgemm(A[fin], B)
     assert np.all(np.abs(C[fin] - ref) <= bound)
+
+
+def test_one_context_shared_by_threads(f4j, oracle):
+    """Four threads issue products on one context at once (ctypes releases the GIL,
+    so the C calls overlap); every C-ABI call holds the context's lock, and each
+    thread's result equals the same product run alone."""
+    import threading
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    m, n, k = 300, 200, 256
+    jobs = [(synth.scaled(m, k, 2, 100 + t, "row"), synth.scaled(k, n, 2, 200 + t, "col")) for t in range(4)]
+    refs = [run_gemm(f4j, A, B, mode="split")[0] for A, B in jobs]
+    rp, ci, v = synth.csr_poisson(5000, 4000, seed=9)
+    x = synth.normal(4000, 1, 10).ravel()
+    y_ref = oracle.spmv(rp, ci, v, x)
+    results, errors = [None] * 4, []
+
+    def worker(i):
+        try:
+            A, B = jobs[i]
+            dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(8 * m * n)
+            S = f4j.CsrMatrix((5000, 4000), v, rp, ci)
+            for _ in range(10):
+                check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, 0, dB.handle, 0, dC.handle,
+                                        _lib.MODE_SPLIT, None))
+                assert np.array_equal(S.mult(f4j.Vector(x)).data, y_ref)
+                C = np.empty((m, n))
+                check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, 0, B.ctypes.data, 0,
+                                             C.ctypes.data, _lib.MODE_SPLIT, None))
+                assert np.array_equal(C, refs[i])
+            results[i] = dC.to_numpy(np.float64, m * n).reshape(m, n)
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
+    for i in range(4):
+        assert np.array_equal(results[i], refs[i])
