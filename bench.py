@@ -634,6 +634,19 @@ def run_ours(args):
             del Ap, Bp
         out["errors_by_phi"] = errs
         del A, B
+        # ---- C1: Matrix.mult at 1024^3, U[-1,1) entries, in AUTO (split), PLAIN and EXACT modes
+        c1n = 1024
+        A1, B1 = synth.uniform(c1n, c1n, 61), synth.uniform(c1n, c1n, 62)
+        dA1, dB1, dC1 = E.dev(A1), E.dev(B1), E.ctx.alloc(8 * c1n * c1n)
+        c1 = {"n": c1n}
+        for name, md in (("auto", L.MODE_AUTO), ("plain", L.MODE_PLAIN), ("exact", L.MODE_EXACT)):
+            r1 = E.gemm(dA1, dB1, dC1, c1n, c1n, c1n, md, report=True)
+            t1 = E.timed(lambda: E.gemm(dA1, dB1, dC1, c1n, c1n, c1n, md), 10, 3)
+            c1[name] = {"ms": t1, "tflops": 2.0 * c1n ** 3 / (t1 * 1e-3) / 1e12, "mode_used": r1.mode_used,
+                        "slices": r1.slices}
+        out["c1_gemm_1024"] = c1
+        out["c1_gemm_1024"]["l2"] = "A, B 8 MiB each: L2-resident across steps (a 1024^3 product fits in L2)"
+        del dA1, dB1, dC1
         # ---- matrix-vector product n x n (Matrix.mult(Vector) in AUTO mode: one FP64 FMA dot product per
         # row, A read once; A is 512 MiB at 8192, larger than L2)
         Av, xv, yv = E.dev(synth.normal(n, n, 51)), E.dev(synth.normal(n, 1, 52)), E.ctx.alloc(8 * n)
@@ -724,6 +737,15 @@ def run_ours(args):
             dcb = dense_cpu_baselines(n // 2, n // 2, n // 4)
             out["complex"]["cpu_baseline"] = dcb["complex"]
             out["adjoint"]["cpu_baseline"] = dcb["adjoint"]
+            # C1 on the CPU: the whole 1024^3 product, all cores, 3 warm-ups, median of 5
+            A1, B1 = synth.uniform(1024, 1024, 61), synth.uniform(1024, 1024, 62)
+            threads = os.cpu_count() or 1
+            for _ in range(3):
+                O.dgemm(A1, B1, threads=threads)
+            t1 = statistics.median(_wall(lambda: O.dgemm(A1, B1, threads=threads)) for _ in range(5))
+            out["c1_gemm_1024"]["cpu_baseline"] = {"value": 2.0 * 1024 ** 3 / t1 / 1e12, "unit": "TFLOP/s",
+                                                   "ms": 1e3 * t1, "cores": threads, "kind": "port",
+                                                   "sample": "the whole 1024^3 product, median of 5 after 3 warm-ups"}
 
     dist.close()
     if rank != 0:
