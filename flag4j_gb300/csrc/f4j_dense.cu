@@ -11,6 +11,8 @@
 //    interleaved tiles (Cr = Ar Br - Ai Bi, Ci = Ar Bi + Ai Br).
 //    Transposed / conjugated operands use transposed TMA boxes; nothing is
 //    materialised.
+//  * k_gemv_rows / k_gemv_cols: matrix-vector products (n == 1) in the fast
+//    modes, FP64 FMA dot products reading A once.
 //  * k_gemm_check: double-double (Dot2) evaluation of sampled entries.
 #include "f4j_internal.cuh"
 #include "f4j_ptx.cuh"

@@ -7,8 +7,13 @@
 //         (src/main/java/org/flag4j/linalg/ops/dense_sparse/csr/real/RealCsrDenseMatMult.java:172-192)
 //   SpMM  RealCsrDenseMatMult.standard (same file :55-82)
 //   S^T X RealCsrOps.transpose + standard (…/sparse/csr/real/RealCsrOps.java:195-225)
+//   S1 S2 RealCsrMatMult, RealComplexCsrMatMult, SemiringCsrMatMult (CSR x CSR)
+// SpMV / SpMM also have an opt-in FMA mode (fused multiply-add in storage
+// order, within 2 k u |S||X|); SDDMM (the sparse adjoint's dS) has no
+// reference counterpart and meets the same bound.
 // Structure (COO->CSR, stable COO sort, transpose permutation) is integer
-// work done with histograms, scans and a stable LSD radix sort.
+// work done with histograms, scans, a row-bucketed sort and a stable LSD
+// radix sort.
 #include <vector>
 
 #include "f4j_internal.cuh"
