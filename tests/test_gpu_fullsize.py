@@ -6,7 +6,8 @@
   inputs, and both stay FP64-accurate.
 - C4 dense adjoint at 4096 x 2048 x 4096: dA = W B^T and dB = A^T W on the split
   path within 2 k u |W||B^T| and 2 k u |A^T||W| of the oracle's restatement of
-  W.multTranspose(B) and A.T().mult(W).
+  W.multTranspose(B) and A.T().mult(W); the Complex128 Hermitian variant at
+  2048^3 within the bound per part.
 - C2 structure at 2^20 rows: the stable COO sort and COO -> CSR of 16.8 M
   shuffled triplets equal the oracle's bit for bit.
 - C5 sparse adjoint at 2^20 rows x 64 columns: S^T dC is bit-identical to
@@ -114,3 +115,24 @@ def test_sparse_adjoint_full_config(f4j, oracle):
     ref = oracle.sddmm(rp, ci, dC, X)
     absab = oracle.sddmm(rp, ci, np.abs(dC), np.abs(X))  # sum |a||b| per nonzero
     assert np.all(np.abs(got - ref) <= 2 * w * U * absab)
+
+
+def test_complex_hermitian_adjoint_full_size(f4j, oracle):
+    """C4's complex variant at 2048^3: dA = W B^H and dB = A^H W (W.mult(B.H()),
+    A.H().mult(W)) on the split path within the bound per part of the oracle's
+    Complex128 restatement."""
+    from flag4j_gb300 import synth
+    n = 2048
+    A = synth.normal(n, n, 11) + 1j * synth.normal(n, n, 12)
+    B = synth.normal(n, n, 13) + 1j * synth.normal(n, n, 14)
+    W = synth.normal(n, n, 15) + 1j * synth.normal(n, n, 16)
+    node = f4j.MatMulNode(f4j.CMatrix(A), f4j.CMatrix(B), mode="split")
+    dA, dB = node.backward(f4j.CMatrix(W))
+    t = oracle.threads_default()
+    for got, L, R in ((dA.toNumpy(), W, np.ascontiguousarray(B.conj().T)),
+                      (dB.toNumpy(), np.ascontiguousarray(A.conj().T), W)):
+        ref = oracle.zgemm(L, R, threads=t)
+        ab_re = np.abs(L.real) @ np.abs(R.real) + np.abs(L.imag) @ np.abs(R.imag)
+        ab_im = np.abs(L.real) @ np.abs(R.imag) + np.abs(L.imag) @ np.abs(R.real)
+        assert np.all(np.abs(got.real - ref.real) <= 2 * n * U * ab_re)
+        assert np.all(np.abs(got.imag - ref.imag) <= 2 * n * U * ab_im)
