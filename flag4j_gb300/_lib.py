@@ -48,6 +48,7 @@ SIGNATURES = {
     "f4j_create": (_i, [_i, _pv]),
     "f4j_destroy": (_i, [_v]),
     "f4j_sync": (_i, [_v]),
+    "f4j_selftest_wait": (_i, [_v, _i64]),
     "f4j_set_stream": (_i, [_v, _v]),
     "f4j_get_stream": (_v, [_v]),
     "f4j_launch_count": (_i64, [_v]),

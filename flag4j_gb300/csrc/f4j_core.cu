@@ -3,6 +3,7 @@
 #include <mutex>
 
 #include "f4j_internal.cuh"
+#include "f4j_ptx.cuh"
 
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_last_error;
@@ -120,6 +121,31 @@ extern "C" int f4j_sync(f4j_ctx* ctx) {
     int rc = f4j_status_take(ctx, F4J_ST_TIMEOUT, &t);
     if (rc) return rc;
     if (t) return f4j_fail(F4J_ERR_TIMEOUT, "a device-side wait gave up (code %d)", t);
+    return F4J_OK;
+}
+
+// Self-test of the bounded device waits: one thread waits on an mbarrier
+// phase that nothing completes, with the wait primitive the GEMM kernels use,
+// gives up after limit_ns, records `code` in the timeout status word and
+// returns.
+__global__ void k_wait_selftest(int* status, unsigned long long limit_ns, int code) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait_ns(&bar, 0, status, code, limit_ns);
+    __syncthreads();
+}
+
+extern "C" int f4j_selftest_wait(f4j_ctx* ctx, int64_t limit_us) {
+    F4J_LOCK(ctx);
+    if (limit_us < 1000 || limit_us > 2000000) return f4j_fail(F4J_ERR_ARG, "limit must be 1 ms .. 2 s");
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    k_wait_selftest<<<1, 32, 0, ctx->stream>>>(ctx->d_status + F4J_ST_TIMEOUT,
+                                               (unsigned long long)limit_us * 1000ull, F4J_SELFTEST_WAIT_CODE);
+    F4J_LAUNCHED(ctx);
     return F4J_OK;
 }
 

@@ -63,15 +63,19 @@ __device__ __forceinline__ uint64_t f4j_globaltimer_ns() {
 #ifndef F4J_WAIT_NS
 #define F4J_WAIT_NS 2000000000ull
 #endif
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status, int code) {
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, uint32_t parity, int* status, int code,
+                                             uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = f4j_globaltimer_ns();
     for (uint32_t it = 0; it < F4J_WAIT_LIMIT; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255) == 255 && f4j_globaltimer_ns() - t0 > F4J_WAIT_NS) break;
+        if ((it & 255) == 255 && f4j_globaltimer_ns() - t0 > limit_ns) break;
     }
     if (status) atomicExch(status, code);
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status, int code) {
+    return mbar_wait_ns(bar, parity, status, code, F4J_WAIT_NS);
 }
 
 // Asynchronous 4- / 8-byte copies global -> shared (no register staging; the

@@ -42,6 +42,7 @@ extern "C" {
 #define F4J_ERR_CUDA (-5)        /* CUDA runtime / launch error -> Flag4jDeviceException */
 #define F4J_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up                 */
 #define F4J_ERR_UNSUPPORTED (-7) /* configuration not supported on this device        */
+#define F4J_SELFTEST_WAIT_CODE 99 /* status code of f4j_selftest_wait's expired wait  */
 
 /* ---- operand transforms and GEMM modes ---------------------------------- */
 #define F4J_OP_N 0 /* op(X) = X                        */
@@ -75,6 +76,12 @@ const char* f4j_last_error(void);
 int f4j_create(int device, f4j_ctx** out);
 int f4j_destroy(f4j_ctx* ctx);
 int f4j_sync(f4j_ctx* ctx);
+/* Diagnostic of the bounded device waits (no Flag4j counterpart): queues a
+ * kernel whose wait on an mbarrier that nothing completes gives up after
+ * limit_us (1 ms .. 2 s), as the GEMM kernels' waits do after about 2 s.  The
+ * next f4j_sync then returns F4J_ERR_TIMEOUT (message with code
+ * F4J_SELFTEST_WAIT_CODE), consumes the status, and the context stays usable. */
+int f4j_selftest_wait(f4j_ctx* ctx, int64_t limit_us);
 /* Run this context's work on an existing cudaStream_t (NULL = own stream). */
 int f4j_set_stream(f4j_ctx* ctx, void* cuda_stream);
 void* f4j_get_stream(f4j_ctx* ctx);
