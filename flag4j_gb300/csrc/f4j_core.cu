@@ -70,6 +70,14 @@ extern "C" int f4j_create(int device, f4j_ctx** out) {
         return f4j_cuda_fail(e, "cudaStreamCreate");
     }
     c->own_stream = true;
+    {   // keep freed pool memory for reuse by later calls (temporaries, CSR results)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    }
     e = cudaMalloc(&c->d_status, F4J_ST_WORDS * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, F4J_ST_WORDS * sizeof(int));
     if (e != cudaSuccess) {
@@ -295,7 +303,7 @@ extern "C" int f4j_buf_alloc(f4j_ctx* ctx, size_t bytes, f4j_buf* out) {
         cudaGetLastError();
         return f4j_fail(F4J_ERR_OOM, "device buffer of %zu bytes: %s", bytes, cudaGetErrorString(e));
     }
-    *out = new f4j_buf_s{p, bytes, true};
+    *out = new f4j_buf_s{p, bytes, true, false};
     return F4J_OK;
 }
 
@@ -328,7 +336,7 @@ extern "C" int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out)
         dev = ptr;
     }
     if (!dev) return f4j_fail(F4J_ERR_ARG, "the memory to wrap has no device address");
-    *out = new f4j_buf_s{dev, bytes, false};
+    *out = new f4j_buf_s{dev, bytes, false, false};
     return F4J_OK;
 }
 
@@ -336,9 +344,21 @@ extern "C" int f4j_buf_free(f4j_ctx* ctx, f4j_buf b) {
     F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!b) return F4J_OK;
-    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (b->owned) cudaFree(b->ptr);
+    if (b->owned && b->pooled) {
+        F4J_CUDA(cudaFreeAsync(b->ptr, ctx->stream));  // after the work queued on it
+    } else {
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (b->owned) cudaFree(b->ptr);
+    }
     delete b;
+    return F4J_OK;
+}
+
+int f4j_buf_alloc_pooled(f4j_ctx* ctx, size_t bytes, f4j_buf* out) {
+    void* p = nullptr;
+    int rc = f4j_dev_alloc(ctx, bytes, &p);
+    if (rc) return rc;
+    *out = new f4j_buf_s{p, bytes, true, true};
     return F4J_OK;
 }
 

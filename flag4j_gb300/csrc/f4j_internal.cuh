@@ -15,8 +15,13 @@
 struct f4j_buf_s {
     void* ptr;
     size_t bytes;
-    bool owned;  // false for f4j_buf_wrap handles
+    bool owned;   // false for f4j_buf_wrap handles
+    bool pooled;  // from the stream-ordered pool (library-made results): freed on the context stream
 };
+
+// A library-made result buffer from the stream-ordered pool, ordered on the
+// context stream (what the library returns inside handles, e.g. CSR results).
+int f4j_buf_alloc_pooled(f4j_ctx* ctx, size_t bytes, f4j_buf* out);
 
 struct f4j_csr_s {
     int64_t rows, cols, nnz;

@@ -976,9 +976,9 @@ extern "C" int f4j_csr_buffers(f4j_csr S, f4j_buf* rowptr, f4j_buf* colidx, f4j_
 
 static int alloc_owned_csr(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_t nnz, f4j_csr* out, int vw = 1) {
     f4j_buf rp = nullptr, ci = nullptr, v = nullptr;
-    int rc = f4j_buf_alloc(ctx, (size_t)(rows + 1) * 4, &rp);
-    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 4, &ci);
-    if (!rc) rc = f4j_buf_alloc(ctx, (size_t)nnz * 8 * vw, &v);
+    int rc = f4j_buf_alloc_pooled(ctx, (size_t)(rows + 1) * 4, &rp);
+    if (!rc) rc = f4j_buf_alloc_pooled(ctx, (size_t)nnz * 4, &ci);
+    if (!rc) rc = f4j_buf_alloc_pooled(ctx, (size_t)nnz * 8 * vw, &v);
     if (rc) {
         f4j_buf_free(ctx, rp);
         f4j_buf_free(ctx, ci);
