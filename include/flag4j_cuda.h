@@ -144,8 +144,9 @@ int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
  * call returns when C is in host memory.  A split product with opA = N runs
  * as row parts of C on their own streams so that C's download overlaps the
  * later parts' products; the result is bitwise the f4j_dgemm result.  This is
- * the entry a JVM binding calls with its arrays' native copies; Flag4j's
- * Matrix.mult(Matrix) has the same arguments and result. */
+ * the entry a JVM binding calls with its arrays' native copies for Flag4j's
+ * Matrix.mult(Matrix) (src/main/java/org/flag4j/arrays/dense/Matrix.java:638-640),
+ * same arguments and result. */
 int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
                    int opB, double* C, int mode, f4j_report* report);
 
