@@ -530,3 +530,33 @@ def test_one_context_shared_by_threads(f4j, oracle):
     assert not errors, errors
     for i in range(4):
         assert np.array_equal(results[i], refs[i])
+
+
+@pytest.mark.parametrize("n", [96, 300])
+def test_symm_pos_def_product_chain(f4j, oracle, n):
+    """RandomDenseTensor.randomSymmPosDefMatrix (RandomDenseTensor.java:649-653) forms
+    Q.T().mult(D).mult(Q) from a random diagonal D and orthogonal Q: two chained products whose
+    intermediate stays a device handle. Q and D come from a seeded generator here (the reference's
+    own generator is not reproducible from its seed)."""
+    rng = np.random.default_rng(n)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    D = np.diag(rng.random(n))
+    got = f4j.Matrix(Q).T().mult(f4j.Matrix(D), mode="exact").mult(f4j.Matrix(Q), mode="exact").toNumpy()
+    ref = oracle.dgemm(oracle.dgemm(np.ascontiguousarray(Q.T), D), Q)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+    assert np.all(np.linalg.eigvalsh((got + got.T) / 2) > -1e-12)
+
+
+@pytest.mark.parametrize("n", [64, 200])
+def test_herm_pos_def_product_chain(f4j, oracle, n):
+    """RandomDenseTensor.randomHermPosDefMatrix (RandomDenseTensor.java:666-670) forms
+    U.H().mult(D).mult(U): a Complex128 x real product (CMatrix.mult(Matrix)) followed by a
+    Complex128 product, each bit-identical to the oracle's k-ascending restatement."""
+    rng = np.random.default_rng(1000 + n)
+    U, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    D = np.diag(rng.random(n))
+    UH = np.ascontiguousarray(U.conj().T)
+    got = f4j.CMatrix(U).H().mult(f4j.Matrix(D), mode="exact").mult(f4j.CMatrix(U), mode="exact").toNumpy()
+    ref = oracle.zgemm(oracle.zgemm(UH, D.astype(np.complex128)), U)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+    assert np.max(np.abs(got - got.conj().T)) < 1e-13
