@@ -495,3 +495,50 @@ def test_complex_csr_csr_bit_identical(f4j, oracle, ak, bk):
     assert np.array_equal(_bits(S.data.view(np.float64)), _bits(v.view(np.float64)))
     with pytest.raises(f4j.LinearAlgebraException):
         A.mult(A)
+
+
+def _adversarial_values(rng, n, specials):
+    """Doubles that stress a multiply-then-add chain's rounding: short significands (exact
+    ties), N(0,1), magnitudes near overflow and underflow (products and sums leave the normal
+    range), subnormals, signed zeros and, with specials, infinities and NaNs."""
+    kind = rng.integers(0, 7, n)
+    out = rng.standard_normal(n)
+    k = kind == 0
+    out[k] = rng.integers(-4096, 4097, k.sum()) * np.exp2(rng.integers(-30, 31, k.sum()))
+    k = kind == 1
+    out[k] = rng.uniform(-2, 2, k.sum()) * np.exp2(rng.integers(480, 1023, k.sum()))
+    k = kind == 2
+    out[k] = rng.uniform(-2, 2, k.sum()) * np.exp2(rng.integers(-1040, -480, k.sum()))
+    k = kind == 3
+    out[k] = rng.choice([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.0, -1.0], k.sum())
+    k = kind == 4
+    out[k] = (1.0 + rng.integers(0, 8, k.sum()) * 2.0 ** -52) * rng.choice([-1.0, 1.0], k.sum())
+    if specials:
+        k = rng.random(n) < 0.01
+        out[k] = rng.choice([np.inf, -np.inf, np.nan], k.sum())
+    return out
+
+
+def _same_bits(a, b):
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint64), b[~nb].view(np.uint64))
+
+
+@pytest.mark.parametrize("specials", [False, True])
+@pytest.mark.parametrize("ncols", [3, 32, 64])
+def test_spmm_exact_rounding_adversarial_operands(f4j, oracle, specials, ncols):
+    """Exact mode on operands whose products and sums round at ties, cancel, overflow, underflow
+    and meet signed zeros and special values: every output, signed zeros included, matches the
+    oracle's multiply-then-add chain bit for bit (NaN where the oracle has NaN), for S X and
+    S^T X, with the 2-column (128-bit load) and 1-column kernels."""
+    from flag4j_gb300 import synth
+    rows = cols = 3000
+    rng = np.random.default_rng(ncols + 100 * specials)
+    rp, ci, _ = synth.csr_poisson(rows, cols, lam=12.0, hi=64, seed=ncols)
+    v = _adversarial_values(rng, len(ci), specials)
+    X = _adversarial_values(rng, cols * ncols, specials).reshape(cols, ncols)
+    X[1::7] = -X[0:-1:7]  # rows that cancel against their neighbours
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    assert _same_bits(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X))
+    trp, tci, tv, _ = oracle.csr_transpose(rows, cols, rp, ci, v)
+    assert _same_bits(S.multTransposeLeft(f4j.Matrix(X)).toNumpy(), oracle.spmm(trp, tci, tv, X))
