@@ -10,6 +10,6 @@ from ._lib import Flag4jDeviceException, load as load_library  # noqa: F401
 from .adjoint import MatMulNode, SpMMNode  # noqa: F401
 from .arrays import CMatrix, CooMatrix, CsrCMatrix, CsrMatrix, CVector, Matrix, Shape, Vector  # noqa: F401
 from .device import (Context, IllegalArgumentException, LinearAlgebraException, default_context,  # noqa: F401
-                     gemm_mode, set_gemm_mode)
+                     gemm_mode, pinned_empty, set_gemm_mode)
 
 __version__ = "0.1.0"

@@ -68,6 +68,8 @@ SIGNATURES = {
     "f4j_buf_download_async": (_i, [_v, _v, _v, _sz, _sz]),
     "f4j_buf_zero": (_i, [_v, _v]),
     "f4j_host_register": (_i, [_v, _sz]),
+    "f4j_host_alloc": (_i, [_sz, ctypes.POINTER(ctypes.c_void_p)]),
+    "f4j_host_free": (_i, [_v]),
     "f4j_host_unregister": (_i, [_v]),
     "f4j_dgemm": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),
     "f4j_dgemm_host": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),

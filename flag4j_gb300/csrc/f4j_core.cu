@@ -429,6 +429,20 @@ extern "C" int f4j_host_unregister(void* host) {
     return F4J_OK;
 }
 
+extern "C" int f4j_host_alloc(size_t bytes, void** out) {
+    if (!out) return f4j_fail(F4J_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!bytes) return f4j_fail(F4J_ERR_ARG, "zero-byte host allocation");
+    F4J_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocPortable));
+    return F4J_OK;
+}
+
+extern "C" int f4j_host_free(void* host) {
+    if (!host) return F4J_OK;
+    F4J_CUDA(cudaFreeHost(host));
+    return F4J_OK;
+}
+
 // ------------------------------------------------------------------ dense front ends
 static int check_gemm_args(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j_buf A,
                            int opA, f4j_buf B, int opB, f4j_buf C, int mode) {

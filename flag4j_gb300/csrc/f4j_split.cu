@@ -888,13 +888,14 @@ static int env_slices() {
     return (env && atoi(env) > 0) ? atoi(env) : 0;
 }
 
-// Levels per band in the slice GEMM's schedule (F4J_SPLIT_BAND, 1..4; default 4).
+// Row parts of a host-buffer split product (F4J_HOST_PARTS, 1..F4J_HOST_PARTS_MAX).
 static int env_host_parts() {
     const char* e = getenv("F4J_HOST_PARTS");
     const int v = e ? atoi(e) : F4J_HOST_PARTS;
     return v < 1 ? 1 : (v > F4J_HOST_PARTS_MAX ? F4J_HOST_PARTS_MAX : v);
 }
 
+// Levels per band in the slice GEMM's schedule (F4J_SPLIT_BAND, 1..4; default 4).
 static int env_band() {
     const char* env = getenv("F4J_SPLIT_BAND");
     const int b = env ? atoi(env) : 0;
@@ -1079,11 +1080,15 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 // ------------------------------------------------------------------ host buffers
 // C = op(A) op(B) from and to host memory (pinned for full copy speed).  For
 // a split product with op(A) = N and at least two tile rows, the slice GEMM
-// runs as F4J_HOST_PARTS launches over row parts of C on their own streams,
-// each followed by its part's gated DMMA fallback and download, so C's
-// download overlaps the later parts' products and each launch's CTAs fill the
-// previous launch's last wave.  Other products upload, multiply and download
-// in turn.  Returns when C is in host memory.
+// runs as F4J_HOST_PARTS launches over shrinking row parts of C on their own
+// streams, each followed by its part's download, so C's download overlaps the
+// other parts' products and each launch's CTAs fill another's last wave.  The
+// parts need not finish in order (the block scheduler interleaves the
+// streams); the small parts keep the exposed final download short.  The gated DMMA fallback (the product when an input is
+// not finite, an empty kernel otherwise) runs once before the parts: queued
+// after a part, its CTAs would wait behind the later parts' persistent CTAs,
+// and that part's download with them.  Other products upload, multiply and
+// download in turn.  Returns when C is in host memory.
 extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                               const double* B, int opB, double* C, int mode, f4j_report* rep) {
     F4J_LOCK(ctx);
@@ -1132,23 +1137,29 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
         F4J_CUDA(cudaEventCreateWithFlags(&ctx->ev_prep, cudaEventDisableTiming));
         ctx->parts_init = true;
     }
+    // the plain product when an input is not finite (the slice launches then return at once)
+    rc = f4j_gemm_dmma(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB, (double*)dC,
+                       &L.prm.plan->nonfinite);
+    if (rc) return rc;
     F4J_CUDA(cudaEventRecord(ctx->ev_prep, ctx->stream));
-    const int* gate = &L.prm.plan->nonfinite;
     int launched = 0;
+    // part p gets a share 2(parts - p) - 1 of the tile rows (7:5:3:1 for four):
+    // the last part's download is the one no product hides
+    int bound[F4J_HOST_PARTS_MAX + 1];
+    bound[0] = 0;
+    for (int p = 1, wsum = 0; p <= parts; p++) {
+        wsum += 2 * (parts - p) + 1;
+        const int b = (int)((int64_t)tiles_m * wsum / (parts * parts));  // the weights sum to parts^2
+        const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);      // every part at least one tile row
+        bound[p] = b < lo ? lo : (b > hi ? hi : b);
+    }
     for (int p = 0; p < parts && !rc; p++) {
-        const int tm0 = (int)((int64_t)tiles_m * p / parts), tm1 = (int)((int64_t)tiles_m * (p + 1) / parts);
+        const int tm0 = bound[p], tm1 = bound[p + 1];
         const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
         const cudaStream_t st = ctx->part_stream[p];
         F4J_CUDA(cudaStreamWaitEvent(st, ctx->ev_prep, 0));
         launched = p + 1;
         rc = split_launch(ctx, L, st, tm0, tm1);
-        if (!rc) {
-            const cudaStream_t saved = ctx->stream;
-            ctx->stream = st;
-            rc = f4j_gemm_dmma(ctx, false, r1 - r0, n, k, (const double*)dA + r0 * k, F4J_OP_N, (const double*)dB,
-                               opB, (double*)dC + r0 * n, gate);
-            ctx->stream = saved;
-        }
         if (!rc) {
             F4J_CUDA(cudaMemcpyAsync(C + r0 * n, (const double*)dC + r0 * n, (size_t)(r1 - r0) * n * 8,
                                      cudaMemcpyDeviceToHost, st));

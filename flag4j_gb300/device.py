@@ -9,6 +9,7 @@ structure -> IllegalArgumentException, device failures -> Flag4jDeviceException.
 import ctypes
 import os
 import threading
+import weakref
 
 import numpy as np
 
@@ -123,6 +124,22 @@ class Context:
         if self.handle is not None:
             self.lib.f4j_destroy(self.handle)
             self.handle = None
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """An uninitialised numpy array in page-locked host memory (f4j_host_alloc),
+    for the host-buffer entry points and async copies: on GB300 its copies run
+    at the host link's full rate.  The memory is freed (f4j_host_free) once the
+    array and every view of it are gone."""
+    lib = _lib.load()
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape, dtype=np.int64))
+    nbytes = max(count * dtype.itemsize, 1)
+    ptr = ctypes.c_void_p()
+    check(lib.f4j_host_alloc(nbytes, ctypes.byref(ptr)))
+    block = (ctypes.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(block, lib.f4j_host_free, ptr.value)
+    return np.frombuffer(block, dtype=dtype, count=count).reshape(shape)
 
 
 _default = None

@@ -429,19 +429,21 @@ def test_wrap_rejects_misaligned_and_null(f4j):
         check(ctx.lib.f4j_buf_wrap(ctx.handle, None, 64, ctypes.byref(h)))
 
 
-@pytest.mark.parametrize("m,n,k,mode,opA,pinned", [
-    (1000, 700, 900, "split", 0, True),     # 8 tile rows: four row parts
-    (300, 260, 520, "split", 0, False),     # 3 tile rows: three parts, pageable host memory
-    (130, 200, 300, "split", 0, True),      # 2 tile rows, the last ragged
-    (100, 90, 80, "split", 0, True),        # one tile row: no parts
-    (600, 500, 400, "split", 1, True),      # op(A) = T: uploaded, multiplied, downloaded in turn
-    (500, 300, 200, "plain", 0, True),
-    (64, 48, 40, "exact", 0, True),
+@pytest.mark.parametrize("m,n,k,mode,opA,host", [
+    (1000, 700, 900, "split", 0, "registered"),  # 8 tile rows: four shrinking row parts (3, 3, 1, 1)
+    (2500, 900, 700, "split", 0, "allocated"),   # 20 tile rows in f4j_host_alloc memory (8, 7, 3, 2)
+    (300, 260, 520, "split", 0, "pageable"),     # 3 tile rows: three parts, pageable host memory
+    (130, 200, 300, "split", 0, "registered"),   # 2 tile rows, the last ragged
+    (100, 90, 80, "split", 0, "allocated"),      # one tile row: no parts
+    (600, 500, 400, "split", 1, "registered"),   # op(A) = T: uploaded, multiplied, downloaded in turn
+    (500, 300, 200, "plain", 0, "registered"),
+    (64, 48, 40, "exact", 0, "allocated"),
 ])
-def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, pinned):
-    """f4j_dgemm_host is bitwise f4j_dgemm on the same operands."""
+def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, host):
+    """f4j_dgemm_host is bitwise f4j_dgemm on the same operands, from registered, pageable or
+    f4j_host_alloc host memory."""
     from flag4j_gb300 import _lib, synth
-    from flag4j_gb300.device import check
+    from flag4j_gb300.device import check, pinned_empty
     ctx = f4j.default_context()
     A = synth.scaled(m, k, 4, 21, "row") if opA == 0 else synth.scaled(k, m, 4, 21, "col")
     B = synth.scaled(k, n, 4, 22, "col")
@@ -449,7 +451,12 @@ def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, pinned):
     check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, 0, dC.handle, _lib.MODES[mode], None))
     ref = dC.to_numpy(np.float64, m * n).reshape(m, n)
     C = np.full((m, n), np.nan)
+    if host == "allocated":
+        pa, pb, pc = pinned_empty(A.shape), pinned_empty(B.shape), pinned_empty(C.shape)
+        pa[...], pb[...], pc[...] = A, B, C
+        A, B, C = pa, pb, pc
     arrays = (A, B, C)
+    pinned = host == "registered"
     if pinned:
         for a in arrays:
             check(ctx.lib.f4j_host_register(a.ctypes.data, a.nbytes))
