@@ -128,6 +128,7 @@ struct SplitGemmParams {
     int* status;
     const SplitPlan* plan;
     int tm0, tm1;           // the launch covers tile rows [tm0, tm1) of C
+    long long* wpart;       // split K: per-chunk int64 sums [nchunks][M][N] (null: whole tiles)
 };
 
 // ------------------------------------------------------------------ stats
@@ -170,13 +171,13 @@ __global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t
     }
 }
 
-// Thread per stored column, blockIdx.y over 256-row chunks: stats of stored columns.
-__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
+// Thread per stored column, blockIdx.y over chunks of `chunk` rows: stats of stored columns.
+__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx, int chunk,
                              unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
                              int* __restrict__ cnt_out, int* __restrict__ bad_out) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cols) return;
-    int64_t r0 = (int64_t)blockIdx.y * 256, r1 = r0 + 256 < rows ? r0 + 256 : rows;
+    int64_t r0 = (int64_t)blockIdx.y * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
     unsigned long long mx = 0;
     long long es = 0;
     int cnt = 0, bad = 0;
@@ -245,14 +246,17 @@ __host__ __device__ inline int slices_for(double spread, int64_t k) {
 // (<= NBUF) levels, the lowest band taking the remainder; each band's A-slice range is cut into chunks of
 // w = (STAGE_TILES - band + 1) / 2 slices, one group each, so a group loads
 // at most 2w + band - 1 <= STAGE_TILES tiles per K block.  Returns the
-// number of rounds per chunk, or -1 if a table would overflow.
-__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int band = NBUF) {
+// number of rounds per chunk, or -1 if a table would overflow.  kcb_cap > 0
+// bounds the chunk (split K for products with few output tiles).
+__host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, SplitPlan* P, int band = NBUF,
+                                          int kcb_cap = 0) {
     if (band < 1) band = 1;
     if (band > NBUF) band = NBUF;
     const int w = (STAGE_TILES - band + 1) / 2;
     const int64_t nkb = Kp / BKB;
     int64_t kcb = 1;
-    while (2 * kcb <= nkb && (int64_t)s * (2 * kcb) * BKB * 256 <= (1ll << 24)) kcb *= 2;
+    while (2 * kcb <= nkb && (int64_t)s * (2 * kcb) * BKB * 256 <= (1ll << 24) && (kcb_cap <= 0 || 2 * kcb <= kcb_cap))
+        kcb *= 2;
     P->nkb = (int)nkb;
     P->kcb = (int)kcb;
     int kbits = 0;
@@ -354,11 +358,11 @@ __host__ __device__ inline int plan_build(int s, int64_t Kp, int64_t klen_cat, S
 // One thread: slice count and the group / round / MMA program from the
 // statistics.  misc: [0] non-finite flag, [1] spread of A x256, [2] of B.
 __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int64_t klen_cat, int s_req,
-                       int band, SplitPlan* __restrict__ plan) {
+                       int band, int kcb_cap, SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
     int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
-    int n = plan_build(s, Kp, klen_cat, plan, band);
+    int n = plan_build(s, Kp, klen_cat, plan, band, kcb_cap);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
     plan->spread = (float)spread;
@@ -600,6 +604,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // per ring slot, the ops with absolute descriptor low words and TMEM addresses
     Op* opx = reinterpret_cast<Op*>(reinterpret_cast<unsigned char*>(sp) + sizeof(SplitPlan));
     const int nkb = plan->nkb, kcb = plan->kcb, nchunks = (nkb + kcb - 1) / kcb;
+    // split K (p.wpart): a unit is one K chunk of one tile; else a whole tile
+    const bool ksplit = p.wpart != nullptr;
+    const int nunits = ksplit ? ntiles * nchunks : ntiles;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -640,11 +647,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 #endif
             int st = 0;  // stages issued, carried across tiles
             bool ok = true;
-            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+                const int tile = ksplit ? u / nchunks : u;
+                const int kc0 = ksplit ? (u % nchunks) * kcb : 0, kc1 = ksplit ? kc0 + kcb : nkb;
                 int m0, n0;
                 tile_origin(tile, tiles_m, tiles_n, m0, n0);
-        m0 += p.tm0 * BM;
-                for (int kc = 0; kc < nkb && ok; kc += kcb) {
+                m0 += p.tm0 * BM;
+                for (int kc = kc0; kc < kc1 && kc < nkb && ok; kc += kcb) {
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
                     for (int g = 0; g < ngroups && ok; g++) {
                         const Group G = gp[g];
@@ -699,8 +708,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             int st = 0;             // stages consumed, carried across tiles
             uint32_t used = 0;      // bit b: buffer b has been filled before
             uint32_t drained = 0;   // bit b: parity of the next accempty[b] phase to wait for
-            for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&abort_flag; tile += gridDim.x) {
-                for (int kc = 0; kc < nkb && !*(volatile int*)&abort_flag; kc += kcb) {
+            for (int u = blockIdx.x; u < nunits && !*(volatile int*)&abort_flag; u += gridDim.x) {
+                const int kc0 = ksplit ? (u % nchunks) * kcb : 0, kc1 = ksplit ? kc0 + kcb : nkb;
+                for (int kc = kc0; kc < kc1 && kc < nkb && !*(volatile int*)&abort_flag; kc += kcb) {
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
                     for (int g = 0; g < ngroups && !*(volatile int*)&abort_flag; g++) {
                         const Group G = gp[g];
@@ -771,7 +781,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         unsigned long long tr_wait = 0;
         const long long tr_start = clock64();
 #endif
-        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int tile = ksplit ? u / nchunks : u;
         int m0, n0;
         tile_origin(tile, tiles_m, tiles_n, m0, n0);
         m0 += p.tm0 * BM;
@@ -782,7 +793,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         bool ok = true;
         // the round program repeats once per K chunk; the rounds of a band
         // complete together, in round order
-        for (int rr = 0; rr < nchunks * nrounds; rr++) {
+        for (int rr = 0; rr < (ksplit ? 1 : nchunks) * nrounds; rr++) {
             const Round R = sp->rounds[rr % nrounds];
             const int buf = R.buf;
             bool w = true;
@@ -822,7 +833,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             if (lane == 0) mbar_arrive(&accempty[buf]);
         }
         if (!ok) break;
-        if (row < p.M) {
+        if (ksplit) {
+            // the chunk's exact sums; k_split_fixup adds the chunks and scales
+            if (row < p.M) {
+                long long* dst = p.wpart + ((int64_t)(u % nchunks) * p.M + row) * p.N;
+#pragma unroll
+                for (int c = 0; c < EPI_COLS; c += 2) {
+                    const int col = n0 + h * EPI_COLS + c;
+                    if (col + 1 < p.N && ((reinterpret_cast<uintptr_t>(dst + col) & 15) == 0)) {
+                        *reinterpret_cast<longlong2*>(dst + col) = make_longlong2(acc[c], acc[c + 1]);
+                    } else {
+                        if (col < p.N) dst[col] = acc[c];
+                        if (col + 1 < p.N) dst[col + 1] = acc[c + 1];
+                    }
+                }
+            }
+        } else if (row < p.M) {
             const int ea = p.ea[row];
 #pragma unroll
             for (int c = 0; c < EPI_COLS; c += 2) {
@@ -862,6 +888,26 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, NBUF * BN);
+    }
+}
+
+// Split K: each C entry is the sum of its tile's chunk sums (exact in int64,
+// so equal to one CTA accumulating the chunks in turn), converted and scaled as
+// the slice GEMM's epilogue does.
+__global__ void __launch_bounds__(256) k_split_fixup(const __grid_constant__ SplitGemmParams p, int nchunks) {
+    if (p.plan->nonfinite) return;  // the gated plain path computes this product
+    const int64_t mn = (int64_t)p.M * p.N;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= mn) return;
+    const int row = (int)(idx / p.N), col = (int)(idx % p.N);
+    long long acc = 0;
+    for (int c = 0; c < nchunks; c++) acc += p.wpart[(int64_t)c * mn + idx];
+    const double v = scale_pow2((double)acc, p.plan->ubits + p.ea[row] + p.eb[col]);
+    if (!p.cplx) {
+        p.C[idx] = v;
+    } else {
+        const int jn = col < p.n_out ? col : col - p.n_out;
+        p.C[2 * ((int64_t)row * p.n_out + jn) + (col < p.n_out ? 0 : 1)] = v;
     }
 }
 
@@ -916,7 +962,50 @@ struct SplitLaunch {
     CUtensorMap ta, tb;
     SplitGemmParams prm;
     int tiles_m, tiles_n;
+    int kchunks;  // split K: chunks per tile, each a work unit (0: whole tiles)
 };
+
+// Split K for products with few output tiles.  The K chunk (a power of two of
+// K blocks) minimising waves x (chunk + 1) over SPLIT_UNITS work units is a
+// function of the shape alone, so every path that plans this product (device,
+// host buffers, no-allocation) gets the same chunks and the same bits; split
+// or not, a tile's int64 sum over its chunks is the same number.  Only for
+// K <= 64 blocks, where the chunk the FP32 exactness budget allows is the
+// largest power of two <= the block count for every slice count.  Returns the
+// chunk cap for the planner (0: none) and, in *nchunks, the chunk count when
+// the product runs split (0 otherwise).
+static_assert(S_MAX * 64 * BKB * 256 <= (1 << 24), "64-block chunks fit the FP32 budget for every slice count");
+constexpr int64_t SPLIT_UNITS = 152;
+static int split_kcb_cap(int64_t tiles, int64_t nkb, int* nchunks) {
+    *nchunks = 0;
+    if (tiles >= SPLIT_UNITS || nkb < 2 || nkb > 64) return 0;
+    int64_t nat = 1;
+    while (2 * nat <= nkb) nat *= 2;
+    int64_t best = nat, best_cost = INT64_MAX;
+    for (int64_t kcb = nat; kcb >= 1; kcb /= 2) {
+        const int64_t cost = f4j_cdiv(tiles * f4j_cdiv(nkb, kcb), SPLIT_UNITS) * (kcb + 1);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = kcb;
+        }
+    }
+    const int64_t nch = f4j_cdiv(nkb, best);
+    if (nch >= 2) *nchunks = (int)nch;
+    return (int)best;
+}
+
+// Column statistics of a stored rows x cols operand.  Row chunks of 256, halved
+// (down to 16) while the grid has fewer than four blocks per SM: a 1024-wide
+// operand otherwise runs as 16 blocks.  The chunk count stays within grid.y.
+static void launch_stats_cols(const double* X, int64_t rows, int64_t cols, int cplx, int sm_count,
+                              unsigned long long* mx, long long* es, int* cn, int* bad, cudaStream_t st) {
+    const int64_t bx = f4j_cdiv(cols, 256);
+    int64_t chunk = 256;
+    while (chunk > 16 && bx * f4j_cdiv(rows, chunk) < 4 * (int64_t)sm_count) chunk /= 2;
+    while (f4j_cdiv(rows, chunk) > 65535) chunk *= 2;
+    k_stats_cols<<<dim3((unsigned)bx, (unsigned)f4j_cdiv(rows, chunk)), 256, 0, st>>>(X, rows, cols, cplx, (int)chunk,
+                                                                                      mx, es, cn, bad);
+}
 
 static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                          const double* B, int opB, double* C, int slices_req, SplitLaunch* L) {
@@ -938,7 +1027,10 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     void *ws1, *ws0;
     int rc = f4j_workspace(ctx, ctx->ws_base + 1, small_bytes, &ws1);
     if (rc) return rc;
-    rc = f4j_workspace(ctx, ctx->ws_base, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX), &ws0);
+    int kchunks = 0;
+    const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks);
+    const size_t wpart_bytes = kchunks ? (size_t)kchunks * M * N * 8 : 0;  // split K: chunk sums
+    rc = f4j_workspace(ctx, ctx->ws_base, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX) + wpart_bytes, &ws0);
     if (rc) return rc;
     char* w = (char*)ws1;
     unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
@@ -963,15 +1055,13 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     if (a_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
     } else {
-        dim3 g((unsigned)f4j_cdiv(M, 256), (unsigned)f4j_cdiv(k, 256));
-        k_stats_cols<<<g, 256, 0, ctx->stream>>>(A, k, M, cplx, mxa, esa, cna, misc);
+        launch_stats_cols(A, k, M, cplx, ctx->sm_count, mxa, esa, cna, misc, ctx->stream);
     }
     F4J_LAUNCHED(ctx);
     if (b_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, ctx->stream>>>(B, n, k, cplx, mxb, esb, cnb, misc);
     } else {
-        dim3 g((unsigned)f4j_cdiv(n, 256), (unsigned)f4j_cdiv(k, 256));
-        k_stats_cols<<<g, 256, 0, ctx->stream>>>(B, k, n, cplx, mxb, esb, cnb, misc);
+        launch_stats_cols(B, k, n, cplx, ctx->sm_count, mxb, esb, cnb, misc, ctx->stream);
     }
     F4J_LAUNCHED(ctx);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, ctx->stream>>>(M, 0, mxa, esa, cna, ea, misc + 1);
@@ -980,7 +1070,7 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
     k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(),
-                                      env_band(), plan);
+                                      env_band(), kcb_cap, plan);
     F4J_LAUNCHED(ctx);
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
@@ -1015,8 +1105,10 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     prm.plan = plan;
     prm.tm0 = 0;
     prm.tm1 = (int)f4j_cdiv(M, BM);
+    prm.wpart = kchunks ? reinterpret_cast<long long*>(slB + al1k(plane_b * S_MAX)) : nullptr;
     L->tiles_m = prm.tm1;
     L->tiles_n = (int)f4j_cdiv(N, BN);
+    L->kchunks = kchunks;
     return F4J_OK;
 }
 
@@ -1028,12 +1120,18 @@ static int split_launch(f4j_ctx* ctx, const SplitLaunch& L, cudaStream_t stream,
     const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
-    const int64_t ntiles = (int64_t)L.tiles_n * (tm1 - tm0);
-    const unsigned grid = (unsigned)(ntiles < ctx->sm_count ? ntiles : ctx->sm_count);
+    const bool ksplit = prm.wpart != nullptr;
+    if (ksplit && (tm0 != 0 || tm1 != L.tiles_m)) return f4j_fail(F4J_ERR_ARG, "split-K slice GEMM over a row part");
+    const int64_t nunits = (int64_t)L.tiles_n * (tm1 - tm0) * (ksplit ? L.kchunks : 1);
+    const unsigned grid = (unsigned)(nunits < ctx->sm_count ? nunits : ctx->sm_count);
     const cudaStream_t saved = ctx->stream;
     ctx->stream = stream;
     f4j_prof_begin(ctx);
     k_split_gemm<<<grid, GEMM_THREADS, smem, stream>>>(L.ta, L.tb, prm);
+    if (ksplit) {
+        k_split_fixup<<<(unsigned)f4j_cdiv((int64_t)prm.M * prm.N, 256), 256, 0, stream>>>(prm, L.kchunks);
+        ctx->launches++;
+    }
     f4j_prof_end(ctx);
     ctx->stream = saved;
     e = cudaGetLastError();
@@ -1117,7 +1215,9 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     const int tiles_m = (int)f4j_cdiv(m, BM);
     const int want = env_host_parts();
     const int parts = tiles_m < want ? tiles_m : want;
-    if (!split || opA != F4J_OP_N || parts < 2) {
+    int kchunks = 0;
+    split_kcb_cap(tiles_m * f4j_cdiv(n, BN), f4j_cdiv(k, BKB), &kchunks);
+    if (!split || opA != F4J_OP_N || parts < 2 || kchunks) {  // split K runs as one launch
         rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,
                            rep);
         if (rc) return rc;
@@ -1269,15 +1369,18 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, st));
 
     const bool a_rows = (opA == F4J_OP_N), b_rows = (opB != F4J_OP_N);
+    int cur = 0, smc = 0;
+    F4J_CUDA(cudaGetDevice(&cur));
+    F4J_CUDA(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, cur));
     if (a_rows) k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, st>>>(A, M, k, 0, mxa, esa, cna, misc);
-    else k_stats_cols<<<dim3((unsigned)f4j_cdiv(M, 256), (unsigned)f4j_cdiv(k, 256)), 256, 0, st>>>(A, k, M, 0, mxa,
-                                                                                                 esa, cna, misc);
+    else launch_stats_cols(A, k, M, 0, smc, mxa, esa, cna, misc, st);
     if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(N, 8), 256, 0, st>>>(B, N, k, 0, mxb, esb, cnb, misc);
-    else k_stats_cols<<<dim3((unsigned)f4j_cdiv(N, 256), (unsigned)f4j_cdiv(k, 256)), 256, 0, st>>>(B, k, N, 0, mxb,
-                                                                                                 esb, cnb, misc);
+    else launch_stats_cols(B, k, N, 0, smc, mxb, esb, cnb, misc, st);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
-    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_band(), plan);
+    int kchunks_na = 0;  // the same chunks as f4j_dgemm plans for this shape, run in turn
+    const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks_na);
+    k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_band(), kcb_cap, plan);
     F4J_CUDA(cudaGetLastError());
     // NaN/Inf operands are rejected, so wait for the plan's verdict
     int hp[4];

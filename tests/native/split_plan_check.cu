@@ -7,7 +7,8 @@
 // that each round respects the exact-FP32 budget s * kchunk * 256 <= 2^24,
 // that continuation chains between groups are well formed, and that within a
 // band every TMEM buffer is acquired once before its first MMA and released
-// once after its last.  Exit status 0 on
+// once after its last, and that the split-K chunk cap for products with few
+// output tiles yields the chunk count the host expects.  Exit status 0 on
 // success.  Launches no kernel.
 #include "../../flag4j_gb300/csrc/f4j_split.cu"
 #include <cstdio>
@@ -78,6 +79,24 @@ int main() {
       if (seen.count(i * 64 + j) != 1) { printf("coverage (%d,%d) x%zu s=%d band=%d\n", i, j, seen.count(i*64+j), s, band); bad++; }
     }
     if ((long long)seen.size() != expect) { printf("coverage size\n"); bad++; }
+  }
+  // split K for few output tiles: the planner's chunk under the host's cap gives
+  // exactly the chunk count the host sized the work units and workspace for,
+  // for every slice count; many tiles or K > 64 blocks leave the plan alone
+  for (long long tiles : {1LL, 8LL, 48LL, 64LL, 100LL, 151LL, 152LL, 4096LL})
+  for (long long K : {64LL, 100LL, 128LL, 512LL, 1000LL, 1024LL, 1536LL, 2048LL, 4096LL, 4097LL, 8192LL}) {
+    long long Kp = (K + BKB - 1) / BKB * BKB, nkb = Kp / BKB;
+    int nch = 0;
+    const int cap = split_kcb_cap(tiles, nkb, &nch);
+    if ((tiles >= SPLIT_UNITS || nkb > 64) && (cap || nch)) { printf("split K outside its range\n"); bad++; }
+    for (int s = 2; s <= 12; s++) {
+      plan_build(s, Kp, K, &P, NBUF, cap);
+      const long long pch = (P.nkb + P.kcb - 1) / P.kcb;
+      if (cap && P.kcb != cap) { printf("chunk %d != cap %d (tiles %lld K %lld s %d)\n", P.kcb, cap, tiles, K, s); bad++; }
+      if (nch && pch != nch) { printf("chunks %lld != %d\n", pch, nch); bad++; }
+      if (cap && !nch && pch != 1) { printf("unsplit plan with %lld chunks\n", pch); bad++; }
+    }
+    if (tiles == 64 && K == 1024) printf("1024^3 (64 tiles, 16 K blocks): chunk %d blocks, %d chunks\n", cap, nch);
   }
   // ops per loaded tile for the default band
   for (int s : {8, 10, 11, 12}) {
