@@ -114,6 +114,8 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
     }
     for (int i = 0; i < 8; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
+    for (int i = 0; i < 2; i++)
+        if (ctx->plan_tab[i]) cudaFree(ctx->plan_tab[i]);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     lock.unlock();

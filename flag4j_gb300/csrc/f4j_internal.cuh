@@ -58,6 +58,11 @@ struct f4j_ctx {
     // Streams of the row parts of a host-buffer GEMM (f4j_dgemm_host), created on first use.
     cudaStream_t part_stream[F4J_HOST_PARTS_MAX];
     cudaEvent_t part_ev[F4J_HOST_PARTS_MAX], ev_prep;
+    // Split GEMM plans for every slice count, per workspace base (0 / 4), built
+    // when the key (Kp, K length, band, chunk cap) changes.
+    void* plan_tab[2];
+    long long plan_key[2][4];
+    bool plan_valid[2];
     bool parts_init;
     int* d_status;     // device status words (bounded-wait timeouts, validation)
     cudaEvent_t ev[16];

@@ -22,6 +22,7 @@
 // so one real product of size m x 2n x 2k gives [Cr | Ci] (the four real
 // products of Complex128.mult, src/main/java/org/flag4j/numbers/Complex128.java:336-341).
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -368,6 +369,37 @@ __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int6
     plan->spread = (float)spread;
     // a plan that does not fit is treated like a non-finite input (plain path)
     plan->nonfinite = (misc[0] != 0 || n < 0) ? 1 : 0;
+}
+
+// The plan of every slice count s = 2..S_MAX (block s - 2, one thread each):
+// tab[s] for a context's plan table.  nrounds < 0 marks a plan that does not fit.
+__global__ void k_plan_table(int64_t Kp, int64_t klen_cat, int band, int kcb_cap, SplitPlan* __restrict__ tab) {
+    if (threadIdx.x != 0) return;
+    const int s = 2 + (int)blockIdx.x;
+    SplitPlan* P = &tab[s];
+    const int n = plan_build(s, Kp, klen_cat, P, band, kcb_cap);
+    P->s = s;
+    P->nrounds = n;
+}
+
+// One warp: k_plan's result from a plan table (the slice count from the
+// statistics, that plan copied, the header filled in).
+__global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int s_req, const SplitPlan* __restrict__ tab,
+                            SplitPlan* __restrict__ plan) {
+    if (blockIdx.x != 0) return;
+    const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
+    const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
+    const uint4* src = reinterpret_cast<const uint4*>(&tab[s]);
+    uint4* dst = reinterpret_cast<uint4*>(plan);
+    for (int i = threadIdx.x; i < (int)(sizeof(SplitPlan) / 16); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int n = tab[s].nrounds;
+        plan->s = s;
+        plan->nrounds = n < 0 ? 0 : n;
+        plan->spread = (float)spread;
+        plan->nonfinite = (misc[0] != 0 || n < 0) ? 1 : 0;
+    }
 }
 
 // ------------------------------------------------------------------ split
@@ -1069,9 +1101,24 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
                                                                           misc + 2);
     F4J_LAUNCHED(ctx);
-    k_plan<<<1, 32, 0, ctx->stream>>>(misc, k, Kp, klen_cat, slices_req > 0 ? slices_req : env_slices(),
-                                      env_band(), kcb_cap, plan);
-    F4J_LAUNCHED(ctx);
+    {   // the plan: from the context's table of plans for every slice count,
+        // rebuilt when the key changes (the one-thread build takes ~10 us)
+        const int t = ctx->ws_base ? 1 : 0;
+        const long long key[4] = {(long long)Kp, (long long)klen_cat, (long long)env_band(), (long long)kcb_cap};
+        if (!ctx->plan_tab[t]) {
+            F4J_CUDA(cudaMalloc(&ctx->plan_tab[t], (size_t)(S_MAX + 1) * sizeof(SplitPlan)));
+            ctx->plan_valid[t] = false;
+        }
+        SplitPlan* tab = (SplitPlan*)ctx->plan_tab[t];
+        if (!ctx->plan_valid[t] || memcmp(key, ctx->plan_key[t], sizeof key) != 0) {
+            k_plan_table<<<S_MAX - 1, 32, 0, ctx->stream>>>(Kp, klen_cat, (int)key[2], kcb_cap, tab);
+            F4J_LAUNCHED(ctx);
+            memcpy(ctx->plan_key[t], key, sizeof key);
+            ctx->plan_valid[t] = true;
+        }
+        k_plan_pick<<<1, 32, 0, ctx->stream>>>(misc, k, slices_req > 0 ? slices_req : env_slices(), tab, plan);
+        F4J_LAUNCHED(ctx);
+    }
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
         dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
         k_split<<<g, 256, 0, ctx->stream>>>(A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, cplx,
