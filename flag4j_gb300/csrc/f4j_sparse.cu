@@ -289,11 +289,49 @@ __global__ void k_count(int64_t n, const int* __restrict__ idx, int* __restrict_
         atomicAdd(&counts_plus1[idx[i] + 1], 1);
 }
 
-// Range check of COO indices: records the first offending position.
-__global__ void k_check_range(int64_t n, const int* __restrict__ idx, int64_t limit, int* __restrict__ first_bad) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int v = idx[i];
+// COO -> CSR row count with the row range check of SparseValidation.validateCoo:
+// one count per in-range row index in counts_plus1[r + 1], and the first
+// position of an out-of-range one in *first_bad.  Lanes of a warp holding the
+// same row add together (COO input is usually row-sorted, so a warp's 32
+// entries fall in a few rows).
+__global__ void k_count_rows_checked(int64_t n, const int* __restrict__ idx, int64_t limit,
+                                     int* __restrict__ counts_plus1, int* __restrict__ first_bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = ((int64_t)gridDim.x * blockDim.x) & ~(int64_t)31;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~(int64_t)31; base < n; base += stride) {
+        const int64_t i = base + lane;
+        const bool in = i < n;
+        const int v = in ? idx[i] : -1;
+        const bool ok = in && v >= 0 && v < limit;
+        if (in && !ok) atomicMin(first_bad, (int)i);
+        const unsigned peers = __match_any_sync(0xffffffffu, ok ? v : -1);
+        if (ok && lane == __ffs(peers) - 1) atomicAdd(&counts_plus1[v + 1], __popc(peers));
+    }
+}
+
+// Copy of COO column indices into the CSR with the column range check:
+// the first offending position in *first_bad.  VEC: 16-byte loads and stores.
+template <bool VEC>
+__global__ void k_copy_cols_checked(int64_t n, const int* __restrict__ src, int64_t limit, int* __restrict__ dst,
+                                    int* __restrict__ first_bad) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t done = 0;
+    if (VEC) {
+        const int64_t n4 = n / 4;
+        for (int64_t j = t; j < n4; j += stride) {
+            const int4 v = reinterpret_cast<const int4*>(src)[j];
+            const int e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (e[q] < 0 || e[q] >= limit) atomicMin(first_bad, (int)(4 * j + q));
+            reinterpret_cast<int4*>(dst)[j] = v;
+        }
+        done = 4 * n4;
+    }
+    for (int64_t i = done + t; i < n; i += stride) {
+        const int v = src[i];
         if (v < 0 || v >= limit) atomicMin(first_bad, (int)i);
+        dst[i] = v;
     }
 }
 
@@ -1004,36 +1042,32 @@ extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_
     if ((int64_t)rows * cols < nnz)
         return f4j_fail(F4J_ERR_CSR, "The number of non-zero entries cannot be greater than the total number of entries");
     F4J_CUDA(cudaSetDevice(ctx->device));
-    // SparseValidation.validateCoo (…/SparseValidation.java:70-98): indices in range.
+    // SparseValidation.validateCoo (…/SparseValidation.java:70-98): indices in
+    // range, checked by the count and the column copy themselves; the handle is
+    // returned only after both checks have passed (one wait, at the end)
     void* ws;
     int rc = f4j_workspace(ctx, 2, 64, &ws);
     if (rc) return rc;
     int h[2] = {INT32_MAX, INT32_MAX};
     F4J_CUDA(cudaMemcpyAsync(ws, h, 8, cudaMemcpyHostToDevice, ctx->stream));
-    if (nnz) {
-        k_check_range<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)rowidx->ptr, rows, (int*)ws);
-        F4J_LAUNCHED(ctx);
-        k_check_range<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)colidx->ptr, cols, (int*)ws + 1);
-        F4J_LAUNCHED(ctx);
-    }
-    F4J_CUDA(cudaMemcpyAsync(h, ws, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (h[0] != INT32_MAX || h[1] != INT32_MAX) {
-        int at = h[0] < h[1] ? h[0] : h[1];
-        int rc2[2];
-        cudaMemcpy(&rc2[0], (int*)rowidx->ptr + at, 4, cudaMemcpyDeviceToHost);
-        cudaMemcpy(&rc2[1], (int*)colidx->ptr + at, 4, cudaMemcpyDeviceToHost);
-        return f4j_fail(F4J_ERR_CSR, "Invalid index [%d, %d] encountered for COO matrix of shape (%lld, %lld)", rc2[0],
-                        rc2[1], (long long)rows, (long long)cols);
-    }
     f4j_csr S;
     rc = alloc_owned_csr(ctx, rows, cols, nnz, &S);
     if (rc) return rc;
     int* rp = (int*)S->rowptr->ptr;
-    // CooMatrix.toCsr (…/CooMatrix.java:457-470): count per row into rp[r+1], inclusive scan.
+    // CooMatrix.toCsr (…/CooMatrix.java:457-470): count per row into rp[r+1],
+    // inclusive scan; column indices and values copied unchanged
     F4J_CUDA(cudaMemsetAsync(rp, 0, (size_t)(rows + 1) * 4, ctx->stream));
     if (nnz) {
-        k_count<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)rowidx->ptr, rp);
+        k_count_rows_checked<<<grid1(nnz), 256, 0, ctx->stream>>>(nnz, (const int*)rowidx->ptr, rows, rp, (int*)ws);
+        F4J_LAUNCHED(ctx);
+        const bool vec = ((reinterpret_cast<uintptr_t>(colidx->ptr) | reinterpret_cast<uintptr_t>(S->colidx->ptr)) &
+                          15) == 0;
+        if (vec)
+            k_copy_cols_checked<true><<<grid1(f4j_cdiv(nnz, 4)), 256, 0, ctx->stream>>>(
+                nnz, (const int*)colidx->ptr, cols, (int*)S->colidx->ptr, (int*)ws + 1);
+        else
+            k_copy_cols_checked<false><<<grid1(nnz), 256, 0, ctx->stream>>>(
+                nnz, (const int*)colidx->ptr, cols, (int*)S->colidx->ptr, (int*)ws + 1);
         F4J_LAUNCHED(ctx);
     }
     rc = scan_inclusive(ctx, rp + 1, rows);
@@ -1041,8 +1075,18 @@ extern "C" int f4j_csr_from_coo(f4j_ctx* ctx, int64_t rows, int64_t cols, int64_
         f4j_csr_free(ctx, S);
         return rc;
     }
-    F4J_CUDA(cudaMemcpyAsync(S->colidx->ptr, colidx->ptr, (size_t)nnz * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     F4J_CUDA(cudaMemcpyAsync(S->vals->ptr, vals->ptr, (size_t)nnz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    F4J_CUDA(cudaMemcpyAsync(h, ws, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h[0] != INT32_MAX || h[1] != INT32_MAX) {
+        f4j_csr_free(ctx, S);
+        int at = h[0] < h[1] ? h[0] : h[1];
+        int rc2[2];
+        cudaMemcpy(&rc2[0], (int*)rowidx->ptr + at, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&rc2[1], (int*)colidx->ptr + at, 4, cudaMemcpyDeviceToHost);
+        return f4j_fail(F4J_ERR_CSR, "Invalid index [%d, %d] encountered for COO matrix of shape (%lld, %lld)", rc2[0],
+                        rc2[1], (long long)rows, (long long)cols);
+    }
     *out = S;
     return F4J_OK;
 }

@@ -542,3 +542,29 @@ def test_spmm_exact_rounding_adversarial_operands(f4j, oracle, specials, ncols):
     assert _same_bits(S.mult(f4j.Matrix(X)).toNumpy(), oracle.spmm(rp, ci, v, X))
     trp, tci, tv, _ = oracle.csr_transpose(rows, cols, rp, ci, v)
     assert _same_bits(S.multTransposeLeft(f4j.Matrix(X)).toNumpy(), oracle.spmm(trp, tci, tv, X))
+
+
+def test_coo_to_csr_range_checks_report_first_bad_entry(f4j):
+    """CooMatrix.toCsr checks the indices inside the row count and the column copy: the first
+    out-of-range entry by position is reported as SparseValidation.validateCoo words it, for rows
+    and columns, in the 16-byte column copy and its tail, and a later bad entry does not win; a
+    valid conversion afterwards still works."""
+    rng = np.random.default_rng(3)
+    n, rows, cols = 100003, 5000, 7000
+    r = np.sort(rng.integers(0, rows, n)).astype(np.int32)
+    c = rng.integers(0, cols, n).astype(np.int32)
+    v = rng.standard_normal(n)
+    cases = [[(n - 1, "col", cols)], [(50001, "row", -1)], [(4, "col", -3), (50001, "row", rows)],
+             [(n - 2, "row", rows)], [(37, "row", rows + 9), (38, "col", -1)]]
+    for bad in cases:
+        rr, cc = r.copy(), c.copy()
+        for pos, which, val in bad:
+            (rr if which == "row" else cc)[pos] = val
+        first = bad[0][0]
+        with pytest.raises(f4j.IllegalArgumentException,
+                           match=r"Invalid index \[%d, %d\]" % (rr[first], cc[first])):
+            f4j.CooMatrix((rows, cols), v, rr, cc).toCsr()
+    S = f4j.CooMatrix((rows, cols), v, r, c).toCsr()
+    assert S.rowPointers[-1] == n
+    assert np.array_equal(np.diff(S.rowPointers), np.bincount(r, minlength=rows))
+    assert np.array_equal(S.colIndices, c) and np.array_equal(S.data, v)
