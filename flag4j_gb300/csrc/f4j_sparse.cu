@@ -561,8 +561,9 @@ __device__ __forceinline__ void coo_emit(int64_t pos, int row, unsigned long lon
     if (po) po[pos] = (int)(unsigned)k;
 }
 
-// a warp per row; rows of up to 32 entries are ranked in registers (keys are
-// unique), longer ones are listed for k_coo_seg_block
+// a warp per row; rows of up to 64 entries are ranked in registers, two keys
+// per lane (keys are unique, so the ranks are a permutation), longer ones are
+// listed for k_coo_seg_block
 __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const unsigned long long* __restrict__ key,
                                int* __restrict__ ro, int* __restrict__ co, const double* __restrict__ vin,
                                double* __restrict__ vo, int* __restrict__ po, int* __restrict__ longlist,
@@ -571,17 +572,29 @@ __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const u
     const int lane = threadIdx.x % 32;
     if (row >= rows) return;
     const int q0 = __ldg(&rp[row]), len = __ldg(&rp[row + 1]) - q0;
-    if (len > 32) {
+    if (len > 64) {
         if (lane == 0) longlist[atomicAdd(nlong, 1)] = (int)row;
         return;
     }
-    const unsigned long long k = lane < len ? key[q0 + lane] : ~0ull;
-    int rank = 0;
-    for (int j = 0; j < len; j++) rank += __shfl_sync(0xffffffffu, k, j) < k;
-    if (lane < len) coo_emit(q0 + rank, (int)row, k, ro, co, vin, vo, po);
+    const unsigned long long k0 = lane < len ? key[q0 + lane] : ~0ull;
+    const unsigned long long k1 = lane + 32 < len ? key[q0 + 32 + lane] : ~0ull;
+    const int n0 = len < 32 ? len : 32, n1 = len - n0;
+    int r0 = 0, r1 = 0;
+    for (int j = 0; j < n0; j++) {
+        const unsigned long long x = __shfl_sync(0xffffffffu, k0, j);
+        r0 += x < k0;
+        r1 += x < k1;
+    }
+    for (int j = 0; j < n1; j++) {
+        const unsigned long long x = __shfl_sync(0xffffffffu, k1, j);
+        r0 += x < k0;
+        r1 += x < k1;
+    }
+    if (lane < len) coo_emit(q0 + r0, (int)row, k0, ro, co, vin, vo, po);
+    if (lane + 32 < len) coo_emit(q0 + r1, (int)row, k1, ro, co, vin, vo, po);
 }
 
-// a block per listed row (33 .. pmax entries, pmax a power of two up to
+// a block per listed row (65 .. pmax entries, pmax a power of two up to
 // SEG_CAP): bitonic sort in shared memory (pmax keys)
 __global__ void __launch_bounds__(512) k_coo_seg_block(const int* __restrict__ longlist, const int* __restrict__ nlong,
                                                        const int* __restrict__ rp,
@@ -1196,7 +1209,7 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, in
     unsigned long long* key = nullptr;
     double* vin = nullptr;
     int* longlist = nullptr;
-    const int64_t maxlong = std::min<int64_t>(rows, nnz / 33 + 1);
+    const int64_t maxlong = std::min<int64_t>(rows, nnz / 65 + 1);
     if (!rc) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&key);
     if (!rc && v) rc = f4j_dev_alloc(ctx, (size_t)nnz * 8, (void**)&vin);
     if (!rc) rc = f4j_dev_alloc(ctx, (size_t)maxlong * 4, (void**)&longlist);
@@ -1207,14 +1220,17 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, in
         k_coo_bucket<<<red_grid, 256, 0, ctx->stream>>>(nnz, r, c, rp, cur, key);
         k_coo_seg_warp<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, rp, key, r, c, vin, v,
                                                                                    perm_out, longlist, mm);
-        // block path sized to the longest row: pmax keys of shared memory, pmax / 2 threads
-        int pmax = 64;
-        while (pmax < hm[3]) pmax <<= 1;
-        const int bthreads = pmax / 2 < 512 ? pmax / 2 : 512;
-        const unsigned bgrid = (unsigned)std::min<int64_t>(maxlong, (int64_t)ctx->sm_count * 32);
-        k_coo_seg_block<<<bgrid, bthreads, (size_t)pmax * 8, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v,
-                                                                            perm_out);
-        ctx->launches += 3;
+        ctx->launches += 2;
+        if (hm[3] > 64) {
+            // block path sized to the longest row: pmax keys of shared memory, pmax / 2 threads
+            int pmax = 128;
+            while (pmax < hm[3]) pmax <<= 1;
+            const int bthreads = pmax / 2 < 512 ? pmax / 2 : 512;
+            const unsigned bgrid = (unsigned)std::min<int64_t>(maxlong, (int64_t)ctx->sm_count * 32);
+            k_coo_seg_block<<<bgrid, bthreads, (size_t)pmax * 8, ctx->stream>>>(longlist, mm, rp, key, r, c, vin, v,
+                                                                                perm_out);
+            ctx->launches++;
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "coo sort");
     }

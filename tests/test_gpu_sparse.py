@@ -218,14 +218,15 @@ def _shuffled_coo(rng, lens, cols, dup=0):
 
 @pytest.mark.parametrize("case", ["segments", "beyond_segment_cap", "no_values"])
 def test_coo_sort_row_lengths_and_paths(f4j, oracle, case):
-    """Rows of 0..32 entries (ranked in a warp), 33..4096 (sorted in shared
-    memory) and beyond 4096 (the radix path), duplicates included."""
+    """Rows of 0..64 entries (ranked in a warp, two keys per lane), 65..4096
+    (sorted in shared memory) and beyond 4096 (the radix path), duplicates
+    included, with lengths on both sides of 32 and 64."""
     rng = np.random.default_rng(len(case))
     lens = rng.integers(0, 40, 3000)
     if case == "beyond_segment_cap":
         lens[[10, 2000]] = [5000, 4097]
     else:
-        lens[[5, 6, 700, 1500, 2999]] = [33, 64, 1000, 4096, 100]
+        lens[[5, 6, 7, 8, 9, 700, 1500, 2999]] = [33, 64, 65, 63, 32, 1000, 4096, 100]
     r, c, v = _shuffled_coo(rng, lens, 6000, dup=700)
     er, ec, ev, _ = oracle.coo_sort(r, c, v)
     ro, co, vo = _coo_sort_abi(f4j, r, c, None if case == "no_values" else v)
