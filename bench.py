@@ -281,7 +281,7 @@ def cpu_baseline(n, k, seconds_target=15.0):
     O.dgemm(A, B, threads=threads)
     dt = time.perf_counter() - t0
     rows = max(threads, int(rows * seconds_target / max(dt, 1e-3)) // threads * threads)
-    rows = min(rows, 4096)
+    rows = min(rows, 4096, n)
     A = synth.scaled(rows, k, 8, 1, "row")
     t0 = time.perf_counter()
     O.dgemm(A, B, threads=threads)
@@ -759,14 +759,16 @@ def run_ours(args):
             "data": "synthetic (seeded PCG64)",
             "config": {"workload": "FP64-accurate GEMM %d^3 (split path), A u*2^e per row, B per column, "
                                    "u~U[-1,1), e~U[-8,8]" % n,
-                       "l2": "inputs larger than L2 (A, B 512 MiB each), no flush",
+                       "l2": ("inputs larger than L2 (A, B %d MiB each), no flush" % (8 * n * n >> 20)
+                              if 8 * n * n > (129 << 20) else
+                              "A, B %d MiB each: L2-resident across steps" % (8 * n * n >> 20)),
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": ws * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes,
                     "path": "f4j_dgemm_host (split) on page-locked host A, B, C (f4j_host_alloc): A, B up; "
                             "C down in 4 shrinking row parts, each part's download overlapping the other parts' "
-                            "products"},
+                            "products (one launch and one download for products that split K)"},
             "gpu_launches": launches, "clocks": clocks}
     line.update(out)
     print(json.dumps(line))
