@@ -382,8 +382,8 @@ __global__ void k_plan_table(int64_t Kp, int64_t klen_cat, int band, int kcb_cap
     P->nrounds = n;
 }
 
-// One warp: k_plan's result from a plan table (the slice count from the
-// statistics, that plan copied, the header filled in).
+// One block of 128 threads: k_plan's result from a plan table (the slice count
+// from the statistics, that plan copied, the header filled in).
 __global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int s_req, const SplitPlan* __restrict__ tab,
                             SplitPlan* __restrict__ plan) {
     if (blockIdx.x != 0) return;
@@ -391,6 +391,7 @@ __global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int s_req, 
     const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
     const uint4* src = reinterpret_cast<const uint4*>(&tab[s]);
     uint4* dst = reinterpret_cast<uint4*>(plan);
+#pragma unroll 4
     for (int i = threadIdx.x; i < (int)(sizeof(SplitPlan) / 16); i += blockDim.x) dst[i] = src[i];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1116,7 +1117,7 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
             memcpy(ctx->plan_key[t], key, sizeof key);
             ctx->plan_valid[t] = true;
         }
-        k_plan_pick<<<1, 32, 0, ctx->stream>>>(misc, k, slices_req > 0 ? slices_req : env_slices(), tab, plan);
+        k_plan_pick<<<1, 128, 0, ctx->stream>>>(misc, k, slices_req > 0 ? slices_req : env_slices(), tab, plan);
         F4J_LAUNCHED(ctx);
     }
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
