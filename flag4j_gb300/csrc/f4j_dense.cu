@@ -440,15 +440,22 @@ __global__ void __launch_bounds__(256) k_gemv_rows(int64_t m, int64_t k, const d
     if (row >= m) return;
     double re = 0.0, im = 0.0;
     if (!CPLX) {
+        // four independent chains, their eight loads issued together: the
+        // FP64 pipe (2 lanes per clock per SM) bounds this kernel, and two
+        // chains per warp left it waiting on loads
         const double* a = A + row * k;
-        double r1 = 0.0;
+        double r1 = 0.0, r2 = 0.0, r3 = 0.0;
         int64_t j = lane;
-        for (; j + 32 < k; j += 64) {
-            re = fma(__ldg(&a[j]), __ldg(&x[j]), re);
-            r1 = fma(__ldg(&a[j + 32]), __ldg(&x[j + 32]), r1);
+        for (; j + 96 < k; j += 128) {
+            const double a0 = __ldg(&a[j]), a1 = __ldg(&a[j + 32]), a2 = __ldg(&a[j + 64]), a3 = __ldg(&a[j + 96]);
+            const double x0 = __ldg(&x[j]), x1 = __ldg(&x[j + 32]), x2 = __ldg(&x[j + 64]), x3 = __ldg(&x[j + 96]);
+            re = fma(a0, x0, re);
+            r1 = fma(a1, x1, r1);
+            r2 = fma(a2, x2, r2);
+            r3 = fma(a3, x3, r3);
         }
-        if (j < k) re = fma(__ldg(&a[j]), __ldg(&x[j]), re);
-        re += r1;
+        for (; j < k; j += 32) re = fma(__ldg(&a[j]), __ldg(&x[j]), re);
+        re = (re + r1) + (r2 + r3);
     } else {
         const double2* a = reinterpret_cast<const double2*>(A) + row * k;
         const double2* xv = reinterpret_cast<const double2*>(x);
