@@ -271,13 +271,12 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int u = 0; u < 8; u++) a[u] = b[u] = make_double2(0.0, 0.0);
     }
-    double s0 = 0.0, s1 = 0.0;
+    // one chain: the FP64 pipe (2 lanes per clock per SM) bounds this kernel and
+    // other warps fill it while a chain waits, so a second chain's closing add
+    // would only cost an instruction
+    double s = 0.0;
 #pragma unroll
-    for (int u = 0; u < 8; u += 2) {
-        s0 = fma(a[u].y, b[u].y, fma(a[u].x, b[u].x, s0));
-        s1 = fma(a[u + 1].y, b[u + 1].y, fma(a[u + 1].x, b[u + 1].x, s1));
-    }
-    double s = s0 + s1;
+    for (int u = 0; u < 8; u++) s = fma(a[u].y, b[u].y, fma(a[u].x, b[u].x, s));
     s += __shfl_xor_sync(0xffffffffu, s, 2);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     if (q < nnz && l4 == 0) out[q] = s;
