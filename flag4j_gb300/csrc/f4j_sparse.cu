@@ -562,14 +562,16 @@ __device__ __forceinline__ void coo_emit(int64_t pos, int row, unsigned long lon
 
 // a warp per row; rows of up to 64 entries are ranked in registers, two keys
 // per lane (keys are unique, so the ranks are a permutation), longer ones are
-// listed for k_coo_seg_block
+// listed for k_coo_seg_block (nlong[0] counts them; nlong[3] is the longest row)
 __global__ void k_coo_seg_warp(int64_t rows, const int* __restrict__ rp, const unsigned long long* __restrict__ key,
                                int* __restrict__ ro, int* __restrict__ co, const double* __restrict__ vin,
                                double* __restrict__ vo, int* __restrict__ po, int* __restrict__ longlist,
                                int* __restrict__ nlong) {
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x % 32;
-    if (row >= rows) return;
+    // nlong[3]: the longest row; beyond SEG_CAP the host sorts by radix from
+    // the untouched input instead
+    if (row >= rows || nlong[3] > SEG_CAP) return;
     const int q0 = __ldg(&rp[row]), len = __ldg(&rp[row + 1]) - q0;
     if (len > 64) {
         if (lane == 0) longlist[atomicAdd(nlong, 1)] = (int)row;
@@ -1192,19 +1194,9 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, in
         ctx->launches += 2;
         rc = scan_inclusive(ctx, rp + 1, rows);
     }
-    if (!rc) {
-        F4J_CUDA(cudaMemcpyAsync(&hm[3], mm + 3, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (hm[3] > SEG_CAP) {
-            f4j_dev_free(ctx, rp);
-            f4j_dev_free(ctx, cur);
-            f4j_dev_free(ctx, mm);
-            int rb = 0, cb = 0;
-            while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
-            while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
-            return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false, perm_out);
-        }
-    }
+    // buckets and the warp segment sort are queued before the host reads the
+    // longest row, so the GPU never waits on the host between them; the warp
+    // kernel leaves the input untouched when a row exceeds SEG_CAP
     unsigned long long* key = nullptr;
     double* vin = nullptr;
     int* longlist = nullptr;
@@ -1220,6 +1212,20 @@ static int coo_sort_dev(f4j_ctx* ctx, int64_t nnz, int* r, int* c, double* v, in
         k_coo_seg_warp<<<(unsigned)f4j_cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(rows, rp, key, r, c, vin, v,
                                                                                    perm_out, longlist, mm);
         ctx->launches += 2;
+        F4J_CUDA(cudaMemcpyAsync(&hm[3], mm + 3, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (hm[3] > SEG_CAP) {
+            f4j_dev_free(ctx, key);
+            f4j_dev_free(ctx, vin);
+            f4j_dev_free(ctx, longlist);
+            f4j_dev_free(ctx, rp);
+            f4j_dev_free(ctx, cur);
+            f4j_dev_free(ctx, mm);
+            int rb = 0, cb = 0;
+            while (rb < 31 && (1ll << rb) <= hm[1]) rb++;
+            while (cb < 31 && (1ll << cb) <= hm[2]) cb++;
+            return coo_sort_radix(ctx, nnz, r, c, v, rb, cb, false, perm_out);
+        }
         if (hm[3] > 64) {
             // block path sized to the longest row: pmax keys of shared memory, pmax / 2 threads
             int pmax = 128;
