@@ -145,11 +145,13 @@ int f4j_buf_wrap(f4j_ctx* ctx, void* ptr, size_t bytes, f4j_buf* out);
  * A is stored m x k (opA N) or k x m (opA T); B k x n (N) or n x k (T). */
 int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA, f4j_buf B,
               int opB, f4j_buf C, int mode, f4j_report* report);
-/* f4j_dgemm from and to host memory: A, B, C are host pointers (row-major,
- * pinned with f4j_host_register for full copy speed; pageable works), and the
- * call returns when C is in host memory.  A split product with opA = N runs
- * as row parts of C on their own streams so that C's download overlaps the
- * later parts' products; the result is bitwise the f4j_dgemm result.  This is
+/* f4j_dgemm from and to host memory: A, B, C are host pointers (row-major;
+ * page-locked by f4j_host_alloc or f4j_host_register for full copy speed,
+ * pageable works), and the call returns when C is in host memory.  A split
+ * product with opA = N and 152 or more output tiles runs as shrinking row parts
+ * of C on their own streams so that C's downloads overlap the other parts'
+ * products; smaller products (split K) run as one launch.  The result is
+ * bitwise the f4j_dgemm result.  This is
  * the entry a JVM binding calls with its arrays' native copies for Flag4j's
  * Matrix.mult(Matrix) (src/main/java/org/flag4j/arrays/dense/Matrix.java:638-640),
  * same arguments and result. */
