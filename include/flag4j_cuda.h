@@ -148,10 +148,10 @@ int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
 /* f4j_dgemm from and to host memory: A, B, C are host pointers (row-major;
  * page-locked by f4j_host_alloc or f4j_host_register for full copy speed,
  * pageable works), and the call returns when C is in host memory.  A split
- * product with opA = N and 152 or more output tiles runs as shrinking row parts
- * of C on their own streams so that C's downloads overlap the other parts'
- * products; smaller products (split K) run as one launch.  The result is
- * bitwise the f4j_dgemm result.  This is
+ * product with opA = N runs as shrinking row parts of C on their own streams
+ * so that C's downloads overlap the other parts' products, unless it splits K
+ * (fewer than 152 output tiles and K <= 4096), which runs as one launch.  The
+ * result is bitwise the f4j_dgemm result.  This is
  * the entry a JVM binding calls with its arrays' native copies for Flag4j's
  * Matrix.mult(Matrix) (src/main/java/org/flag4j/arrays/dense/Matrix.java:638-640),
  * same arguments and result. */
