@@ -1331,19 +1331,27 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
 }
 
 // ------------------------------------------------------------------ no-allocation variant
-// Some callers cannot allocate device memory: code running inside a CUDA graph
-// being captured or replayed, engines that hand out a fixed memory pool and
-// forbid cudaMalloc after start-up, and JVM or other runtime hosts that only
-// pass in buffers they already own.  f4j_dgemm_split_noalloc serves them: it
-// runs the same split GEMM as f4j_dgemm(..., F4J_MODE_SPLIT, ...) but takes
-// its scratch (exponent statistics and the FP8 slice planes) from the
-// file-scope array below, so it calls no allocator at all.
+// Some callers cannot allocate device memory: engines that hand out a fixed
+// memory pool and forbid cudaMalloc after start-up, and JVM or other runtime
+// hosts that only pass in buffers they already own.  f4j_dgemm_split_noalloc
+// serves them: it runs the same split GEMM as f4j_dgemm(..., F4J_MODE_SPLIT,
+// ...) but takes its scratch (exponent statistics, the plan and the FP8 slice
+// planes) from the file-scope array below, so it calls no allocator at all.
 //
 // The array holds F4J_NOALLOC_SCRATCH_BYTES on every GPU that loads this
 // library, until the process exits.  It is shared by every call on a device and
 // keeps the last call's contents; each call clears what must start at zero.
 // Calls whose GPU work overlaps (e.g. on two streams) race on it.
+//
+// A call needs at most F4J_NOALLOC_NEED(m, n, Kp) bytes of it (Kp = k rounded
+// up to 64): 12 slice planes of (m + n) x Kp bytes, 24 bytes of statistics and
+// exponents per row of op(A) and column of op(B), and under 16 KiB for the
+// plan, the status words and the 1 KiB roundings of each part.  The call is
+// rejected exactly when that formula exceeds the array.
 #define F4J_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define F4J_NOALLOC_NEED(m, n, Kp) \
+    ((size_t)12 * (size_t)((m) + (n)) * (size_t)(Kp) + (size_t)24 * (size_t)((m) + (n)) + (size_t)16384)
+static_assert(sizeof(SplitPlan) <= 4096, "the no-allocation bound's fixed part counts the plan as at most 4 KiB");
 static __device__ __align__(256) unsigned char g_f4j_noalloc_scratch[F4J_NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mu;
@@ -1371,6 +1379,8 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     if (slices_out) *slices_out = 0;
     if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null matrix pointer");
     if (m < 0 || n < 0 || k < 0) return f4j_fail(F4J_ERR_ARG, "negative dimension");
+    if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX)
+        return f4j_fail(F4J_ERR_ARG, "dimension exceeds Flag4j's int range");
     if (opA == F4J_OP_C) opA = F4J_OP_T;
     if (opB == F4J_OP_C) opB = F4J_OP_T;
     if (opA < 0 || opA > F4J_OP_T || opB < 0 || opB > F4J_OP_T) return f4j_fail(F4J_ERR_ARG, "bad op");
@@ -1382,19 +1392,21 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     }
     const int64_t M = m, N = n;
     const int64_t Kp = f4j_cdiv(k, BKB) * BKB;
+    if (F4J_NOALLOC_NEED(M, N, Kp) > F4J_NOALLOC_SCRATCH_BYTES)
+        return f4j_fail(F4J_ERR_ARG,
+                        "f4j_dgemm_split_noalloc: m=%lld n=%lld k=%lld needs %zu bytes of scratch "
+                        "(12*(m+n)*roundup(k,64) + 24*(m+n) + 16384), more than the %u-byte static limit; "
+                        "use f4j_dgemm",
+                        (long long)m, (long long)n, (long long)k, F4J_NOALLOC_NEED(M, N, Kp),
+                        F4J_NOALLOC_SCRATCH_BYTES);
     const size_t off_mxa = 0, off_esa = off_mxa + al1k(M * 8), off_cna = off_esa + al1k(M * 8);
     const size_t off_mxb = off_cna + al1k(M * 4), off_esb = off_mxb + al1k(N * 8), off_cnb = off_esb + al1k(N * 8);
     const size_t off_ea = off_cnb + al1k(N * 4), off_eb = off_ea + al1k(M * 4);
     const size_t off_misc = off_eb + al1k(N * 4);
     const size_t off_plan = off_misc + 1024;
     const size_t off_sl = off_plan + al1k(sizeof(SplitPlan));
-    // worst case over the slice counts this function may pick
-    const size_t need = off_sl + al1k((size_t)M * Kp * S_MAX) + al1k((size_t)N * Kp * S_MAX);
-    if (need > F4J_NOALLOC_SCRATCH_BYTES)
-        return f4j_fail(F4J_ERR_ARG,
-                        "f4j_dgemm_split_noalloc: m=%lld n=%lld k=%lld needs %zu bytes of scratch, more than the "
-                        "%u-byte static limit ((m+n)*roundup(k,64)*12 + small); use f4j_dgemm",
-                        (long long)m, (long long)n, (long long)k, need, F4J_NOALLOC_SCRATCH_BYTES);
+    if (off_sl + al1k((size_t)M * Kp * S_MAX) + al1k((size_t)N * Kp * S_MAX) > F4J_NOALLOC_NEED(M, N, Kp))
+        return f4j_fail(F4J_ERR_UNSUPPORTED, "f4j_dgemm_split_noalloc: scratch layout exceeds its stated bound");
     void* base;
     int rc = noalloc_scratch(&base);
     if (rc) return rc;
@@ -1410,32 +1422,25 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     int* cnb = (int*)(w + off_cnb);
     int* ea = (int*)(w + off_ea);
     int* eb = (int*)(w + off_eb);
-    int* misc = (int*)(w + off_misc);  // [0] non-finite, [1..2] spreads, [8] wait status
+    int* misc = (int*)(w + off_misc);  // [0] non-finite input, [1..2] spreads, [8] wait status
     SplitPlan* plan = (SplitPlan*)(w + off_plan);
     // statistics accumulate with atomics and the status word must read 0
     F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, st));
     F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, st));
 
     const bool a_rows = (opA == F4J_OP_N), b_rows = (opB != F4J_OP_N);
-    int cur = 0, smc = 0;
-    F4J_CUDA(cudaGetDevice(&cur));
-    F4J_CUDA(cudaDeviceGetAttribute(&smc, cudaDevAttrMultiProcessorCount, cur));
     if (a_rows) k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, st>>>(A, M, k, 0, mxa, esa, cna, misc);
-    else launch_stats_cols(A, k, M, 0, smc, mxa, esa, cna, misc, st);
+    else launch_stats_cols(A, k, M, 0, sms, mxa, esa, cna, misc, st);
     if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(N, 8), 256, 0, st>>>(B, N, k, 0, mxb, esb, cnb, misc);
-    else launch_stats_cols(B, k, N, 0, smc, mxb, esb, cnb, misc, st);
+    else launch_stats_cols(B, k, N, 0, sms, mxb, esb, cnb, misc, st);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
     int kchunks_na = 0;  // the same chunks as f4j_dgemm plans for this shape, run in turn
     const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks_na);
     k_plan<<<1, 32, 0, st>>>(misc, k, Kp, k, env_slices(), env_band(), kcb_cap, plan);
     F4J_CUDA(cudaGetLastError());
-    // NaN/Inf operands are rejected, so wait for the plan's verdict
-    int hp[4];
-    F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, st));
-    F4J_CUDA(cudaStreamSynchronize(st));
-    if (hp[3])
-        return f4j_fail(F4J_ERR_ARG, "f4j_dgemm_split_noalloc: NaN or Inf in an operand; use f4j_dgemm (AUTO)");
+    // The slicing and slice GEMM kernels read the plan's verdict on the device
+    // and return at once for a NaN/Inf operand or a plan that does not fit.
     uint8_t* slA = (uint8_t*)(w + off_sl);
     uint8_t* slB = slA + al1k((size_t)M * Kp * S_MAX);
     k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
@@ -1467,6 +1472,21 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
     k_split_gemm<<<grid, GEMM_THREADS, smem, st>>>(ta, tb, prm);
     F4J_CUDA(cudaGetLastError());
+    // One wait, after all the work: the plan header (s, nrounds, ubits,
+    // nonfinite), the input flag and the slice GEMM's wait status.
+    int hp[4], hm[9];
+    F4J_CUDA(cudaMemcpyAsync(hp, plan, sizeof hp, cudaMemcpyDeviceToHost, st));
+    F4J_CUDA(cudaMemcpyAsync(hm, misc, sizeof hm, cudaMemcpyDeviceToHost, st));
+    F4J_CUDA(cudaStreamSynchronize(st));
+    if (hm[8])
+        return f4j_fail(F4J_ERR_TIMEOUT,
+                        "f4j_dgemm_split_noalloc: a device-side wait gave up (code %d); C is incomplete", hm[8]);
+    if (hm[0])
+        return f4j_fail(F4J_ERR_ARG,
+                        "f4j_dgemm_split_noalloc: NaN or Inf in an operand; C is not written; use f4j_dgemm (AUTO)");
+    if (hp[3])
+        return f4j_fail(F4J_ERR_UNSUPPORTED,
+                        "f4j_dgemm_split_noalloc: no split plan fits this shape; C is not written; use f4j_dgemm");
     if (slices_out) *slices_out = hp[0];
     return F4J_OK;
 }

@@ -178,19 +178,25 @@ int f4j_zgemm_adjoint(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, 
                       f4j_buf dC, f4j_buf dA, f4j_buf dB, int mode, f4j_report* report);
 
 /* No-allocation variant of the split GEMM (no counterpart in the reference).
- * For callers that may not allocate device memory: work captured into or
- * replayed from a CUDA graph, engines that own a fixed memory pool, and JVM or
- * other hosts that only pass in buffers they already hold.  Same arithmetic as
- * f4j_dgemm(..., F4J_MODE_SPLIT, ...) on real float64; A, B and C are the
- * caller's device pointers, `stream` a cudaStream_t (NULL = default stream).
- * Scratch comes from a static 32 MiB device array inside the library (held on
- * every GPU that loads it until exit), so sizes with
- *   (m + n) * roundup(k, 64) * 12 + 64 * (m + n) + 4096 > 32 MiB
- * are rejected with F4J_ERR_ARG; NaN/Inf operands are rejected too.  The first
- * call on a device looks up the array's address, so make that call before
- * any stream capture.  All calls share the array: calls whose GPU work
- * overlaps race.  Calls no cudaMalloc/cudaFree.  `slices_out` (may be NULL)
- * receives the slice count used. */
+ * For callers that may not allocate device memory: engines that own a fixed
+ * memory pool and forbid allocation after start-up, and JVM or other hosts
+ * that only pass in buffers they already hold.  Same arithmetic as
+ * f4j_dgemm(..., F4J_MODE_SPLIT, ...) on real float64, bitwise; A, B and C are
+ * the caller's device pointers, `stream` a cudaStream_t (NULL = default
+ * stream).  Scratch comes from a static 32 MiB device array inside the library
+ * (held on every GPU that loads it until exit); a call is rejected with
+ * F4J_ERR_ARG exactly when
+ *   12 * (m + n) * roundup(k, 64) + 24 * (m + n) + 16384 > 32 MiB
+ * (e.g. 1024 x 1024 x 1344 fits, 1024 x 1024 x 1408 does not).  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress), so make
+ * that call before any stream capture.  All calls share the array and it
+ * keeps the last call's contents: calls whose GPU work overlaps race.  The
+ * call queues its kernels on `stream`, then waits for them once and returns
+ * F4J_OK with C written; F4J_ERR_ARG for a NaN/Inf operand and
+ * F4J_ERR_UNSUPPORTED when no split plan fits (C not written; f4j_dgemm
+ * handles both); F4J_ERR_TIMEOUT when a bounded device wait gave up (C
+ * incomplete).  Calls no cudaMalloc/cudaFree or allocating library routine.
+ * `slices_out` (may be NULL) receives the slice count used. */
 int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
                             int opB, double* C, void* stream, int32_t* slices_out);
 

@@ -22,12 +22,32 @@ _lock = threading.Lock()
 _lib = None
 
 
+def _digest():
+    """SHA-256 of the source, the flags and the machine: the stamp a reusable build carries."""
+    import hashlib
+    import platform
+    h = hashlib.sha256()
+    with open(SRC, "rb") as f:
+        h.update(f.read())
+    h.update(repr((CFLAGS, platform.machine())).encode())
+    return h.hexdigest()
+
+
 def build(force=False):
-    """Compile the oracle shared library (a second or two)."""
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        tmp = LIB + ".tmp%d" % os.getpid()
-        subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
-        os.replace(tmp, LIB)
+    """Compile the oracle shared library (a second or two) unless the stamp
+    beside it matches this source, these flags and this machine."""
+    stamp = LIB + ".sha256"
+    digest = _digest()
+    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+        with open(stamp) as f:
+            if f.read().strip() == digest:
+                return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    with open(stamp + ".tmp%d" % os.getpid(), "w") as f:
+        f.write(digest + "\n")
+    os.replace(stamp + ".tmp%d" % os.getpid(), stamp)
     return LIB
 
 

@@ -16,7 +16,7 @@ Files read (paths within the Flag4j project):
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealComplexCsrCsrMatMultTests.java
 
-Usage:  python tests/golden/make_golden.py [/path/to/flag4j]
+Usage:  python tests/golden/make_golden.py /path/to/flag4j
 The fixture is committed; the GPU machine never needs the reference tree.
 """
 import json
@@ -191,4 +191,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/flag4j (the Flag4j project root)")
+    main(sys.argv[1])

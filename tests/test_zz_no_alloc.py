@@ -1,8 +1,8 @@
 """The no-allocation split GEMM entry point (f4j_dgemm_split_noalloc).
 
-Callers such as CUDA-graph capture, fixed-pool engines and JVM hosts cannot
-allocate device memory; this entry point takes its scratch from a static array
-in the library instead.  It must agree with the allocating f4j_dgemm split path
+Callers such as engines that own a fixed device-memory pool, or JVM hosts that
+only hand over buffers they already hold, cannot allocate device memory; this
+entry point takes its scratch from a static array in the library instead.  It must agree with the allocating f4j_dgemm split path
 within the same componentwise bound the other tests use, on two calls in a row
 (the shared scratch keeps the previous call's contents).  Collected last so a
 failure here never hides another test's result.
@@ -60,18 +60,41 @@ def test_noalloc_matches_allocating_split_twice(f4j, oracle):
         assert np.array_equal(got, ref_path), "noalloc vs f4j_dgemm split"
 
 
-def test_noalloc_rejects_oversize_and_nonfinite(f4j):
+def test_noalloc_size_limit_is_the_documented_formula(f4j, oracle):
+    """12 (m + n) roundup(k, 64) + 24 (m + n) + 16384 <= 32 MiB: 1024 x 1024 x 1344 is the
+    largest k at m = n = 1024 that fits (and matches f4j_dgemm); 1408 is rejected."""
+    from flag4j_gb300 import _lib, synth
     ctx = f4j.default_context()
+    limit = 32 << 20
+    need = lambda m, n, k: 12 * (m + n) * (-(-k // 64) * 64) + 24 * (m + n) + 16384
+    assert need(1024, 1024, 1344) <= limit < need(1024, 1024, 1408)
     big = ctx.alloc(8)
-    rc = ctx.lib.f4j_dgemm_split_noalloc(4096, 4096, 4096, ctx.lib.f4j_buf_device_ptr(big.handle), 0,
-                                         ctx.lib.f4j_buf_device_ptr(big.handle), 0,
-                                         ctx.lib.f4j_buf_device_ptr(big.handle), None, None)
-    from flag4j_gb300 import _lib
+    p = ctx.lib.f4j_buf_device_ptr(big.handle)
+    rc = ctx.lib.f4j_dgemm_split_noalloc(1024, 1024, 1408, p, 0, p, 0, p, None, None)
     assert rc == _lib.F4J_ERR_ARG and "static limit" in _lib.last_error()
+    m = n = 1024
+    k = 1344
+    As, Bs = synth.scaled(m, k, 8, 5, "row"), synth.scaled(k, n, 8, 6, "col")
+    dA, dB = ctx.from_numpy(As), ctx.from_numpy(Bs)
+    dC1, dC2 = ctx.alloc(8 * m * n), ctx.alloc(8 * m * n)
+    ref_path = _alloc_path(f4j, dA, dB, dC1, m, n, k)
+    assert 2 <= _noalloc(f4j, dA, dB, dC2, m, n, k) <= 12
+    assert np.array_equal(dC2.to_numpy(np.float64, m * n).reshape(m, n), ref_path)
+
+
+def test_noalloc_rejects_nonfinite_then_recovers(f4j):
+    from flag4j_gb300 import _lib, synth
+    ctx = f4j.default_context()
     A = np.ones((64, 64))
     A[1, 1] = np.inf
     dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(np.ones((64, 64))), ctx.alloc(8 * 64 * 64)
     rc = ctx.lib.f4j_dgemm_split_noalloc(64, 64, 64, ctx.lib.f4j_buf_device_ptr(dA.handle), 0,
                                          ctx.lib.f4j_buf_device_ptr(dB.handle), 0,
                                          ctx.lib.f4j_buf_device_ptr(dC.handle), None, None)
-    assert rc == _lib.F4J_ERR_ARG
+    assert rc == _lib.F4J_ERR_ARG and "NaN or Inf" in _lib.last_error()
+    # the next call clears the shared scratch's flags and computes normally
+    As, Bs = synth.uniform(64, 64, 7), synth.uniform(64, 64, 8)
+    dA2, dB2 = ctx.from_numpy(As), ctx.from_numpy(Bs)
+    ref_path = _alloc_path(f4j, dA2, dB2, ctx.alloc(8 * 64 * 64), 64, 64, 64)
+    _noalloc(f4j, dA2, dB2, dC, 64, 64, 64)
+    assert np.array_equal(dC.to_numpy(np.float64, 64 * 64).reshape(64, 64), ref_path)
