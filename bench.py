@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--n", type=int, default=0, help="override the GEMM size n (profiling)")
     p.add_argument("--skip-extras", action="store_true", help="headline GEMM only (for profiling)")
     p.add_argument("--only-sparse", action="store_true", help="CSR products only (for profiling)")
+    p.add_argument("--only-dmma", action="store_true", help="plain DMMA GEMM only (for profiling)")
     return p.parse_args()
 
 
@@ -228,11 +229,17 @@ def fp8_peak_from_file():
     return 2 * 1900.0, "2 x fallback bf16 1.9 PFLOP/s"
 
 
-# DRAM bytes of one k_split_gemm launch at 8192^3 (s = 11), from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass):
+# DRAM bytes of one k_split_gemm launch at 8192^3 by slice count, from one ncu
+# capture each (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass):
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
 #       -k regex:k_split_gemm -s 2 -c 1 python bench.py --skip-extras --steps 2 --warmup 3
-SPLIT_GEMM_DRAM_BYTES_8192 = 15.077633e9 + 0.636095e9
+SPLIT_GEMM_DRAM_BYTES_8192 = {11: 15.077633e9 + 0.636095e9}
+
+# DRAM bytes of one 2^20-row, 32-column SpMM launch (k_spmm), exact and FMA
+# modes, from the ncu capture in profiles/k_spmm_k_spmv_1M_rows.md
+SPMM_DRAM_BYTES_1M = {"exact": 3.255e9 + 0.266e9, "fma": 3.257e9 + 0.265e9}
+# FP64-pipe activity of the same launches (sm__pipe_fp64_cycles_active, of active cycles)
+SPMM_FP64_PIPE_1M = {"exact": 0.839, "fma": 0.933}
 
 
 def fp64_peak_tflops():
@@ -449,16 +456,32 @@ def sparse_section(E, full, steps=20, cpu=False):
     b_spmm = 12.0 * nnz + 4.0 * (rows + 1) + 2 * 8.0 * 32 * rows
     b_spmm_g = 12.0 * nnz + 8.0 * 32 * nnz + 8.0 * 32 * rows
     hbm, hbm_src = measured_peaks()
-    res = {"rows": rows, "nnz": nnz, "spmm_ms": t_spmm, "spmm_gbs_compulsory": b_spmm / t_spmm / 1e6,
-           "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm / 1e6,
-           "spmm_frac_compulsory": b_spmm / t_spmm / 1e6 / hbm, "spmv_ms": t_spmv,
+    # SpMM's binding resource is the FP64 pipe (2 lane-operations per clock per SM on GB300):
+    # 2 * 32 * nnz lane-operations exact, 32 * nnz with FMA.  DRAM GB/s uses the bytes ncu
+    # measured for the same launch (the X-row gathers miss L2 80 % of the time), not a byte
+    # count: gather-inclusive bytes count L2 hits as well.
+    dram = SPMM_DRAM_BYTES_1M if full else None
+
+    def spmm_keys(t, mode):
+        d = {"spmm_ms": t, "spmm_gbs_compulsory": b_spmm / t / 1e6, "spmm_frac_compulsory": b_spmm / t / 1e6 / hbm,
+             "spmm_gbs_gather_inclusive": b_spmm_g / t / 1e6,
+             "spmm_fp64_lane_ops_per_s": (2.0 if mode == "exact" else 1.0) * 32 * nnz / (t * 1e-3)}
+        if dram:
+            d.update({"spmm_dram_gbs_ncu_bytes": dram[mode] / t / 1e6, "spmm_dram_frac": dram[mode] / t / 1e6 / hbm,
+                      "spmm_fp64_pipe_busy_ncu": SPMM_FP64_PIPE_1M[mode],
+                      "spmm_bound": "FP64 pipe (%.1f %% busy in ncu)" % (100 * SPMM_FP64_PIPE_1M[mode])})
+        return d
+
+    res = {"rows": rows, "nnz": nnz, "spmv_ms": t_spmv,
            "spmv_gbs": b_spmv / t_spmv / 1e6, "spmv_frac": b_spmv / t_spmv / 1e6 / hbm,
            "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src, "bit_identical_to_reference_order": True,
-           "fma_mode": {"spmm_ms": t_spmm_f, "spmm_gbs_compulsory": b_spmm / t_spmm_f / 1e6,
-                        "spmm_gbs_gather_inclusive": b_spmm_g / t_spmm_f / 1e6,
-                        "spmm_frac_gather_inclusive": b_spmm_g / t_spmm_f / 1e6 / hbm,
-                        "spmv_ms": t_spmv_f, "spmv_gbs": b_spmv / t_spmv_f / 1e6,
+           "spmm_bytes_note": "compulsory = 12 nnz + 4 (rows + 1) + 2 * 8 * 32 rows; gather-inclusive counts "
+                              "a 256-byte X row per nonzero, L2 hits included; DRAM from ncu's bytes",
+           "fma_mode": {"spmv_ms": t_spmv_f, "spmv_gbs": b_spmv / t_spmv_f / 1e6,
+                        "spmv_frac": b_spmv / t_spmv_f / 1e6 / hbm,
                         "bound": "|y - y_ref| <= 2 k u |S||x| per row"}}
+    res.update(spmm_keys(t_spmm, "exact"))
+    res["fma_mode"].update(spmm_keys(t_spmm_f, "fma"))
     del x, y, X, Y
 
     # ---- structure: stable COO sort of shuffled triplets, then COO -> CSR
@@ -701,7 +724,7 @@ def run_ours(args):
     fp8_peak, fp8_src = fp8_peak_from_file()
     fp8_run, fp8_run_src = fp8_peak_tflops() if not args.skip_extras else (None, None)
     achieved = fp8_flops / (kms * 1e-3) / 1e12
-    traffic = SPLIT_GEMM_DRAM_BYTES_8192 if n == 8192 else None
+    traffic = SPLIT_GEMM_DRAM_BYTES_8192.get(s) if n == 8192 else None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp8_peak, "traffic": traffic,
                 "traffic_note": "DRAM bytes per launch from one ncu capture of the 8192^3 launch (read + write); "
@@ -715,6 +738,14 @@ def run_ours(args):
     fp64_peak = fp64_peak_tflops() if not args.skip_extras else None
     if fp64_peak:
         out["fp64_dgemm_peak_tflops"] = fp64_peak
+        # plain DMMA against the same run's cuBLAS DGEMM: GB300 issues mma.sync f64 to its FP64
+        # pipe, which ncu shows 93 % busy in k_gemm_dmma (profiles/k_gemm_dmma_2048cube.md)
+        pt = out["plain_dmma"]["tflops"]
+        out["plain_dmma"]["roofline"] = {"bound": "fp64 (DMMA on the FP64 pipe)", "achieved": pt, "peak": fp64_peak,
+                                         "unit": "TFLOP/s", "frac": pt / fp64_peak, "kernel": "k_gemm_dmma",
+                                         "peak_source": "cuBLAS DGEMM 8192^3 (torch.matmul float64) in this run, "
+                                                        "best of 3; MEASURED_PEAKS.json has no FP64 figure",
+                                         "basis": "2 n^3 flops per product"}
 
     # ---- end to end through the host-buffer API (page-locked host memory from f4j_host_alloc)
     from flag4j_gb300.device import pinned_empty
@@ -774,12 +805,27 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_dmma_only(args):
+    """Profiling helper: the plain DMMA GEMM alone, n^3 (2048 with --case small), uniform[-1, 1) operands;
+    prints its own numbers, not the contract line."""
+    from flag4j_gb300 import build, synth
+    build.build()
+    E = Eng(dist_env()[2])
+    n = args.n if args.n > 0 else (8192 if args.case == "full" else 2048)
+    A, B, C = E.dev(synth.uniform(n, n, 1)), E.dev(synth.uniform(n, n, 2)), E.ctx.alloc(8 * n * n)
+    ms = E.timed(lambda: E.gemm(A, B, C, n, n, n, E.L.MODE_PLAIN), args.steps, args.warmup)
+    print(json.dumps({"kernel": "k_gemm_dmma", "n": n, "ms": ms, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12,
+                      "steps": args.steps, "warmup": args.warmup}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.only_sparse:
         run_sparse_only(args)
+    elif args.only_dmma:
+        run_dmma_only(args)
     else:
         run_ours(args)
 

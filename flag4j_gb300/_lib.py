@@ -26,10 +26,30 @@ SPARSE_MODES = {"exact": SPARSE_EXACT, "fma": SPARSE_FMA}
 MODES = {"plain": MODE_PLAIN, "split": MODE_SPLIT, "auto": MODE_AUTO, "exact": MODE_EXACT}
 
 
+CHECK_PLAIN = 1
+
+REF_KERNELS = ["STRD", "REORD", "BLK", "BLK_REORD", "MT_STRD", "MT_REORD", "MT_BLK", "MT_BLK_REORD",
+               "STRD_VEC_AS_MAT", "BLK_VEC_AS_MAT", "MT_STRD_VEC_AS_MAT", "MT_BLK_VEC_AS_MAT"]
+
+
 class f4j_report(ctypes.Structure):
     _fields_ = [("mode_used", ctypes.c_int32), ("slices", ctypes.c_int32), ("launches", ctypes.c_int32),
                 ("frac_bits", ctypes.c_int32), ("flops", ctypes.c_double), ("bytes", ctypes.c_double),
-                ("exp_spread", ctypes.c_double)]
+                ("exp_spread", ctypes.c_double), ("check_samples", ctypes.c_int32), ("check_flags", ctypes.c_int32),
+                ("max_abs_err", ctypes.c_double), ("max_rel_err", ctypes.c_double),
+                ("plain_bound_rel", ctypes.c_double), ("plain_max_abs_err", ctypes.c_double),
+                ("plain_max_rel_err", ctypes.c_double), ("ref_kernel", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class f4j_dispatch_config(ctypes.Structure):
+    _fields_ = [("cache_size", ctypes.c_double), ("aspect_threshold", ctypes.c_double),
+                ("small_threshold", ctypes.c_int32), ("square_mt_standard_threshold", ctypes.c_int32),
+                ("square_mt_reordered_threshold", ctypes.c_int32), ("wide_mt_reordered_threshold", ctypes.c_int32),
+                ("square_sequential_vec_threshold", ctypes.c_int32), ("min_dim_small_threshold", ctypes.c_int32),
+                ("gpu_gemm_mode", ctypes.c_int32), ("loaded", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -78,6 +98,12 @@ SIGNATURES = {
     "f4j_zgemm_adjoint": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _v, _v, _i, _rep]),
     "f4j_gemm_check": (_i, [_v, _i, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i64, _u64, _pd, _pd]),
     "f4j_dgemm_split_noalloc": (_i, [_i64, _i64, _i64, _v, _i, _v, _i, _v, _v, ctypes.POINTER(ctypes.c_int32)]),
+    "f4j_config_load": (_i, [ctypes.c_char_p]),
+    "f4j_config_reset": (_i, []),
+    "f4j_config_get": (_i, [_i, ctypes.POINTER(f4j_dispatch_config)]),
+    "f4j_config_general": (_i, [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "f4j_dispatch": (_i, [_i, _i64, _i64, _i64, _i, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "f4j_ref_kernel_name": (ctypes.c_char_p, [_i]),
     "f4j_csr_wrap": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _i, _pv]),
     "f4j_csr_from_coo": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _pv]),
     "f4j_coo_sort": (_i, [_v, _i64, _v, _v, _v]),

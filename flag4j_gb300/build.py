@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflag4j_cuda.so")
 STAMP = LIB + ".sha256"
-SOURCES = ["f4j_core.cu", "f4j_dense.cu", "f4j_split.cu", "f4j_sparse.cu"]
+SOURCES = ["f4j_core.cu", "f4j_dense.cu", "f4j_split.cu", "f4j_sparse.cu", "f4j_config.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]

@@ -472,16 +472,20 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     if (rep) {
         *rep = f4j_report{};
         rep->flops = (cplx ? 8.0 : 2.0) * (double)m * (double)n * (double)k;
+        rep->max_abs_err = rep->max_rel_err = rep->plain_max_abs_err = rep->plain_max_rel_err = -1.0;
     }
     if (!cplx) {  // conjugation is the identity for real data
         if (opA == F4J_OP_C) opA = F4J_OP_T;
         if (opB == F4J_OP_C) opB = F4J_OP_T;
     }
     if (m == 0 || n == 0) return F4J_OK;
-    // AUTO on tiny products (a few microseconds of work) runs Flag4j's own
-    // order, so small results are bit-identical to the reference.
-    const double work = (cplx ? 8.0 : 2.0) * (double)m * (double)n * (double)k;
-    if (mode == F4J_MODE_AUTO && work <= (double)(1 << 24)) mode = F4J_MODE_EXACT;
+    // AUTO follows the dispatcher configuration: the reference's small-product
+    // rule and products of a few microseconds of work run Flag4j's own order
+    // (bit-identical); larger ones take the configured GPU path (f4j_config.cu).
+    if (mode == F4J_MODE_AUTO) {
+        mode = f4j_resolve_mode(cplx, m, n, k, mode);
+        if (mode == F4J_MODE_AUTO) mode = F4J_MODE_SPLIT;
+    }
     int rc = F4J_OK;
     int used = mode;
     if (k == 0) {
@@ -513,24 +517,61 @@ int f4j_gemm_impl(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     return rc;
 }
 
+// The accuracy part of a dense product's report (f4j_report's check fields):
+// the sampled double-double error of C, the plain FP64 bound on the same
+// scale, and with F4J_CHECK_PLAIN the plain DMMA product's error on the same
+// entries (that product goes to pool scratch and is freed again).
+
+int f4j_report_accuracy(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                        const double* B, int opB, const double* C, int samples, int flags, f4j_report* rep) {
+    if (!rep) return F4J_OK;
+    rep->check_samples = samples;
+    rep->check_flags = flags;
+    int32_t rk = 0;
+    f4j_dispatch(cplx ? 1 : 0, m, n, k, F4J_MODE_AUTO, nullptr, &rk);
+    rep->ref_kernel = rk;
+    rep->plain_bound_rel = (cplx ? 2.0 : 1.0) * (double)k * 0x1p-53;
+    rep->max_abs_err = rep->max_rel_err = -1.0;
+    rep->plain_max_abs_err = rep->plain_max_rel_err = -1.0;
+    if (samples <= 0 || m == 0 || n == 0) return F4J_OK;
+    int rc = f4j_check_sampled(ctx, cplx, m, n, k, A, opA, B, opB, C, samples, F4J_CHECK_SEED, &rep->max_abs_err,
+                               &rep->max_rel_err);
+    if (rc || !(flags & F4J_CHECK_PLAIN)) return rc;
+    void* C2 = nullptr;
+    rc = f4j_dev_alloc(ctx, (size_t)m * n * (cplx ? 16 : 8), &C2);
+    if (rc) return rc;
+    rc = f4j_gemm_impl(ctx, cplx, m, n, k, A, opA, B, opB, (double*)C2, F4J_MODE_PLAIN, nullptr);
+    if (rc == F4J_OK)
+        rc = f4j_check_sampled(ctx, cplx, m, n, k, A, opA, B, opB, (const double*)C2, samples, F4J_CHECK_SEED,
+                               &rep->plain_max_abs_err, &rep->plain_max_rel_err);
+    f4j_dev_free(ctx, C2);
+    return rc;
+}
+
+static int dense_entry(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA, f4j_buf B,
+                       int opB, f4j_buf C, int mode, f4j_report* rep) {
+    int rc = check_gemm_args(ctx, cplx, m, n, k, A, opA, B, opB, C, mode);
+    if (rc) return rc;
+    if (rep && rep->check_samples < 0) return f4j_fail(F4J_ERR_ARG, "negative check_samples");
+    const int samples = rep ? rep->check_samples : 0, flags = rep ? rep->check_flags : 0;
+    F4J_CUDA(cudaSetDevice(ctx->device));
+    rc = f4j_gemm_impl(ctx, cplx, m, n, k, (const double*)A->ptr, opA, (const double*)B->ptr, opB,
+                       (double*)C->ptr, mode, rep);
+    if (rc) return rc;
+    return f4j_report_accuracy(ctx, cplx, m, n, k, (const double*)A->ptr, opA, (const double*)B->ptr, opB,
+                               (const double*)C->ptr, samples, flags, rep);
+}
+
 extern "C" int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                          f4j_buf B, int opB, f4j_buf C, int mode, f4j_report* rep) {
     F4J_LOCK(ctx);
-    int rc = check_gemm_args(ctx, false, m, n, k, A, opA, B, opB, C, mode);
-    if (rc) return rc;
-    F4J_CUDA(cudaSetDevice(ctx->device));
-    return f4j_gemm_impl(ctx, false, m, n, k, (const double*)A->ptr, opA, (const double*)B->ptr,
-                         opB, (double*)C->ptr, mode, rep);
+    return dense_entry(ctx, false, m, n, k, A, opA, B, opB, C, mode, rep);
 }
 
 extern "C" int f4j_zgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                          f4j_buf B, int opB, f4j_buf C, int mode, f4j_report* rep) {
     F4J_LOCK(ctx);
-    int rc = check_gemm_args(ctx, true, m, n, k, A, opA, B, opB, C, mode);
-    if (rc) return rc;
-    F4J_CUDA(cudaSetDevice(ctx->device));
-    return f4j_gemm_impl(ctx, true, m, n, k, (const double*)A->ptr, opA, (const double*)B->ptr,
-                         opB, (double*)C->ptr, mode, rep);
+    return dense_entry(ctx, true, m, n, k, A, opA, B, opB, C, mode, rep);
 }
 
 static int adjoint(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j_buf A, f4j_buf B,
@@ -577,7 +618,7 @@ static int adjoint(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, f4j
         if (rep) {
             *rep = f4j_report{};
             rep->flops = 2.0 * (cplx ? 8.0 : 2.0) * (double)m * (double)n * (double)k;
-            rep->mode_used = mode == F4J_MODE_AUTO && rep->flops / 2 <= (double)(1 << 24) ? F4J_MODE_EXACT : mode;
+            rep->mode_used = f4j_resolve_mode(cplx, m, k, n, mode);  // dA's shape; dB's resolves alike
             rep->launches = (int32_t)(ctx->launches - l0);
             if (g1 || g2) {
                 // the plans' headers: s, nrounds, ubits, nonfinite, spread (the gate is nonfinite)

@@ -14,6 +14,8 @@
 //  * k_gemv_rows / k_gemv_cols: matrix-vector products (n == 1) in the fast
 //    modes, FP64 FMA dot products reading A once.
 //  * k_gemm_check: double-double (Dot2) evaluation of sampled entries.
+#include <cstring>
+
 #include "f4j_internal.cuh"
 #include "f4j_ptx.cuh"
 
@@ -378,8 +380,9 @@ __global__ void k_gemm_check(int64_t m, int64_t n, int64_t k, const double* __re
     const int64_t s = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
     if (s >= samples) return;
-    const int64_t i = (int64_t)(mix64(seed ^ (2 * s)) % (uint64_t)m);
-    const int64_t j = (int64_t)(mix64(seed ^ (2 * s + 1)) % (uint64_t)n);
+    const uint64_t base = mix64(seed);  // every seed bit reaches the samples
+    const int64_t i = (int64_t)(mix64(base ^ (2 * s)) % (uint64_t)m);
+    const int64_t j = (int64_t)(mix64(base ^ (2 * s + 1)) % (uint64_t)n);
     DD re{0, 0}, im{0, 0};
     double absr = 0, absi = 0;
     for (int64_t q = lane; q < k; q += 32) {
@@ -601,6 +604,38 @@ int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, cons
     return F4J_OK;
 }
 
+int f4j_check_sampled(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                      const double* B, int opB, const double* C, int64_t samples, uint64_t seed, double* max_abs,
+                      double* max_rel) {
+    if (!cplx) {
+        if (opA == F4J_OP_C) opA = F4J_OP_T;
+        if (opB == F4J_OP_C) opB = F4J_OP_T;
+    }
+    const int64_t lda = (opA == F4J_OP_N) ? k : m;
+    const int64_t ldb = (opB == F4J_OP_N) ? n : k;
+    void* ws = nullptr;
+    int rc = f4j_dev_alloc(ctx, 16, &ws);
+    if (rc) return rc;
+    F4J_CUDA(cudaMemsetAsync(ws, 0, 16, ctx->stream));
+    const unsigned blocks = (unsigned)f4j_cdiv(samples, 4);
+    if (cplx)
+        k_gemm_check<true><<<blocks, 128, 0, ctx->stream>>>(m, n, k, A, lda, opA, B, ldb, opB, C, samples, seed,
+                                                             (unsigned long long*)ws);
+    else
+        k_gemm_check<false><<<blocks, 128, 0, ctx->stream>>>(m, n, k, A, lda, opA, B, ldb, opB, C, samples, seed,
+                                                              (unsigned long long*)ws);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, ws, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    f4j_dev_free(ctx, ws);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return f4j_cuda_fail(e, "sampled accuracy check");
+    memcpy(max_abs, &h[0], 8);
+    memcpy(max_rel, &h[1], 8);
+    return F4J_OK;
+}
+
 extern "C" int f4j_gemm_check(f4j_ctx* ctx, int cplx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
                               f4j_buf B, int opB, f4j_buf C, int64_t samples, uint64_t seed,
                               double* max_abs, double* max_rel) {
@@ -611,35 +646,9 @@ extern "C" int f4j_gemm_check(f4j_ctx* ctx, int cplx, int64_t m, int64_t n, int6
     size_t es = cplx ? 16 : 8;
     if ((size_t)m * k * es > A->bytes || (size_t)k * n * es > B->bytes || (size_t)m * n * es > C->bytes)
         return f4j_fail(F4J_ERR_ARG, "buffer too small");
-    if (!cplx) {
-        if (opA == F4J_OP_C) opA = F4J_OP_T;
-        if (opB == F4J_OP_C) opB = F4J_OP_T;
-    }
     F4J_CUDA(cudaSetDevice(ctx->device));
-    int64_t lda = (opA == F4J_OP_N) ? k : m;
-    int64_t ldb = (opB == F4J_OP_N) ? n : k;
-    void* ws;
-    int rc = f4j_workspace(ctx, 1, 16, &ws);
-    if (rc) return rc;
-    F4J_CUDA(cudaMemsetAsync(ws, 0, 16, ctx->stream));
-    unsigned blocks = (unsigned)f4j_cdiv(samples, 4);
-    if (cplx)
-        k_gemm_check<true><<<blocks, 128, 0, ctx->stream>>>(m, n, k, (const double*)A->ptr, lda, opA,
-                                                             (const double*)B->ptr, ldb, opB,
-                                                             (const double*)C->ptr, samples, seed,
-                                                             (unsigned long long*)ws);
-    else
-        k_gemm_check<false><<<blocks, 128, 0, ctx->stream>>>(m, n, k, (const double*)A->ptr, lda, opA,
-                                                              (const double*)B->ptr, ldb, opB,
-                                                              (const double*)C->ptr, samples, seed,
-                                                              (unsigned long long*)ws);
-    F4J_LAUNCHED(ctx);
-    unsigned long long h[2];
-    F4J_CUDA(cudaMemcpyAsync(h, ws, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    memcpy(max_abs, &h[0], 8);
-    memcpy(max_rel, &h[1], 8);
-    return F4J_OK;
+    return f4j_check_sampled(ctx, cplx != 0, m, n, k, (const double*)A->ptr, opA, (const double*)B->ptr, opB,
+                             (const double*)C->ptr, samples, seed, max_abs, max_rel);
 }
 
 int f4j_gemv(f4j_ctx* ctx, bool cplx, int64_t m, int64_t k, const double* A, int opA, const double* x, bool conj_x,

@@ -142,6 +142,15 @@ static inline int64_t f4j_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline bool f4j_aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 static inline bool f4j_aligned(const void* p, uintptr_t n) { return (reinterpret_cast<uintptr_t>(p) % n) == 0; }
 
+// The mode a dense product runs in: F4J_MODE_AUTO resolved by the dispatcher
+// configuration (f4j_config.cu); other modes unchanged.
+int f4j_resolve_mode(bool cplx, int64_t m, int64_t n, int64_t k, int mode);
+
+// Fills a dense product's report with its accuracy fields (check_samples,
+// check_flags as the caller set them; see f4j_report).
+int f4j_report_accuracy(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                        const double* B, int opB, const double* C, int samples, int flags, f4j_report* rep);
+
 // Internal GEMM entry points shared by the dense front ends.
 // `gate_out` (may be null): for a split product, the device word of its plan
 // that flags a NaN/Inf stand-down; the plan's header (s, nrounds, ubits,
@@ -157,6 +166,12 @@ int f4j_gemv(f4j_ctx* ctx, bool cplx, int64_t m, int64_t k, const double* A, int
              double* y);
 int f4j_gemm_dmma(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                   int opA, const double* B, int opB, double* C, const int* gate = nullptr);
+// Sampled accuracy of C = op(A) op(B): `samples` seeded entries evaluated in
+// double-double (Dot2) on the GPU; max |C - C_true| and max |C - C_true| /
+// sum|a||b| (synchronises the stream).
+int f4j_check_sampled(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                      const double* B, int opB, const double* C, int64_t samples, uint64_t seed, double* max_abs,
+                      double* max_rel);
 int f4j_gemm_exact(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
                    int opA, const double* B, int opB, double* C);
 int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,

@@ -225,16 +225,27 @@ __global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long l
 }
 
 // ------------------------------------------------------------------ plan
-// Slice count from the measured exponent spread sigma (bits between a row's
-// largest and its mean element exponent) and the inner dimension k.  The
-// truncation error of an element is 2^-F of its row's 2^e; it must stay below
-// the plain FP64 product's error, which grows with k while the truncation
-// error grows only with sqrt(k):  F >= max(48 + sigma, 54 + sigma - log2 k).
-__host__ __device__ inline int slices_for(double spread, int64_t k) {
-    const double sg = spread > 0 ? spread : 0.0;
+// Slice count from the measured exponent spreads sa, sb of op(A)'s rows and
+// op(B)'s columns (bits between the largest element exponent and the mean
+// exponent, maximised over rows / columns) and the length k of the sums (2k
+// for a complex product's concatenated K).  Error model, fitted on GB300 to
+// the largest sampled error |C - C_true| / sum|a||b| (double-double truth) of
+// split products with F = 4 + 5(s - 1) fraction bits:
+//   err(F) ~ 2.2e-16 * 2^(49 - F) * 2^(0.81 (sa + sb - 2.12)) * (k / 8192)^-0.36
+// (uniform and N(0,1) operands, k from 256 to 65536, s from 8 to 11; the
+// dropped slice products of level s + 2 dominate it).  The plain FP64 DMMA
+// product's error on the same scale measured 3.2e-16 .. 4.8e-16 over the same
+// range; s is the smallest count whose modelled error is at most 0.8 x 3.2e-16:
+//   F >= 51.74 + 0.81 (sa + sb) - 0.36 log2 k.
+// A second floor, F >= 54 + max(sa, sb) - floor(log2 k), keeps short sums
+// within the componentwise bound 2 k u |A||B|.
+__host__ __device__ inline int slices_for(double sa, double sb, int64_t k, int64_t klen) {
+    sa = sa > 0 ? sa : 0.0;
+    sb = sb > 0 ? sb : 0.0;
     int lk = 0;
     while (lk < 62 && (2ll << lk) <= k) lk++;  // floor(log2 k)
-    const double need = fmax(48.0 + sg, 54.0 + sg - (double)lk);
+    const double lklen = log2((double)(klen > 1 ? klen : 1));
+    const double need = fmax(51.74 + 0.81 * (sa + sb) - 0.36 * lklen, 54.0 + fmax(sa, sb) - (double)lk);
     int s = 1 + (int)ceil((need - 4.0) / 5.0);
     return s < 2 ? 2 : (s > S_MAX ? S_MAX : s);
 }
@@ -362,7 +373,8 @@ __global__ void k_plan(const int* __restrict__ misc, int64_t k, int64_t Kp, int6
                        int band, int kcb_cap, SplitPlan* __restrict__ plan) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
-    int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
+    int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req))
+                      : slices_for(misc[1] / 256.0, misc[2] / 256.0, k, klen_cat);
     int n = plan_build(s, Kp, klen_cat, plan, band, kcb_cap);
     plan->s = s;
     plan->nrounds = n < 0 ? 0 : n;
@@ -384,11 +396,12 @@ __global__ void k_plan_table(int64_t Kp, int64_t klen_cat, int band, int kcb_cap
 
 // One block of 128 threads: k_plan's result from a plan table (the slice count
 // from the statistics, that plan copied, the header filled in).
-__global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int s_req, const SplitPlan* __restrict__ tab,
-                            SplitPlan* __restrict__ plan) {
+__global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int64_t klen_cat, int s_req,
+                            const SplitPlan* __restrict__ tab, SplitPlan* __restrict__ plan) {
     if (blockIdx.x != 0) return;
     const double spread = (misc[1] > misc[2] ? misc[1] : misc[2]) / 256.0;
-    const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req)) : slices_for(spread, k);
+    const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req))
+                            : slices_for(misc[1] / 256.0, misc[2] / 256.0, k, klen_cat);
     const uint4* src = reinterpret_cast<const uint4*>(&tab[s]);
     uint4* dst = reinterpret_cast<uint4*>(plan);
 #pragma unroll 4
@@ -1117,7 +1130,8 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
             memcpy(ctx->plan_key[t], key, sizeof key);
             ctx->plan_valid[t] = true;
         }
-        k_plan_pick<<<1, 128, 0, ctx->stream>>>(misc, k, slices_req > 0 ? slices_req : env_slices(), tab, plan);
+        k_plan_pick<<<1, 128, 0, ctx->stream>>>(misc, k, klen_cat, slices_req > 0 ? slices_req : env_slices(), tab,
+                                                plan);
         F4J_LAUNCHED(ctx);
     }
     {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
@@ -1246,7 +1260,12 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     if (opA < F4J_OP_N || opA > F4J_OP_C || opB < F4J_OP_N || opB > F4J_OP_C) return f4j_fail(F4J_ERR_ARG, "bad op");
     if (mode < F4J_MODE_PLAIN || mode > F4J_MODE_EXACT) return f4j_fail(F4J_ERR_ARG, "bad mode %d", mode);
     F4J_CUDA(cudaSetDevice(ctx->device));
-    if (rep) *rep = f4j_report{};
+    if (rep && rep->check_samples < 0) return f4j_fail(F4J_ERR_ARG, "negative check_samples");
+    const int check_samples = rep ? rep->check_samples : 0, check_flags = rep ? rep->check_flags : 0;
+    if (rep) {
+        *rep = f4j_report{};
+        rep->max_abs_err = rep->max_rel_err = rep->plain_max_abs_err = rep->plain_max_rel_err = -1.0;
+    }
     if (m == 0 || n == 0) return F4J_OK;
     if (opA == F4J_OP_C) opA = F4J_OP_T;  // real data
     if (opB == F4J_OP_C) opB = F4J_OP_T;
@@ -1259,7 +1278,7 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
     if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
     const double work = 2.0 * (double)m * (double)n * (double)k;
-    const bool split = k > 0 && (mode == F4J_MODE_SPLIT || (mode == F4J_MODE_AUTO && work > (double)(1 << 24)));
+    const bool split = k > 0 && f4j_resolve_mode(false, m, n, k, mode) == F4J_MODE_SPLIT;
     const int tiles_m = (int)f4j_cdiv(m, BM);
     const int want = env_host_parts();
     const int parts = tiles_m < want ? tiles_m : want;
@@ -1271,7 +1290,8 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
         if (rc) return rc;
         F4J_CUDA(cudaMemcpyAsync(C, dC, cb, cudaMemcpyDeviceToHost, ctx->stream));
         F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-        return F4J_OK;
+        return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB,
+                                   (const double*)dC, check_samples, check_flags, rep);
     }
     const int64_t l0 = ctx->launches;
     SplitLaunch L;
@@ -1327,7 +1347,9 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
         rep->launches = (int32_t)(ctx->launches - l0);
     }
     F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    return rc;
+    if (rc) return rc;
+    return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (const double*)dC,
+                               check_samples, check_flags, rep);
 }
 
 // ------------------------------------------------------------------ no-allocation variant

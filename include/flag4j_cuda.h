@@ -51,24 +51,114 @@ extern "C" {
 
 #define F4J_MODE_PLAIN 0 /* FP64 DMMA tensor-core GEMM (mma.sync f64)                   */
 #define F4J_MODE_SPLIT 1 /* FP64-accurate split GEMM: FP8 slices on tcgen05, exact FP32 */
-#define F4J_MODE_AUTO 2  /* EXACT for tiny products (<= 2^24 flops); otherwise SPLIT for
-                            finite inputs and PLAIN when a NaN/Inf is present           */
+#define F4J_MODE_AUTO 2  /* the dispatcher configuration's choice (f4j_config_load): EXACT
+                            below smallThreshold entries or 2^24 flops; otherwise
+                            gpuGemmMode, by default SPLIT for finite inputs and PLAIN
+                            when a NaN/Inf is present                                   */
 #define F4J_MODE_EXACT 3 /* Flag4j's own order: k-ascending, no FMA -> bit-identical     */
 
 typedef struct f4j_ctx f4j_ctx;
 typedef struct f4j_buf_s* f4j_buf;
 typedef struct f4j_csr_s* f4j_csr;
 
-/* Optional per-call report (pass NULL to skip). */
+/* Optional per-call report (pass NULL to skip).  Zero it before the call; the
+ * call fills the outputs.  Accuracy report (f4j_dgemm, f4j_zgemm,
+ * f4j_dgemm_host; no counterpart in Flag4j): with check_samples > 0 the call
+ * also evaluates that many seeded entries of its result in double-double
+ * (compensated Dot2) on the GPU and reports the largest error, next to the
+ * componentwise bound a plain FP64 product guarantees on the same scale; with
+ * F4J_CHECK_PLAIN in check_flags it also runs the plain DMMA product into
+ * scratch memory and reports that product's error on the same entries.  The
+ * check costs one extra kernel and a wait (plus the plain product when asked);
+ * without it the call is unchanged. */
+#define F4J_CHECK_PLAIN 1
+/* Entry s (0-based) of a check is C[i][j] with b = mix(F4J_CHECK_SEED),
+ * i = mix(b ^ 2s) mod m, j = mix(b ^ (2s + 1)) mod n, mix the splitmix64
+ * finaliser (f4j_gemm_check samples the same way with its own seed). */
+#define F4J_CHECK_SEED 0x5EED0F4A6D5EEDull
 typedef struct f4j_report {
-    int32_t mode_used;   /* F4J_MODE_* that actually ran                          */
-    int32_t slices;      /* SPLIT: slice count s per operand                      */
-    int32_t launches;    /* kernels this call launched                            */
-    int32_t frac_bits;   /* SPLIT: fixed-point bits kept per element (4 + 5(s-1)) */
-    double flops;        /* algorithmic flops: 2mnk real, 8mnk complex, 2*nnz*cols */
-    double bytes;        /* algorithmic (compulsory) bytes of sparse products     */
-    double exp_spread;   /* SPLIT: measured exponent spread of the operands (bits) */
+    int32_t mode_used;        /* F4J_MODE_* that actually ran                             */
+    int32_t slices;           /* SPLIT: slice count s per operand                         */
+    int32_t launches;         /* kernels this call launched                               */
+    int32_t frac_bits;        /* SPLIT: fixed-point bits kept per element (4 + 5(s-1))    */
+    double flops;             /* algorithmic flops: 2mnk real, 8mnk complex, 2*nnz*cols   */
+    double bytes;             /* algorithmic (compulsory) bytes of sparse products        */
+    double exp_spread;        /* SPLIT: measured exponent spread of the operands (bits)   */
+    int32_t check_samples;    /* in: entries of C to check (0: no accuracy report)        */
+    int32_t check_flags;      /* in: F4J_CHECK_PLAIN                                      */
+    double max_abs_err;       /* out: max |C - C_true| over the checked entries           */
+    double max_rel_err;       /* out: max |C - C_true| / sum_k |a||b| over the same        */
+    double plain_bound_rel;   /* out: k u (real) or 2k u (complex, per part): the bound a  */
+                              /*      plain FP64 product guarantees, on max_rel_err's scale */
+    double plain_max_abs_err; /* out: the plain DMMA product's max_abs_err (F4J_CHECK_PLAIN; else -1) */
+    double plain_max_rel_err; /* out: the plain DMMA product's max_rel_err (F4J_CHECK_PLAIN; else -1) */
+    int32_t ref_kernel;       /* out: F4J_REF_* kernel Flag4j's dispatcher runs for these shapes */
+    int32_t reserved;
 } f4j_report;
+
+/* ---- dispatcher configuration (./configs/*.properties) ------------------- */
+/* Flag4j's dense-product dispatchers read java.util.Properties files from
+ * ./configs at class initialisation and fall back to defaults when a file is
+ * absent:
+ *   ReDeMatMult.properties    ReDeMatMultDispatchConfigs
+ *     (src/main/java/org/flag4j/linalg/ops/dispatch/configs/ReDeMatMultDispatchConfigs.java:52-121)
+ *   CmDeMatMult.properties    Cm128DeMatMultDispatchConfigs (same directory, :52-108)
+ *   GeneralConfigs.properties Configurations
+ *     (src/main/java/org/flag4j/concurrency/Configurations.java:65-88)
+ * This library reads the same files, keys, defaults and number syntax
+ * (Integer.parseInt / Double.parseDouble), plus the key
+ *   gpuGemmMode = auto | split | plain | exact
+ * (GeneralConfigs.properties for both dispatchers; ReDeMatMult.properties /
+ * CmDeMatMult.properties override it per dispatcher).  F4J_MODE_AUTO then
+ * resolves as the reference's dispatch() does first
+ * (ReDeMatMultDispatcher.java:157-171, Cm128DeMatMultDispatcher.java:155-170):
+ *   dataLength(A) + dataLength(B) < smallThreshold   -> F4J_MODE_EXACT
+ *   otherwise, products of at most 2^24 flops        -> F4J_MODE_EXACT
+ *   otherwise gpuGemmMode (auto: SPLIT, with PLAIN for NaN/Inf operands).
+ * The files are read on the first AUTO product from ./configs relative to the
+ * working directory (a malformed file there leaves the defaults), or when
+ * f4j_config_load is called. */
+typedef struct f4j_dispatch_config {
+    double cache_size;                       /* cacheSize (the reference's shape-cache size)      */
+    double aspect_threshold;                 /* aspectThreshold                                    */
+    int32_t small_threshold;                 /* smallThreshold: entries of A plus B                */
+    int32_t square_mt_standard_threshold;    /* squareMtStandardThreshold                          */
+    int32_t square_mt_reordered_threshold;   /* squareMtReorderedThreshold                         */
+    int32_t wide_mt_reordered_threshold;     /* wideMtReorderedThreshold                           */
+    int32_t square_sequential_vec_threshold; /* squareSequentialVecThreshold (real only)           */
+    int32_t min_dim_small_threshold;         /* minDimSmallThreshold                               */
+    int32_t gpu_gemm_mode;                   /* F4J_MODE_* that AUTO uses above the small rules   */
+    int32_t loaded;                          /* 1 when the dispatcher's file was read             */
+} f4j_dispatch_config;
+
+/* The CPU kernels the reference's dispatchers choose between
+ * (ReDeMatMultDispatcher.getFunc, ReDeMatMultDispatcher.java:184-237;
+ *  Cm128DeMatMultDispatcher.getFunc, Cm128DeMatMultDispatcher.java:184-226). */
+enum {
+    F4J_REF_STRD = 0, F4J_REF_REORD, F4J_REF_BLK, F4J_REF_BLK_REORD, F4J_REF_MT_STRD, F4J_REF_MT_REORD,
+    F4J_REF_MT_BLK, F4J_REF_MT_BLK_REORD, F4J_REF_STRD_VEC_AS_MAT, F4J_REF_BLK_VEC_AS_MAT,
+    F4J_REF_MT_STRD_VEC_AS_MAT, F4J_REF_MT_BLK_VEC_AS_MAT
+};
+
+/* Reads dir/ReDeMatMult.properties, dir/CmDeMatMult.properties and
+ * dir/GeneralConfigs.properties (dir NULL: "./configs"); absent files keep the
+ * defaults.  F4J_ERR_ARG (message with Java's NumberFormatException text) for
+ * a value Integer.parseInt / Double.parseDouble would reject, or a bad
+ * gpuGemmMode; the previous configuration then stays in force. */
+int f4j_config_load(const char* dir);
+/* Back to the built-in defaults (no files). */
+int f4j_config_reset(void);
+/* The configuration in force for real (cplx 0) or complex (cplx 1) products. */
+int f4j_config_get(int cplx, f4j_dispatch_config* out);
+/* GeneralConfigs.properties: blockSize and the resolved parallelism
+ * (ThreadManager.setParallelismLevel: values <= 0 mean processors + value, at least 1). */
+int f4j_config_general(int32_t* block_size, int32_t* parallelism);
+/* The mode a product C (m x n) = A (m x k) B (k x n) runs in under `mode`
+ * (F4J_MODE_AUTO resolved by the rules above), and the reference kernel
+ * (F4J_REF_*) Flag4j's dispatcher would run for the same shapes. */
+int f4j_dispatch(int cplx, int64_t m, int64_t n, int64_t k, int mode, int32_t* mode_out, int32_t* ref_kernel_out);
+/* Name of an F4J_REF_* kernel as the dispatcher spells it ("MT_BLK_REORD"). */
+const char* f4j_ref_kernel_name(int code);
 
 /* ---- library / context --------------------------------------------------- */
 int f4j_version(void); /* 10000*major + 100*minor + patch */

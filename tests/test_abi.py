@@ -40,4 +40,5 @@ def test_errors_without_device(lib):
 
 def test_report_struct_layout():
     from flag4j_gb300 import _lib
-    assert ctypes.sizeof(_lib.f4j_report) == 40
+    assert ctypes.sizeof(_lib.f4j_report) == 96
+    assert ctypes.sizeof(_lib.f4j_dispatch_config) == 48

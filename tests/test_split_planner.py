@@ -20,7 +20,7 @@ def test_split_planner_program_is_complete_and_in_range(tmp_path):
     csrc = os.path.join(ROOT, "flag4j_gb300", "csrc")
     cmd = ["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "--expt-relaxed-constexpr",
            "-I", os.path.join(ROOT, "include"), "-o", exe, os.path.join(HERE, "native", "split_plan_check.cu"),
-           os.path.join(csrc, "f4j_core.cu"), os.path.join(csrc, "f4j_dense.cu")]
+           os.path.join(csrc, "f4j_core.cu"), os.path.join(csrc, "f4j_dense.cu"), os.path.join(csrc, "f4j_config.cu")]
     subprocess.run(cmd, check=True, capture_output=True, timeout=600)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout[-2000:] + out.stderr[-2000:]
