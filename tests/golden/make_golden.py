@@ -16,6 +16,12 @@ Files read (paths within the Flag4j project):
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealCsrCsrMatMultTests.java
   src/test/java/org/flag4j/arrays/sparse/csr_matrix/RealComplexCsrCsrMatMultTests.java
 
+Matrix Market read fixtures ("matrix_market" key): the twelve input files
+MatrixMarketReadTests reads (src/test/java/org/flag4j/io/MatrixMarketReadTests.java,
+from src/test/data/matrix_market/{array,coordinate}/), each with its text and
+the expected result stated in src/test/java/org/flag4j/io/MatrixMarketMatrices.java
+(COO expectations sorted as that class's static block does with sortIndices).
+
 Usage:  python tests/golden/make_golden.py /path/to/flag4j
 The fixture is committed; the GPU machine never needs the reference tree.
 """
@@ -181,10 +187,79 @@ def cases_of(path, rel):
     return out
 
 
+MM_TESTS = T + "io/MatrixMarketReadTests.java"
+MM_MATRICES = T + "io/MatrixMarketMatrices.java"
+
+
+def mm_expected(src):
+    """The expected matrices of MatrixMarketMatrices.java, by field name:
+    {"kind": "dense" | "cdense" | "coo", "shape", "data" (dense: rows; coo: values),
+    "rows", "cols" (coo: sorted by (row, col), stable, as sortIndices does)}."""
+    out = {}
+    for m in re.finditer(r"static final (double\[\]\[\]|Complex128\[\]\[\]|CooMatrix|Matrix|CMatrix)\s+(\w+)\s*=", src):
+        typ, name = m.group(1), m.group(2)
+        p = m.end()
+        depth, q = 0, p
+        while True:  # the initialiser runs to the ';' at bracket depth 0
+            c = src[q]
+            depth += (c in "({") - (c in ")}")
+            if c == ";" and depth == 0:
+                break
+            q += 1
+        init = src[p:q].strip()
+        if typ in ("double[][]", "Complex128[][]"):
+            rows = Lit(init).value()
+        elif typ in ("Matrix", "CMatrix"):
+            inner = init[init.index("(") + 1:init.rindex(")")]
+            rows = Lit(inner).value()
+        else:  # CooMatrix(new Shape(r, c), new double[]{...}, new int[]{rows}, new int[]{cols})
+            shape = [int(v) for v in re.search(r"new Shape\((\d+),\s*(\d+)\)", init).groups()]
+            arrays = []
+            lit = Lit(init)
+            lit.p = init.index("new double[]")
+            for _ in range(3):
+                arrays.append(lit.value())
+                lit.ws()
+                if lit.peek(","):
+                    lit.eat(",")
+            vals, r, c = arrays
+            order = sorted(range(len(vals)), key=lambda i: (r[i], c[i]))  # stable, as CooDataSorter
+            out[name] = {"kind": "coo", "shape": shape, "data": [vals[i] for i in order],
+                         "rows": [int(r[i]) for i in order], "cols": [int(c[i]) for i in order]}
+            continue
+        cplx = typ.startswith("Complex") or typ == "CMatrix"
+        out[name] = {"kind": "cdense" if cplx else "dense", "shape": [len(rows), len(rows[0])], "data": rows}
+    return out
+
+
+def mm_cases(root):
+    tests = open(os.path.join(root, MM_TESTS)).read()
+    expected = mm_expected(open(os.path.join(root, MM_MATRICES)).read())
+    cases = []
+    methods = []
+    for m in re.finditer(r"@Test\s+void\s+(\w+)\s*\(\s*\)\s*(?:throws\s+\w+\s*)?\{", tests):
+        depth, p = 1, m.end()
+        while depth:
+            depth += (tests[p] == "{") - (tests[p] == "}")
+            p += 1
+        methods.append((m.group(1), tests[m.end():p - 1], tests[:m.end()].count("\n") + 1))
+    for name, body, line0 in methods:
+        for m in re.finditer(r'fileName\s*=\s*"\./(src/test/data/matrix_market/[^"]+)";\s*'
+                             r'exp\s*=\s*(?:new \w+\()?MatrixMarketMatrices\.(\w+)', body):
+            rel = m.group(1)
+            with open(os.path.join(root, rel)) as fh:
+                text = fh.read()
+            cases.append({"file": rel, "method": name, "test_file": MM_TESTS,
+                          "line": line0 + body[:m.start()].count("\n"), "expected_name": m.group(2),
+                          "expected": expected[m.group(2)], "text": text})
+    return cases
+
+
 def main(root):
     golden = {}
     for key, rel in FILES.items():
         golden[key] = cases_of(os.path.join(root, rel), rel)
+    golden["matrix_market"] = mm_cases(root)
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
     print({k: len(v) for k, v in golden.items()})

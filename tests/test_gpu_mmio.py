@@ -46,3 +46,33 @@ def test_complex_file_to_device_csr(f4j, oracle, tmp_path):
     assert np.array_equal(S.rowPointers, rp) and np.array_equal(S.colIndices, ci) and np.array_equal(S.data, vz)
     X = rng.standard_normal((cols, 4)) + 1j * rng.standard_normal((cols, 4))
     assert np.array_equal(S.mult(f4j.CMatrix(X)).toNumpy(), oracle.zspmm(rp, ci, vz, X))
+
+
+def _golden_coordinate_cases():
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "reference_golden.json")) as fh:
+        return [c for c in json.load(fh)["matrix_market"] if c["expected"]["kind"] == "coo"]
+
+
+@pytest.mark.parametrize("case", _golden_coordinate_cases(), ids=lambda c: c["file"].rsplit("/", 1)[-1])
+def test_reference_fixture_to_device_csr(f4j, oracle, case, tmp_path):
+    """The reference's coordinate fixtures (MatrixMarketReadTests, src/test/java/org/flag4j/io/
+    MatrixMarketReadTests.java:75-146) to CSR on the GPU: row pointers, column indices and values equal
+    CooMatrix.toCsr of the expected sorted triplets of MatrixMarketMatrices.java (the oracle's
+    restatement), and S x equals the oracle's SpMV on them bit for bit."""
+    from flag4j_gb300 import mmio
+    p = tmp_path / case["file"].rsplit("/", 1)[-1]
+    p.write_text(case["text"])
+    S = mmio.read_csr(str(p))
+    exp = case["expected"]
+    rows, cols = exp["shape"]
+    er = np.asarray(exp["rows"], np.int32)
+    rp = oracle.coo_to_csr(rows, er)
+    assert np.array_equal(S.rowPointers, rp)
+    assert np.array_equal(S.colIndices, np.asarray(exp["cols"], np.int32))
+    assert np.array_equal(S.data, np.asarray(exp["data"], np.float64))
+    x = np.random.default_rng(5).standard_normal(cols)
+    assert np.array_equal(S.mult(f4j.Vector(x)).data,
+                          oracle.spmv(rp, np.asarray(exp["cols"], np.int32), np.asarray(exp["data"]), x))
