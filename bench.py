@@ -233,7 +233,7 @@ def fp8_peak_from_file():
 # capture each (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass):
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
 #       -k regex:k_split_gemm -s 2 -c 1 python bench.py --skip-extras --steps 2 --warmup 3
-SPLIT_GEMM_DRAM_BYTES_8192 = {11: 15.077633e9 + 0.636095e9}
+SPLIT_GEMM_DRAM_BYTES_8192 = {11: 15.077633e9 + 0.636095e9, 10: 12.27e9 + 0.65615e9}
 
 # DRAM bytes of one 2^20-row, 32-column SpMM launch (k_spmm), exact and FMA
 # modes, from the ncu capture in profiles/k_spmm_k_spmv_1M_rows.md
