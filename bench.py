@@ -48,6 +48,10 @@ def parse():
     p.add_argument("--skip-extras", action="store_true", help="headline GEMM only (for profiling)")
     p.add_argument("--only-sparse", action="store_true", help="CSR products only (for profiling)")
     p.add_argument("--only-dmma", action="store_true", help="plain DMMA GEMM only (for profiling)")
+    p.add_argument("--only-spmv", action="store_true",
+                   help="SpMV alone at 2^20 rows, exact then FMA (for profiling; about 220 MB on the device)")
+    p.add_argument("--only-sddmm", action="store_true",
+                   help="SDDMM alone at 2^20 rows x 64 columns (for profiling; about 1.4 GB on the device)")
     return p.parse_args()
 
 
@@ -818,6 +822,42 @@ def run_dmma_only(args):
                       "steps": args.steps, "warmup": args.warmup}))
 
 
+def run_spmv_only(args):
+    """Profiling helper: SpMV y = S x at 2^20 rows, Poisson(16) row lengths (S is 200 MB, larger than
+    L2), `warmup` + `steps` exact launches, then as many FMA launches; prints its own numbers."""
+    from flag4j_gb300 import build, synth
+    build.build()
+    E = Eng(dist_env()[2])
+    rows = 1 << 20
+    rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
+    S = E.f.CsrMatrix((rows, rows), v, rp, ci)  # owns the handle's buffers: keep it alive
+    hS = S.handle(E.ctx)
+    x, y = E.dev(synth.normal(rows, 1, 5).ravel()), E.ctx.alloc(8 * rows)
+    out = {"kernel": "k_spmv", "rows": rows, "nnz": len(v)}
+    for name, mode in (("exact", E.L.SPARSE_EXACT), ("fma", E.L.SPARSE_FMA)):
+        out[name + "_ms"] = E.timed(lambda: E.check(E.lib.f4j_spmv_ex(E.ctx.handle, hS, x.handle, y.handle, mode,
+                                                                        None)), args.steps, args.warmup)
+    print(json.dumps(out))
+    del S
+
+
+def run_sddmm_only(args):
+    """Profiling helper: SDDMM on S's pattern at 2^20 rows x 64 columns, `warmup` + `steps` launches."""
+    from flag4j_gb300 import build, synth
+    build.build()
+    E = Eng(dist_env()[2])
+    rows = 1 << 20
+    rp, ci, v = synth.csr_poisson(rows, rows, seed=2024)
+    S = E.f.CsrMatrix((rows, rows), v, rp, ci)  # owns the handle's buffers: keep it alive
+    hS = S.handle(E.ctx)
+    A, B, o = E.dev(synth.normal(rows, 64, 9)), E.dev(synth.normal(rows, 64, 8)), E.ctx.alloc(8 * len(v))
+    ms = E.timed(lambda: E.check(E.lib.f4j_sddmm(E.ctx.handle, hS, A.handle, B.handle, 64, o.handle, None)),
+                 args.steps, args.warmup)
+    print(json.dumps({"kernel": "k_sddmm64s", "rows": rows, "nnz": len(v), "ms": ms,
+                      "fp64_lane_ops_per_s": 64.0 * len(v) / (ms * 1e-3)}))
+    del S
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -826,6 +866,10 @@ def main():
         run_sparse_only(args)
     elif args.only_dmma:
         run_dmma_only(args)
+    elif args.only_spmv:
+        run_spmv_only(args)
+    elif args.only_sddmm:
+        run_sddmm_only(args)
     else:
         run_ours(args)
 

@@ -22,84 +22,108 @@
 namespace {
 
 // ------------------------------------------------------------------ SpMV
-// Each warp owns 32 consecutive rows, one per lane, and walks their nonzeros
-// in chunks of up to CAP (normally the whole span at once):
-//   1. lanes copy the chunk's column indices and values to shared memory with
-//      asynchronous copies (coalesced, all in flight together);
-//   2. each lane gathers x[col] for its CAP/32 entries into registers, all
-//      gathers in flight together, and forms the rounded products v * x[col]
-//      in place (dense FP64 instructions);
-//   3. each lane adds its row's products in storage order.
-// Products and sums round exactly as RealCsrDenseMatMult.standardVector does,
-// so y is bit-identical.  With uniformly scattered columns the random 8-byte
-// gathers of x (one L2 sector each) bound the kernel; GB300's FP64 pipe
-// (2 lane-operations per clock per SM) comes next.
-// FUSED (the opt-in FMA mode) keeps values and gathered x and accumulates
-// fma(v, x, acc) in storage order, one FP64 instruction per nonzero instead
-// of two, within the reference's componentwise bound.
-constexpr int SPMV_WARPS = 8;
-template <bool FUSED>
-struct SpmvShape {
-    static constexpr int CAP = FUSED ? 576 : 640;  // entries per warp chunk, a multiple of 32
-    // shared memory per warp: values / products, column indices, gathered x (FUSED)
-    static constexpr size_t WARP_BYTES = (size_t)CAP * (FUSED ? 20 : 12);
-    static constexpr size_t SMEM = SPMV_WARPS * WARP_BYTES;
-};
+// Load-balanced lanes.  A warp owns rpw consecutive rows [w0, w1) with
+// nonzeros [E0, E1).  Lane l owns the rows whose first nonzero lies in
+// [E0 + ceil(l * span / 32), E0 + ceil((l + 1) * span / 32)), span = E1 - E0:
+// consecutive rows holding about span / 32 nonzeros, found by a lower-bound
+// search on the row pointers.  Rows of different lengths therefore share the
+// warp's work evenly (a lane per row made every warp wait for its longest
+// row: about 1.75 add steps per nonzero at Poisson(16) lengths).  Each lane
+// walks its contiguous nonzeros 8 at a time: column indices and values with
+// 16-byte loads (VEC; the loads of a group stay inside the arrays, entries
+// outside the lane's range are loaded and ignored), the 8 gathers of x in
+// flight together, then the products and the running sum in storage order,
+// storing y at each row end.  Each product and each sum is rounded as
+// RealCsrDenseMatMult.standardVector rounds them (acc starts at +0.0), so y is
+// bit-identical.  GB300's FP64 pipe (2 lane-operations per clock per SM, two
+// per nonzero) bounds the exact mode; the random 8-byte gathers of x (one L2
+// sector each) come next.  No shared memory, so L1 keeps its full size for
+// the gathers.
+// FUSED (the opt-in FMA mode) accumulates fma(v, x, acc) in the same order,
+// one FP64 instruction per nonzero, within the reference's componentwise bound.
+constexpr int SPMV_RPW_MAX = 256;  // rows per warp for large matrices
+constexpr int SPMV_BLOCK = 256;
 
-template <bool FUSED>
-__global__ void __launch_bounds__(SPMV_WARPS * 32)
-    k_spmv(int64_t rows, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+template <bool FUSED, bool VEC>
+__global__ void __launch_bounds__(SPMV_BLOCK, 4)
+    k_spmv(int64_t rows, int64_t nnz, int rpw, const int* __restrict__ rowptr, const int* __restrict__ colidx,
            const double* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
-    constexpr int CAP = SpmvShape<FUSED>::CAP, PER = CAP / 32;
-    extern __shared__ __align__(16) unsigned char spmv_smem[];
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    double* sv = reinterpret_cast<double*>(spmv_smem + warp * SpmvShape<FUSED>::WARP_BYTES);
-    int* si = reinterpret_cast<int*>(sv + CAP);
-    double* sx = reinterpret_cast<double*>(si + CAP);  // FUSED only
-    const int64_t wrow0 = ((int64_t)blockIdx.x * SPMV_WARPS + warp) * 32;
-    if (wrow0 >= rows) return;
-    const int64_t wrow1 = wrow0 + 32 < rows ? wrow0 + 32 : rows;
-    const int p0 = __ldg(&rowptr[wrow0]), p1 = __ldg(&rowptr[wrow1]);
-    const int64_t row = wrow0 + lane;
-    int q = p1, qend = p1;
-    if (row < rows) {
-        q = __ldg(&rowptr[row]);
-        qend = __ldg(&rowptr[row + 1]);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * SPMV_BLOCK + threadIdx.x) >> 5;
+    const int64_t w0 = warp * rpw;
+    if (w0 >= rows) return;
+    const int64_t w1 = w0 + rpw < rows ? w0 + rpw : rows;
+    const int64_t E0 = __ldg(rowptr + w0), span = (int64_t)__ldg(rowptr + w1) - E0;
+    // first row whose first nonzero is at or after this lane's target
+    const int64_t target = E0 + (span * lane + 31) / 32;
+    int64_t lo = w0, hi = w1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)__ldg(rowptr + mid) >= target) hi = mid;
+        else lo = mid + 1;
     }
+    const int64_t a = lo;
+    int64_t b = __shfl_down_sync(0xffffffffu, a, 1);
+    if (lane == 31) b = w1;
+    if (a >= b) return;
+    const int qs = __ldg(rowptr + a), qe = __ldg(rowptr + b);
+    // rend: end of row r; rnext: end of row r + 1, loaded one row ahead so that
+    // a row end never waits for a load on the running sum's chain
+    int64_t r = a;
+    int rend = __ldg(rowptr + a + 1);
+    int rnext = a + 1 < b ? __ldg(rowptr + a + 2) : qe;
     double acc = 0.0;
-    for (int c0 = p0; c0 < p1;) {
-        const int cn = (p1 - c0) < CAP ? (p1 - c0) : CAP;
-        for (int e = lane; e < cn; e += 32) {
-            cp_async4(&si[e], &colidx[c0 + e]);
-            cp_async8(&sv[e], &vals[c0 + e]);
-        }
-        cp_async_wait_all();
-        __syncwarp();
-        double xv[PER];
+    while (rend == qs) {  // empty rows before the lane's first nonzero
+        y[r] = 0.0;
+        if (++r == b) return;
+        rend = rnext;
+        rnext = r + 1 < b ? __ldg(rowptr + r + 2) : qe;
+    }
+    for (int qb = VEC ? (qs & ~3) : qs; qb < qe; qb += 8) {
+        int c[8];
+        double v[8];
+        if (VEC && (int64_t)qb + 8 <= nnz) {
+            const int4 c0 = __ldg(reinterpret_cast<const int4*>(colidx + qb));
+            const int4 c1 = __ldg(reinterpret_cast<const int4*>(colidx + qb + 4));
+            c[0] = c0.x, c[1] = c0.y, c[2] = c0.z, c[3] = c0.w, c[4] = c1.x, c[5] = c1.y, c[6] = c1.z, c[7] = c1.w;
 #pragma unroll
-        for (int u = 0; u < PER; u++) {
-            const int e = lane + 32 * u;
-            xv[u] = e < cn ? __ldg(&x[si[e]]) : 0.0;
-        }
+            for (int h = 0; h < 4; h++) {
+                const double2 vv = __ldg(reinterpret_cast<const double2*>(vals + qb) + h);
+                v[2 * h] = vv.x;
+                v[2 * h + 1] = vv.y;
+            }
+        } else {
 #pragma unroll
-        for (int u = 0; u < PER; u++) {
-            const int e = lane + 32 * u;
-            if (e < cn) {
-                if (FUSED) sx[e] = xv[u];
-                else sv[e] = __dmul_rn(sv[e], xv[u]);
+            for (int u = 0; u < 8; u++) {
+                const bool ok = qb + u < qe;
+                c[u] = ok ? __ldg(colidx + qb + u) : 0;
+                v[u] = ok ? __ldg(vals + qb + u) : 0.0;
             }
         }
-        __syncwarp();
-        const int cend = c0 + cn;
-        const int stop = qend < cend ? qend : cend;
-        if (FUSED)
-            for (; q < stop; q++) acc = __fma_rn(sv[q - c0], sx[q - c0], acc);
-        else
-            for (; q < stop; q++) acc = __dadd_rn(acc, sv[q - c0]);
-        __syncwarp();
-        c0 = cend;
+        double xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int q = qb + u;
+            xv[u] = (q >= qs && q < qe) ? __ldg(x + c[u]) : 0.0;
+        }
+        if (!FUSED) {
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = __dmul_rn(v[u], xv[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int q = qb + u;
+            if (q < qs || q >= qe) continue;
+            acc = FUSED ? __fma_rn(v[u], xv[u], acc) : __dadd_rn(acc, v[u]);
+            while (q + 1 == rend) {  // row r ends here (and any empty rows after it)
+                y[r] = acc;
+                acc = 0.0;
+                if (++r == b) break;
+                rend = rnext;
+                rnext = r + 1 < b ? __ldg(rowptr + r + 2) : qe;
+            }
+        }
     }
-    if (row < rows) y[row] = acc;
 }
 
 // ------------------------------------------------------------------ SpMM
@@ -248,35 +272,75 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// SDDMM with 64 columns, flat over the nonzeros: a warp takes 8 consecutive
-// nonzeros whatever their rows, a group of 4 lanes one nonzero, a lane 16
-// columns of the row of A and of the row of B (16-byte loads), 16 FMAs and a
-// 2-step tree sum: 18 FP64 warp instructions per 8 nonzeros, and no partly
-// filled groups at the ends of rows.  rowidx: the row of each nonzero.
-__global__ void __launch_bounds__(256)
-    k_sddmm64f(int64_t nnz, const int* __restrict__ rowidx, const int* __restrict__ colidx,
+// SDDMM with 64 columns, flat over the nonzeros: a block takes 64 consecutive
+// nonzeros whatever their rows, a group of 4 lanes one nonzero.  The block's
+// distinct rows of A (rows are sorted, so equal rows are adjacent) are staged
+// in shared memory once, so a lane holds only its 16 values of the row of B
+// in registers (60 registers and 4 blocks per SM, against 74 and about 20
+// warps per SM with A in registers too).  Lane l4 of a group owns the
+// 16-byte pairs l4, l4 + 4, ..., l4 + 28 of the 64 columns: the group's four
+// lanes read 64 contiguous bytes per step from shared memory and from B, and
+// the padded row stride (33 pairs) puts neighbouring rows in other banks.
+// 16 FMAs and a 2-step tree sum per lane: 18 FP64 warp instructions per 8
+// nonzeros.  The B loads are issued first, so they are in flight while the
+// block stages A.  rowidx: the row of each nonzero.
+constexpr int SD_NNZ = 64;        // nonzeros per block (256 threads)
+constexpr int SD_PAIRS = 33;      // padded row stride of the staged rows, in 16-byte pairs
+__global__ void __launch_bounds__(256, 4)
+    k_sddmm64s(int64_t nnz, const int* __restrict__ rowidx, const int* __restrict__ colidx,
                const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ out) {
-    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 4;
-    const int l4 = threadIdx.x % 4;
-    double2 a[8], b[8];
+    __shared__ double2 sA[SD_NNZ * SD_PAIRS];
+    __shared__ int slot[SD_NNZ], srow[SD_NNZ], s_nrows;
+    const int64_t q0 = (int64_t)blockIdx.x * SD_NNZ;
+    const int tid = threadIdx.x, g = tid >> 2, l4 = tid & 3;
+    const int64_t q = q0 + g;
+    double2 b[8];
     if (q < nnz) {
-        const double2* arow = reinterpret_cast<const double2*>(A + (int64_t)__ldg(&rowidx[q]) * 64) + l4 * 8;
-        const double2* brow = reinterpret_cast<const double2*>(B + (int64_t)__ldg(&colidx[q]) * 64) + l4 * 8;
+        const double2* brow = reinterpret_cast<const double2*>(B + (int64_t)__ldg(&colidx[q]) * 64) + l4;
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            a[u] = __ldg(arow + u);
-            b[u] = __ldg(brow + u);
-        }
+        for (int u = 0; u < 8; u++) b[u] = __ldg(brow + 4 * u);
     } else {
 #pragma unroll
-        for (int u = 0; u < 8; u++) a[u] = b[u] = make_double2(0.0, 0.0);
+        for (int u = 0; u < 8; u++) b[u] = make_double2(0.0, 0.0);
     }
-    // one chain: the FP64 pipe (2 lanes per clock per SM) bounds this kernel and
-    // other warps fill it while a chain waits, so a second chain's closing add
-    // would only cost an instruction
-    double s = 0.0;
+    if (tid < 32) {  // warp 0: slots of the block's nonzeros (two per lane) and the distinct rows
+        int r[2];
+        bool head[2];
 #pragma unroll
-    for (int u = 0; u < 8; u++) s = fma(a[u].y, b[u].y, fma(a[u].x, b[u].x, s));
+        for (int h = 0; h < 2; h++) {
+            const int t = tid + 32 * h;
+            const int64_t qq = q0 + t;
+            r[h] = qq < nnz ? __ldg(&rowidx[qq]) : -1;
+            head[h] = qq < nnz && (t == 0 || __ldg(&rowidx[qq - 1]) != r[h]);
+        }
+        const unsigned b0 = __ballot_sync(0xffffffffu, head[0]), b1 = __ballot_sync(0xffffffffu, head[1]);
+        const unsigned below = (1u << tid) - 1u;
+        const int n0 = __popc(b0);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int t = tid + 32 * h;
+            const int idx = (h ? n0 + __popc(b1 & below) : __popc(b0 & below)) + (head[h] ? 1 : 0) - 1;
+            slot[t] = idx;
+            if (head[h]) srow[idx] = r[h];
+        }
+        if (tid == 0) s_nrows = n0 + __popc(b1);
+    }
+    __syncthreads();
+    const int nrows = s_nrows;
+    for (int i = tid; i < nrows * 32; i += 256) {
+        const int rr = i >> 5, pr = i & 31;
+        sA[rr * SD_PAIRS + pr] = __ldg(reinterpret_cast<const double2*>(A + (int64_t)srow[rr] * 64) + pr);
+    }
+    __syncthreads();
+    double s = 0.0;
+    if (q < nnz) {
+        const double2* arow = sA + slot[g] * SD_PAIRS + l4;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const double2 a = arow[4 * u];
+            s = fma(a.y, b[u].y, fma(a.x, b[u].x, s));
+        }
+    }
     s += __shfl_xor_sync(0xffffffffu, s, 2);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     if (q < nnz && l4 == 0) out[q] = s;
@@ -1493,20 +1557,22 @@ extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mo
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     if (S->rows) {
-        const unsigned blocks = (unsigned)f4j_cdiv(S->rows, SPMV_WARPS * 32);
+        // rows per warp: as many as fill every SM's 4 blocks of 8 warps once
+        // (216 at 2^20 rows), so the SMs finish together; more rows per warp
+        // balance the lanes better, up to 256; at least 32
+        const int64_t slots = (int64_t)ctx->sm_count * 4 * (SPMV_BLOCK / 32);
+        int64_t rpw64 = f4j_cdiv(S->rows, slots);
+        const int rpw = (int)(rpw64 < 32 ? 32 : (rpw64 > SPMV_RPW_MAX ? SPMV_RPW_MAX : rpw64));
+        const unsigned blocks = (unsigned)f4j_cdiv(f4j_cdiv(S->rows, rpw), SPMV_BLOCK / 32);
         const bool fused = mode == F4J_SPARSE_FMA;
-        const size_t smem = fused ? SpmvShape<true>::SMEM : SpmvShape<false>::SMEM;
-        F4J_CUDA(cudaFuncSetAttribute(fused ? k_spmv<true> : k_spmv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+        // 16-byte loads of column indices and values when both arrays start 16-byte aligned
+        const bool vec = f4j_aligned16(S->colidx->ptr) && f4j_aligned16(S->vals->ptr);
+        auto kern = fused ? (vec ? k_spmv<true, true> : k_spmv<true, false>)
+                          : (vec ? k_spmv<false, true> : k_spmv<false, false>);
         f4j_prof_begin(ctx);
-        if (fused)
-            k_spmv<true><<<blocks, SPMV_WARPS * 32, smem, ctx->stream>>>(
-                S->rows, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
-                (const double*)x->ptr, (double*)y->ptr);
-        else
-            k_spmv<false><<<blocks, SPMV_WARPS * 32, smem, ctx->stream>>>(
-                S->rows, (const int*)S->rowptr->ptr, (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
-                (const double*)x->ptr, (double*)y->ptr);
+        kern<<<blocks, SPMV_BLOCK, 0, ctx->stream>>>(S->rows, S->nnz, rpw, (const int*)S->rowptr->ptr,
+                                                     (const int*)S->colidx->ptr, (const double*)S->vals->ptr,
+                                                     (const double*)x->ptr, (double*)y->ptr);
         f4j_prof_end(ctx);
         F4J_LAUNCHED(ctx);
     }
@@ -1625,7 +1691,7 @@ extern "C" int f4j_sddmm(f4j_ctx* ctx, f4j_csr S, f4j_buf A, f4j_buf B, int64_t 
         if (ncols == 64 && ((reinterpret_cast<uintptr_t>(A->ptr) | reinterpret_cast<uintptr_t>(B->ptr)) & 15) == 0) {
             int rc = ensure_rowidx(ctx, S);
             if (rc) return rc;
-            k_sddmm64f<<<(unsigned)f4j_cdiv(S->nnz * 4, 256), 256, 0, ctx->stream>>>(
+            k_sddmm64s<<<(unsigned)f4j_cdiv(S->nnz, SD_NNZ), 256, 0, ctx->stream>>>(
                 S->nnz, (const int*)S->rowidx, (const int*)S->colidx->ptr, (const double*)A->ptr,
                 (const double*)B->ptr, (double*)out->ptr);
         } else

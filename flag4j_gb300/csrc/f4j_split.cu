@@ -144,11 +144,12 @@ __device__ __forceinline__ void stat_elem(double x, unsigned long long& mx, long
     }
 }
 
-// One warp per stored row: stats of stored rows.
-__global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
-                             unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
-                             int* __restrict__ cnt_out, int* __restrict__ bad_out) {
-    int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+// One warp per stored row: stats of stored rows (block blk covers rows 8 blk .. 8 blk + 7).
+__device__ __forceinline__ void stats_rows_body(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
+                                                int64_t blk, unsigned long long* __restrict__ mx_out,
+                                                long long* __restrict__ esum_out, int* __restrict__ cnt_out,
+                                                int* __restrict__ bad_out) {
+    int64_t r = blk * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x % 32;
     if (r >= rows) return;
     unsigned long long mx = 0;
@@ -172,13 +173,21 @@ __global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t
     }
 }
 
-// Thread per stored column, blockIdx.y over chunks of `chunk` rows: stats of stored columns.
-__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx, int chunk,
+__global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
                              unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
                              int* __restrict__ cnt_out, int* __restrict__ bad_out) {
-    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    stats_rows_body(X, rows, cols, cplx, blockIdx.x, mx_out, esum_out, cnt_out, bad_out);
+}
+
+// Thread per stored column, block (bx, by) over chunks of `chunk` rows: stats of stored columns.
+__device__ __forceinline__ void stats_cols_body(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
+                                                int chunk, int64_t bx, int64_t by,
+                                                unsigned long long* __restrict__ mx_out,
+                                                long long* __restrict__ esum_out, int* __restrict__ cnt_out,
+                                                int* __restrict__ bad_out) {
+    int64_t c = bx * blockDim.x + threadIdx.x;
     if (c >= cols) return;
-    int64_t r0 = (int64_t)blockIdx.y * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
+    int64_t r0 = by * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
     unsigned long long mx = 0;
     long long es = 0;
     int cnt = 0, bad = 0;
@@ -198,11 +207,43 @@ __global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t
     if (bad) atomicExch(bad_out, 1);
 }
 
-// Exponent bound e (max|x| < 2^e) per target, spread (x256, max-reduced).
-__global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long long* __restrict__ mx,
-                                 const long long* __restrict__ esum, const int* __restrict__ cnt,
-                                 int* __restrict__ e_out, int* __restrict__ spread_x256) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx, int chunk,
+                             unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
+                             int* __restrict__ cnt_out, int* __restrict__ bad_out) {
+    stats_cols_body(X, rows, cols, cplx, chunk, blockIdx.x, blockIdx.y, mx_out, esum_out, cnt_out, bad_out);
+}
+
+// One operand's statistics pass inside k_stats_pair: stored rows (a warp per
+// row, 8 rows a block) or stored columns (a thread per column, gx column
+// blocks by row chunks of `chunk`), `blocks` blocks in all.
+struct StatsPass {
+    const double* X;
+    int64_t rows, cols;
+    int cplx, by_rows, chunk;
+    int64_t gx, blocks;
+    unsigned long long* mx;
+    long long* es;
+    int* cn;
+};
+
+// Both operands' statistics in one launch: blocks [0, a.blocks) run A's pass,
+// the rest B's.
+__global__ void __launch_bounds__(256, 8) k_stats_pair(const StatsPass a, const StatsPass b,
+                                                       int* __restrict__ bad_out) {
+    int64_t blk = blockIdx.x;
+    const bool second = blk >= a.blocks;
+    const StatsPass op = second ? b : a;
+    if (second) blk -= a.blocks;
+    if (op.by_rows) stats_rows_body(op.X, op.rows, op.cols, op.cplx, blk, op.mx, op.es, op.cn, bad_out);
+    else stats_cols_body(op.X, op.rows, op.cols, op.cplx, op.chunk, blk % op.gx, blk / op.gx, op.mx, op.es, op.cn,
+                         bad_out);
+}
+
+// Exponent bound e (max|x| < 2^e) of target t, and its spread (x256).
+__device__ __forceinline__ int finalize_target(int64_t t, int64_t targets, int dup,
+                                               const unsigned long long* __restrict__ mx,
+                                               const long long* __restrict__ esum, const int* __restrict__ cnt,
+                                               int* __restrict__ e_out) {
     int sp = 0;
     if (t < targets) {
         unsigned long long b = mx[t];
@@ -221,6 +262,15 @@ __global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long l
         int o = __shfl_xor_sync(0xffffffffu, sp, off);
         sp = o > sp ? o : sp;
     }
+    return sp;
+}
+
+// Exponent bound e (max|x| < 2^e) per target, spread (x256, max-reduced).
+__global__ void k_stats_finalize(int64_t targets, int dup, const unsigned long long* __restrict__ mx,
+                                 const long long* __restrict__ esum, const int* __restrict__ cnt,
+                                 int* __restrict__ e_out, int* __restrict__ spread_x256) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int sp = finalize_target(t, targets, dup, mx, esum, cnt, e_out);
     if ((threadIdx.x & 31) == 0 && sp) atomicMax(spread_x256, sp);
 }
 
@@ -416,6 +466,56 @@ __global__ void k_plan_pick(const int* __restrict__ misc, int64_t k, int64_t kle
     }
 }
 
+// Both operands' exponent bounds and spreads, then the plan, in one launch:
+// blocks [0, cdiv(ta, 256)) finalise op(A)'s targets, the rest op(B)'s (dupb:
+// the complex B_cat's targets appear twice).  Each block counts itself done
+// on misc[4] (zeroed with misc before the statistics); the block that counts
+// last has seen every spread and picks the plan as k_plan_pick does.  No
+// block waits for another.
+__global__ void __launch_bounds__(256) k_finalize_pick(int64_t ta, int64_t tb, int dupb,
+                                                       const unsigned long long* __restrict__ mxa,
+                                                       const long long* __restrict__ esa,
+                                                       const int* __restrict__ cna,
+                                                       const unsigned long long* __restrict__ mxb,
+                                                       const long long* __restrict__ esb,
+                                                       const int* __restrict__ cnb, int* __restrict__ ea,
+                                                       int* __restrict__ eb, int* misc, int64_t k,
+                                                       int64_t klen_cat, int s_req,
+                                                       const SplitPlan* __restrict__ tab,
+                                                       SplitPlan* __restrict__ plan) {
+    const int64_t nba = (ta + 255) / 256;
+    const bool is_b = (int64_t)blockIdx.x >= nba;
+    const int64_t t = ((int64_t)blockIdx.x - (is_b ? nba : 0)) * 256 + threadIdx.x;
+    const int sp = is_b ? finalize_target(t, tb, dupb, mxb, esb, cnb, eb)
+                        : finalize_target(t, ta, 0, mxa, esa, cna, ea);
+    if ((threadIdx.x & 31) == 0 && sp) atomicMax(&misc[is_b ? 2 : 1], sp);
+    __shared__ int last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&misc[4], 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // every block's spreads are in; read them past L1
+    const int sa = atomicAdd(&misc[1], 0), sb = atomicAdd(&misc[2], 0), bad = atomicAdd(&misc[0], 0);
+    const double spread = (sa > sb ? sa : sb) / 256.0;
+    const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req))
+                            : slices_for(sa / 256.0, sb / 256.0, k, klen_cat);
+    const uint4* src = reinterpret_cast<const uint4*>(&tab[s]);
+    uint4* dst = reinterpret_cast<uint4*>(plan);
+    for (int i = threadIdx.x; i < (int)(sizeof(SplitPlan) / 16); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int n = tab[s].nrounds;
+        plan->s = s;
+        plan->nrounds = n < 0 ? 0 : n;
+        plan->spread = (float)spread;
+        plan->nonfinite = (bad != 0 || n < 0) ? 1 : 0;
+    }
+}
+
 // ------------------------------------------------------------------ split
 
 // Exact float of an integer |d| < 2^22: d added to the bit pattern of 1.5 * 2^23.
@@ -466,16 +566,16 @@ constexpr int SP_TR = 32, SP_TQ = 64;  // tile: 32 target rows x 64 k-indices
 //   role 0 (A_cat): complex value (re, im) -> out[r][q] = re, out[r][Kh+q] = im
 //   role 1 (B_cat^T): -> out[r][q] = re, out[r][Kh+q] = -im,
 //                        out[n+r][q] = im, out[n+r][Kh+q] = re
-__global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int64_t srows, int64_t scols,
-                                               int transposed, int cplx, int conj, int role,
-                                               int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
-                                               int64_t rows_out, const int* __restrict__ e_t,
-                                               const SplitPlan* __restrict__ plan, uint8_t* __restrict__ out) {
+__device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t srows, int64_t scols,
+                                           int transposed, int cplx, int conj, int role, int64_t targets,
+                                           int64_t klen, int64_t Kh, int64_t Kp, int64_t rows_out,
+                                           const int* __restrict__ e_t, const SplitPlan* __restrict__ plan,
+                                           uint8_t* __restrict__ out, int64_t bx, int64_t by) {
     __shared__ double sre[SP_TR][SP_TQ + 1];
     __shared__ double sim[SP_TR][SP_TQ + 1];
     if (plan->nonfinite) return;
     const int s = plan->s;
-    const int64_t r0 = (int64_t)blockIdx.y * SP_TR, q0 = (int64_t)blockIdx.x * SP_TQ;
+    const int64_t r0 = by * SP_TR, q0 = bx * SP_TQ;
     // ---- stage the tile (zeros outside the matrix)
     for (int e = threadIdx.x; e < SP_TR * SP_TQ; e += 256) {
         int rr, qq;
@@ -551,6 +651,43 @@ __global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int
         for (int j = 0; j < 8; j++)
             f[j] = float_of_small_int(s - 1 < 6 ? L[j] + H[j] * (1 << (30 - 5 * (s - 1))) : H[j]);
         store_e4m3x8(base, f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int64_t srows, int64_t scols,
+                                               int transposed, int cplx, int conj, int role,
+                                               int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
+                                               int64_t rows_out, const int* __restrict__ e_t,
+                                               const SplitPlan* __restrict__ plan, uint8_t* __restrict__ out) {
+    split_body(X, srows, scols, transposed, cplx, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
+               blockIdx.x, blockIdx.y);
+}
+
+// One operand of k_split_pair (the arguments k_split takes for it).
+struct SplitOperand {
+    const double* X;
+    int64_t srows, scols;
+    int transposed, conj, role;
+    int64_t targets, rows_out;
+    const int* e_t;
+    uint8_t* out;
+};
+
+// Both operands' slice planes in one launch: blockIdx.z = 0 slices op(A), 1
+// op(B)_cat^T; blocks past an operand's targets return at once.
+__global__ void __launch_bounds__(256) k_split_pair(const SplitOperand a, const SplitOperand b, int cplx, int64_t klen,
+                                                    int64_t Kh, int64_t Kp, const SplitPlan* __restrict__ plan) {
+    // one inlined copy of the body per operand, each reading its own kernel
+    // parameters directly (selecting the operand first kept every field in
+    // registers: 60 registers against 35, and fewer blocks per SM)
+    if (blockIdx.z == 0) {
+        if ((int64_t)blockIdx.y * SP_TR >= a.targets) return;
+        split_body(a.X, a.srows, a.scols, a.transposed, cplx, a.conj, a.role, a.targets, klen, Kh, Kp, a.rows_out,
+                   a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
+    } else {
+        if ((int64_t)blockIdx.y * SP_TR >= b.targets) return;
+        split_body(b.X, b.srows, b.scols, b.transposed, cplx, b.conj, b.role, b.targets, klen, Kh, Kp, b.rows_out,
+                   b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
     }
 }
 
@@ -1053,6 +1190,32 @@ static void launch_stats_cols(const double* X, int64_t rows, int64_t cols, int c
                                                                                       mx, es, cn, bad);
 }
 
+// One operand's pass of k_stats_pair, with launch_stats_cols's chunking for columns.
+static StatsPass stats_pass(const double* X, int64_t rows, int64_t cols, bool cplx, bool by_rows, int sm_count,
+                            unsigned long long* mx, long long* es, int* cn) {
+    StatsPass p{};
+    p.X = X;
+    p.rows = rows;
+    p.cols = cols;
+    p.cplx = cplx ? 1 : 0;
+    p.by_rows = by_rows ? 1 : 0;
+    p.mx = mx;
+    p.es = es;
+    p.cn = cn;
+    if (by_rows) {
+        p.gx = 1;
+        p.blocks = f4j_cdiv(rows, 8);
+    } else {
+        const int64_t bx = f4j_cdiv(cols, 256);
+        int64_t chunk = 256;
+        while (chunk > 16 && bx * f4j_cdiv(rows, chunk) < 4 * (int64_t)sm_count) chunk /= 2;
+        p.chunk = (int)chunk;
+        p.gx = bx;
+        p.blocks = bx * f4j_cdiv(rows, chunk);
+    }
+    return p;
+}
+
 static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                          const double* B, int opB, double* C, int slices_req, SplitLaunch* L) {
     const int64_t M = m, N = cplx ? 2 * n : n;
@@ -1092,31 +1255,22 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     uint8_t* slA = (uint8_t*)ws0;
     uint8_t* slB = slA + al1k(plane_a * S_MAX);
 
-    F4J_CUDA(cudaMemsetAsync(w, 0, off_ea, ctx->stream));
-    F4J_CUDA(cudaMemsetAsync(w + off_misc, 0, 1024, ctx->stream));
+    // statistics accumulate with atomics and misc holds flags and the block
+    // counter of k_finalize_pick: one clear of everything up to the plan
+    F4J_CUDA(cudaMemsetAsync(w, 0, off_plan, ctx->stream));
 
     const bool a_rows = (opA == F4J_OP_N);  // targets of A (rows of op(A)) are stored rows
     const bool b_rows = (opB != F4J_OP_N);  // targets of B (columns of op(B)) are stored rows
     f4j_prof_begin(ctx, F4J_PROF_PREP);
-    if (a_rows) {
-        k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
-    } else {
-        launch_stats_cols(A, k, M, cplx, ctx->sm_count, mxa, esa, cna, misc, ctx->stream);
+    {   // both operands' statistics in one launch
+        StatsPass pa = stats_pass(A, a_rows ? M : k, a_rows ? k : M, cplx, a_rows, ctx->sm_count, mxa, esa, cna);
+        StatsPass pb = stats_pass(B, b_rows ? n : k, b_rows ? k : n, cplx, b_rows, ctx->sm_count, mxb, esb, cnb);
+        k_stats_pair<<<(unsigned)(pa.blocks + pb.blocks), 256, 0, ctx->stream>>>(pa, pb, misc);
+        F4J_LAUNCHED(ctx);
     }
-    F4J_LAUNCHED(ctx);
-    if (b_rows) {
-        k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, ctx->stream>>>(B, n, k, cplx, mxb, esb, cnb, misc);
-    } else {
-        launch_stats_cols(B, k, n, cplx, ctx->sm_count, mxb, esb, cnb, misc, ctx->stream);
-    }
-    F4J_LAUNCHED(ctx);
-    k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, ctx->stream>>>(M, 0, mxa, esa, cna, ea, misc + 1);
-    F4J_LAUNCHED(ctx);
-    k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, ctx->stream>>>(n, cplx ? 1 : 0, mxb, esb, cnb, eb,
-                                                                          misc + 2);
-    F4J_LAUNCHED(ctx);
-    {   // the plan: from the context's table of plans for every slice count,
-        // rebuilt when the key changes (the one-thread build takes ~10 us)
+    {   // exponents, spreads and the plan in one launch: the plan comes from the
+        // context's table of plans for every slice count, rebuilt when the key
+        // changes (the one-thread build takes ~10 us)
         const int t = ctx->ws_base ? 1 : 0;
         const long long key[4] = {(long long)Kp, (long long)klen_cat, (long long)env_band(), (long long)kcb_cap};
         if (!ctx->plan_tab[t]) {
@@ -1130,20 +1284,23 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
             memcpy(ctx->plan_key[t], key, sizeof key);
             ctx->plan_valid[t] = true;
         }
-        k_plan_pick<<<1, 128, 0, ctx->stream>>>(misc, k, klen_cat, slices_req > 0 ? slices_req : env_slices(), tab,
-                                                plan);
+        const unsigned blocks = (unsigned)(f4j_cdiv(M, 256) + f4j_cdiv(n, 256));
+        k_finalize_pick<<<blocks, 256, 0, ctx->stream>>>(M, n, cplx ? 1 : 0, mxa, esa, cna, mxb, esb, cnb, ea, eb,
+                                                         misc, k, klen_cat,
+                                                         slices_req > 0 ? slices_req : env_slices(), tab, plan);
         F4J_LAUNCHED(ctx);
     }
-    {   // A: targets = rows of op(A); stored m x k (N) or k x m (T/C)
-        dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR));
-        k_split<<<g, 256, 0, ctx->stream>>>(A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, cplx,
-                                            opA == F4J_OP_C, 0, M, k, Kh, Kp, M, ea, plan, slA);
-        F4J_LAUNCHED(ctx);
-    }
-    {   // B: targets = columns of op(B); stored k x n (N, transposed read) or n x k (T/C)
-        dim3 g((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(n, SP_TR));
-        k_split<<<g, 256, 0, ctx->stream>>>(B, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, cplx,
-                                            opB == F4J_OP_C, 1, n, k, Kh, Kp, N, eb, plan, slB);
+    {   // both operands' slice planes in one launch.  A: targets = rows of op(A),
+        // stored m x k (N) or k x m (T/C); B: targets = columns of op(B), stored
+        // k x n (N, transposed read) or n x k (T/C)
+        const SplitOperand sa{A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, opA == F4J_OP_C ? 1 : 0, 0, M, M,
+                              ea, slA};
+        const SplitOperand sb{B, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, opB == F4J_OP_C ? 1 : 0, 1, n, N,
+                              eb, slB};
+        const int64_t gy = f4j_cdiv(M > n ? M : n, SP_TR);
+        if (gy > 65535) return f4j_fail(F4J_ERR_ARG, "split GEMM: %lld rows exceed the slicing grid", (long long)(M > n ? M : n));
+        k_split_pair<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)gy, 2), 256, 0, ctx->stream>>>(sa, sb, cplx, k, Kh, Kp,
+                                                                                          plan);
         F4J_LAUNCHED(ctx);
     }
     f4j_prof_end(ctx);

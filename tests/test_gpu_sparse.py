@@ -569,3 +569,29 @@ def test_coo_to_csr_range_checks_report_first_bad_entry(f4j):
     assert S.rowPointers[-1] == n
     assert np.array_equal(np.diff(S.rowPointers), np.bincount(r, minlength=rows))
     assert np.array_equal(S.colIndices, c) and np.array_equal(S.data, v)
+
+
+@pytest.mark.parametrize("rows,lam,p_empty", [(255, 16, 0.0), (256, 16, 0.1), (257, 16, 0.5), (513, 0.5, 0.5),
+                                              (3000, 5, 0.9), (2000, 16, 0.02)])
+def test_spmv_balanced_lanes_edge_shapes(f4j, oracle, rows, lam, p_empty):
+    """The SpMV kernel splits each 256-row block between its 32 lanes by nonzero
+    count: blocks of empty rows across block and lane boundaries, trailing empty
+    rows and one 3000-nonzero row among short ones stay bit-identical (and within
+    the bound in FMA mode)."""
+    rng = np.random.default_rng(rows)
+    lens = rng.poisson(lam, rows)
+    lens[rng.random(rows) < p_empty] = 0
+    lens[rows // 3: rows // 3 + rows // 5] = 0
+    lens[-3:] = 0
+    lens[rng.integers(0, rows - 3)] = 3000
+    cols = 4000
+    rp = np.zeros(rows + 1, np.int32)
+    np.cumsum(lens, out=rp[1:])
+    ci = np.concatenate([np.sort(rng.choice(cols, n, replace=False)) for n in lens]).astype(np.int32)
+    v = rng.standard_normal(len(ci))
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    x = rng.standard_normal(cols)
+    ref = oracle.spmv(rp, ci, v, x)
+    assert np.array_equal(S.mult(f4j.Vector(x)).data, ref)
+    y = S.mult(f4j.Vector(x), mode="fma").data
+    assert np.all(np.abs(y - ref) <= fma_bound(oracle, rp, ci, v, x[:, None])[:, 0])
