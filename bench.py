@@ -240,7 +240,7 @@ def fp8_peak_from_file():
 SPLIT_GEMM_DRAM_BYTES_8192 = {11: 15.077633e9 + 0.636095e9, 10: 12.27e9 + 0.65615e9}
 
 # DRAM bytes of one 2^20-row, 32-column SpMM launch (k_spmm), exact and FMA
-# modes, from the ncu capture in profiles/k_spmm_k_spmv_1M_rows.md
+# modes, from the ncu capture in profiles/k_spmm_1M_rows_32cols.md
 SPMM_DRAM_BYTES_1M = {"exact": 3.255e9 + 0.266e9, "fma": 3.257e9 + 0.265e9}
 # FP64-pipe activity of the same launches (sm__pipe_fp64_cycles_active, of active cycles)
 SPMM_FP64_PIPE_1M = {"exact": 0.839, "fma": 0.933}

@@ -44,8 +44,15 @@ namespace {
 constexpr int SPMV_RPW_MAX = 256;  // rows per warp for large matrices
 constexpr int SPMV_BLOCK = 256;
 
+// Blocks per SM: 5 for the exact mode (48 registers, no spills), 4 for FMA
+// (whose 48-register build spills).
+template <bool FUSED>
+struct SpmvOcc {
+    static constexpr int BLOCKS = FUSED ? 4 : 5;
+};
+
 template <bool FUSED, bool VEC>
-__global__ void __launch_bounds__(SPMV_BLOCK, 4)
+__global__ void __launch_bounds__(SPMV_BLOCK, SpmvOcc<FUSED>::BLOCKS)
     k_spmv(int64_t rows, int64_t nnz, int rpw, const int* __restrict__ rowptr, const int* __restrict__ colidx,
            const double* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
     const int lane = threadIdx.x & 31;
@@ -1557,10 +1564,11 @@ extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mo
     F4J_CUDA(cudaSetDevice(ctx->device));
     int64_t l0 = ctx->launches;
     if (S->rows) {
-        // rows per warp: as many as fill every SM's 4 blocks of 8 warps once
-        // (216 at 2^20 rows), so the SMs finish together; more rows per warp
-        // balance the lanes better, up to 256; at least 32
-        const int64_t slots = (int64_t)ctx->sm_count * 4 * (SPMV_BLOCK / 32);
+        // rows per warp: as many as fill every SM's resident blocks of 8 warps
+        // once (173 exact / 216 FMA at 2^20 rows), so the SMs finish together;
+        // more rows per warp balance the lanes better, up to 256; at least 32
+        const int bps = mode == F4J_SPARSE_FMA ? SpmvOcc<true>::BLOCKS : SpmvOcc<false>::BLOCKS;
+        const int64_t slots = (int64_t)ctx->sm_count * bps * (SPMV_BLOCK / 32);
         int64_t rpw64 = f4j_cdiv(S->rows, slots);
         const int rpw = (int)(rpw64 < 32 ? 32 : (rpw64 > SPMV_RPW_MAX ? SPMV_RPW_MAX : rpw64));
         const unsigned blocks = (unsigned)f4j_cdiv(f4j_cdiv(S->rows, rpw), SPMV_BLOCK / 32);
