@@ -156,9 +156,12 @@ class Eng:
     def dev(self, arr):
         return self.ctx.from_numpy(arr)
 
-    def gemm(self, A, B, C, m, n, k, mode, cplx=False, opA=0, opB=0, report=False):
-        """One product; with report=True the call also fills (and waits for) the report."""
+    def gemm(self, A, B, C, m, n, k, mode, cplx=False, opA=0, opB=0, report=False, check_samples=0):
+        """One product; with report=True the call also fills (and waits for) the report, and with
+        check_samples > 0 the report carries the sampled double-double error of this result."""
         rep = self.L.f4j_report() if report else None
+        if report:
+            rep.check_samples = check_samples
         fn = self.lib.f4j_zgemm if cplx else self.lib.f4j_dgemm
         self.check(fn(self.ctx.handle, m, n, k, A.handle, opA, B.handle, opB, C.handle, mode,
                       ctypes.byref(rep) if report else None))
@@ -632,6 +635,13 @@ def run_ours(args):
     flops = 2.0 * n ** 3
     value = ws * flops / (ms * 1e-3) / 1e12
     abs_err, rel_err = E.check_err(A, B, C, n, n, n)
+    # the library's own per-result accuracy report on one more product (outside the timed region)
+    arep = E.gemm(A, B, C, n, n, n, L.MODE_SPLIT, report=True, check_samples=4096)
+    accuracy_report = {"check_samples": arep.check_samples, "max_abs_err": arep.max_abs_err,
+                       "max_rel_err": arep.max_rel_err, "plain_bound_rel": arep.plain_bound_rel,
+                       "ref_kernel": L.REF_KERNELS[arep.ref_kernel],
+                       "note": "f4j_report accuracy fields: sampled Dot2 error of this result, k u bound of a plain "
+                               "FP64 product on the same scale, the CPU kernel Flag4j's dispatcher would run"}
 
     # dominant kernel time: the tcgen05 slice GEMM alone (same inputs), for the roofline
     s = rep.slices
@@ -640,7 +650,7 @@ def run_ours(args):
     fp8_flops = prods * 2.0 * n * n * kp
     out["split"] = {"slices": s, "frac_bits": rep.frac_bits, "exp_spread_bits": round(rep.exp_spread, 3),
                     "launches_per_step": launches / args.steps, "max_abs_err": abs_err, "max_rel_err": rel_err,
-                    "ms": ms_local, "fp8_products": prods}
+                    "ms": ms_local, "fp8_products": prods, "accuracy_report": accuracy_report}
 
     if not args.skip_extras:
         # ---- plain DMMA path on the same inputs

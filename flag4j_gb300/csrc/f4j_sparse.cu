@@ -29,10 +29,12 @@ namespace {
 // search on the row pointers.  Rows of different lengths therefore share the
 // warp's work evenly (a lane per row made every warp wait for its longest
 // row: about 1.75 add steps per nonzero at Poisson(16) lengths).  Each lane
-// walks its contiguous nonzeros 8 at a time: column indices and values with
-// 16-byte loads (VEC; the loads of a group stay inside the arrays, entries
-// outside the lane's range are loaded and ignored), the 8 gathers of x in
-// flight together, then the products and the running sum in storage order,
+// walks its contiguous nonzeros 8 at a time, from a multiple of 8: column
+// indices and values with 32-byte loads, one L2 sector each (VEC; a group's
+// loads stay inside the arrays, entries outside the lane's range are loaded
+// and ignored; two 16-byte loads per sector reached L2 about twice), the 8
+// gathers of x in flight together, then the products and the running sum in
+// storage order,
 // storing y at each row end.  Each product and each sum is rounded as
 // RealCsrDenseMatMult.standardVector rounds them (acc starts at +0.0), so y is
 // bit-identical.  GB300's FP64 pipe (2 lane-operations per clock per SM, two
@@ -50,6 +52,17 @@ template <bool FUSED>
 struct SpmvOcc {
     static constexpr int BLOCKS = FUSED ? 4 : 5;
 };
+
+// 32-byte read-only loads (one sector): 8 column indices, 4 values.  The
+// address must be 32-byte aligned.
+__device__ __forceinline__ void ld_nc_v8_b32(const int* p, int (&c)[8]) {
+    asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3]), "=r"(c[4]), "=r"(c[5]), "=r"(c[6]), "=r"(c[7])
+                 : "l"(p));
+}
+__device__ __forceinline__ void ld_nc_v4_f64(const double* p, double& a, double& b, double& c, double& d) {
+    asm volatile("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a), "=d"(b), "=d"(c), "=d"(d) : "l"(p));
+}
 
 template <bool FUSED, bool VEC>
 __global__ void __launch_bounds__(SPMV_BLOCK, SpmvOcc<FUSED>::BLOCKS)
@@ -86,19 +99,14 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SpmvOcc<FUSED>::BLOCKS)
         rend = rnext;
         rnext = r + 1 < b ? __ldg(rowptr + r + 2) : qe;
     }
-    for (int qb = VEC ? (qs & ~3) : qs; qb < qe; qb += 8) {
+    for (int qb = VEC ? (qs & ~7) : qs; qb < qe; qb += 8) {
         int c[8];
         double v[8];
         if (VEC && (int64_t)qb + 8 <= nnz) {
-            const int4 c0 = __ldg(reinterpret_cast<const int4*>(colidx + qb));
-            const int4 c1 = __ldg(reinterpret_cast<const int4*>(colidx + qb + 4));
-            c[0] = c0.x, c[1] = c0.y, c[2] = c0.z, c[3] = c0.w, c[4] = c1.x, c[5] = c1.y, c[6] = c1.z, c[7] = c1.w;
-#pragma unroll
-            for (int h = 0; h < 4; h++) {
-                const double2 vv = __ldg(reinterpret_cast<const double2*>(vals + qb) + h);
-                v[2 * h] = vv.x;
-                v[2 * h + 1] = vv.y;
-            }
+            // qb is a multiple of 8: one 32-byte sector of indices, two of values
+            ld_nc_v8_b32(colidx + qb, c);
+            ld_nc_v4_f64(vals + qb, v[0], v[1], v[2], v[3]);
+            ld_nc_v4_f64(vals + qb + 4, v[4], v[5], v[6], v[7]);
         } else {
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -1573,8 +1581,8 @@ extern "C" int f4j_spmv_ex(f4j_ctx* ctx, f4j_csr S, f4j_buf x, f4j_buf y, int mo
         const int rpw = (int)(rpw64 < 32 ? 32 : (rpw64 > SPMV_RPW_MAX ? SPMV_RPW_MAX : rpw64));
         const unsigned blocks = (unsigned)f4j_cdiv(f4j_cdiv(S->rows, rpw), SPMV_BLOCK / 32);
         const bool fused = mode == F4J_SPARSE_FMA;
-        // 16-byte loads of column indices and values when both arrays start 16-byte aligned
-        const bool vec = f4j_aligned16(S->colidx->ptr) && f4j_aligned16(S->vals->ptr);
+        // 32-byte loads of column indices and values when both arrays start 32-byte aligned
+        const bool vec = f4j_aligned(S->colidx->ptr, 32) && f4j_aligned(S->vals->ptr, 32);
         auto kern = fused ? (vec ? k_spmv<true, true> : k_spmv<true, false>)
                           : (vec ? k_spmv<false, true> : k_spmv<false, false>);
         f4j_prof_begin(ctx);
