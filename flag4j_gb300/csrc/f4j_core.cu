@@ -109,8 +109,8 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
             cudaStreamSynchronize(ctx->part_stream[i]);
             cudaStreamDestroy(ctx->part_stream[i]);
             cudaEventDestroy(ctx->part_ev[i]);
+            cudaEventDestroy(ctx->part_prep_ev[i]);
         }
-        cudaEventDestroy(ctx->ev_prep);
     }
     for (int i = 0; i < 8; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);

@@ -37,9 +37,10 @@ struct f4j_csr_s {
     void* rowidx;
 };
 
-// Row parts of a host-buffer GEMM (C's download overlaps the later parts'
-// products): F4J_HOST_PARTS by default, up to F4J_HOST_PARTS_MAX through the
-// F4J_HOST_PARTS environment variable.
+// Row parts of a host-buffer GEMM (a part's upload and slicing overlap the
+// earlier parts' products, its download the later ones'): F4J_HOST_PARTS by
+// default, up to F4J_HOST_PARTS_MAX through the F4J_HOST_PARTS environment
+// variable.
 #define F4J_HOST_PARTS 4
 #define F4J_HOST_PARTS_MAX 8
 
@@ -55,9 +56,11 @@ struct f4j_ctx {
     int ws_base;       // first split workspace slot (0, or 4 while an adjoint's second product is queued)
     cudaStream_t aux_stream;  // second stream of an adjoint (created on first use)
     cudaEvent_t ev_fork, ev_join;
-    // Streams of the row parts of a host-buffer GEMM (f4j_dgemm_host), created on first use.
+    // Streams of the row parts of a host-buffer GEMM (f4j_dgemm_host), created
+    // on first use, with an event per part for its slices being ready
+    // (part_prep_ev, on the context stream) and its download done (part_ev).
     cudaStream_t part_stream[F4J_HOST_PARTS_MAX];
-    cudaEvent_t part_ev[F4J_HOST_PARTS_MAX], ev_prep;
+    cudaEvent_t part_ev[F4J_HOST_PARTS_MAX], part_prep_ev[F4J_HOST_PARTS_MAX];
     // Split GEMM plans for every slice count, per workspace base (0 / 4), built
     // when the key (Kp, K length, band, chunk cap) changes.
     void* plan_tab[2];

@@ -490,6 +490,19 @@ __global__ void __launch_bounds__(256) k_finalize_pick(int64_t ta, int64_t tb, i
     }
 }
 
+// One thread, after every statistic of both operands is in: misc[5] = 1 when
+// the slice count those statistics give differs from the one `plan` was
+// picked with (from part of op(A)), or an operand holds a NaN / Inf, or the
+// plan stood down; 0 when the product sliced with `plan` is the one k_plan
+// would have planned.
+__global__ void k_spec_check(int* __restrict__ misc, int64_t k, int64_t klen_cat, int s_req,
+                             const SplitPlan* __restrict__ plan) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int s = s_req > 0 ? (s_req > S_MAX ? S_MAX : (s_req < 2 ? 2 : s_req))
+                            : slices_for(misc[1] / 256.0, misc[2] / 256.0, k, klen_cat);
+    misc[5] = (s != plan->s || misc[0] != 0 || plan->nonfinite) ? 1 : 0;
+}
+
 // ------------------------------------------------------------------ split
 
 // Exact float of an integer |d| < 2^22: d added to the bit pattern of 1.5 * 2^23.
@@ -1164,6 +1177,50 @@ static void launch_stats_cols(const double* X, int64_t rows, int64_t cols, int c
                                                                                       mx, es, cn, bad);
 }
 
+// Offsets in the small workspace of one split GEMM (M rows of op(A), n
+// columns of op(B), N = n or 2n slice rows of B_cat^T): per-target statistics
+// and exponents, the flag words, the plan.  Everything before `plan` starts at
+// zero for each product (one memset).
+struct SmallLayout {
+    size_t mxa, esa, cna, mxb, esb, cnb, ea, eb, misc, plan, total;
+};
+static SmallLayout small_layout(int64_t M, int64_t n, int64_t N) {
+    SmallLayout L;
+    L.mxa = 0;
+    L.esa = L.mxa + al1k(M * 8);
+    L.cna = L.esa + al1k(M * 8);
+    L.mxb = L.cna + al1k(M * 4);
+    L.esb = L.mxb + al1k(n * 8);
+    L.cnb = L.esb + al1k(n * 8);
+    L.ea = L.cnb + al1k(n * 4);
+    L.eb = L.ea + al1k(M * 4);
+    L.misc = L.eb + al1k(N * 4);
+    L.plan = L.misc + 1024;
+    L.total = L.plan + al1k(sizeof(SplitPlan));
+    return L;
+}
+
+// The context's table of plans for every slice count (k_plan_table), queued
+// for a rebuild on the context stream when its key (K, summed length, band,
+// K-chunk cap) changes; the one-thread build of a plan takes ~10 us.
+static int plan_table(f4j_ctx* ctx, int64_t Kp, int64_t klen_cat, int kcb_cap, SplitPlan** out) {
+    const int t = ctx->ws_base ? 1 : 0;
+    const long long key[4] = {(long long)Kp, (long long)klen_cat, (long long)env_band(), (long long)kcb_cap};
+    if (!ctx->plan_tab[t]) {
+        F4J_CUDA(cudaMalloc(&ctx->plan_tab[t], (size_t)(S_MAX + 1) * sizeof(SplitPlan)));
+        ctx->plan_valid[t] = false;
+    }
+    SplitPlan* tab = (SplitPlan*)ctx->plan_tab[t];
+    if (!ctx->plan_valid[t] || memcmp(key, ctx->plan_key[t], sizeof key) != 0) {
+        k_plan_table<<<S_MAX - 1, 32, 0, ctx->stream>>>(Kp, klen_cat, (int)key[2], kcb_cap, tab);
+        F4J_LAUNCHED(ctx);
+        memcpy(ctx->plan_key[t], key, sizeof key);
+        ctx->plan_valid[t] = true;
+    }
+    *out = tab;
+    return F4J_OK;
+}
+
 static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                          const double* B, int opB, double* C, int slices_req, SplitLaunch* L) {
     const int64_t M = m, N = cplx ? 2 * n : n;
@@ -1173,16 +1230,11 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "split GEMM too large");
 
     // ---- small workspace (slot 1): statistics, exponents, plan
-    const size_t off_mxa = 0, off_esa = off_mxa + al1k(M * 8), off_cna = off_esa + al1k(M * 8);
-    const size_t off_mxb = off_cna + al1k(M * 4), off_esb = off_mxb + al1k(n * 8), off_cnb = off_esb + al1k(n * 8);
-    const size_t off_ea = off_cnb + al1k(n * 4), off_eb = off_ea + al1k(M * 4);
-    const size_t off_misc = off_eb + al1k(N * 4);
-    const size_t off_plan = off_misc + 1024;
-    const size_t small_bytes = off_plan + al1k(sizeof(SplitPlan));
+    const SmallLayout Lo = small_layout(M, n, N);
     // ---- bulk workspace (slot 0): S_MAX slice planes per operand
     const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
     void *ws1, *ws0;
-    int rc = f4j_workspace(ctx, ctx->ws_base + 1, small_bytes, &ws1);
+    int rc = f4j_workspace(ctx, ctx->ws_base + 1, Lo.total, &ws1);
     if (rc) return rc;
     int kchunks = 0;
     const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks);
@@ -1190,22 +1242,22 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     rc = f4j_workspace(ctx, ctx->ws_base, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX) + wpart_bytes, &ws0);
     if (rc) return rc;
     char* w = (char*)ws1;
-    unsigned long long* mxa = (unsigned long long*)(w + off_mxa);
-    long long* esa = (long long*)(w + off_esa);
-    int* cna = (int*)(w + off_cna);
-    unsigned long long* mxb = (unsigned long long*)(w + off_mxb);
-    long long* esb = (long long*)(w + off_esb);
-    int* cnb = (int*)(w + off_cnb);
-    int* ea = (int*)(w + off_ea);
-    int* eb = (int*)(w + off_eb);
-    int* misc = (int*)(w + off_misc);  // [0] non-finite seen, [1] spread A x256, [2] spread B x256
-    SplitPlan* plan = (SplitPlan*)(w + off_plan);
+    unsigned long long* mxa = (unsigned long long*)(w + Lo.mxa);
+    long long* esa = (long long*)(w + Lo.esa);
+    int* cna = (int*)(w + Lo.cna);
+    unsigned long long* mxb = (unsigned long long*)(w + Lo.mxb);
+    long long* esb = (long long*)(w + Lo.esb);
+    int* cnb = (int*)(w + Lo.cnb);
+    int* ea = (int*)(w + Lo.ea);
+    int* eb = (int*)(w + Lo.eb);
+    int* misc = (int*)(w + Lo.misc);  // [0] non-finite seen, [1] spread A x256, [2] spread B x256
+    SplitPlan* plan = (SplitPlan*)(w + Lo.plan);
     uint8_t* slA = (uint8_t*)ws0;
     uint8_t* slB = slA + al1k(plane_a * S_MAX);
 
     // statistics accumulate with atomics and misc holds flags and the block
     // counter of k_finalize_pick: one clear of everything up to the plan
-    F4J_CUDA(cudaMemsetAsync(w, 0, off_plan, ctx->stream));
+    F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, ctx->stream));
 
     const bool a_rows = (opA == F4J_OP_N);  // targets of A (rows of op(A)) are stored rows
     const bool b_rows = (opB != F4J_OP_N);  // targets of B (columns of op(B)) are stored rows
@@ -1227,19 +1279,9 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     {   // exponents, spreads and the plan in one launch: the plan comes from the
         // context's table of plans for every slice count, rebuilt when the key
         // changes (the one-thread build takes ~10 us)
-        const int t = ctx->ws_base ? 1 : 0;
-        const long long key[4] = {(long long)Kp, (long long)klen_cat, (long long)env_band(), (long long)kcb_cap};
-        if (!ctx->plan_tab[t]) {
-            F4J_CUDA(cudaMalloc(&ctx->plan_tab[t], (size_t)(S_MAX + 1) * sizeof(SplitPlan)));
-            ctx->plan_valid[t] = false;
-        }
-        SplitPlan* tab = (SplitPlan*)ctx->plan_tab[t];
-        if (!ctx->plan_valid[t] || memcmp(key, ctx->plan_key[t], sizeof key) != 0) {
-            k_plan_table<<<S_MAX - 1, 32, 0, ctx->stream>>>(Kp, klen_cat, (int)key[2], kcb_cap, tab);
-            F4J_LAUNCHED(ctx);
-            memcpy(ctx->plan_key[t], key, sizeof key);
-            ctx->plan_valid[t] = true;
-        }
+        SplitPlan* tab = nullptr;
+        rc = plan_table(ctx, Kp, klen_cat, kcb_cap, &tab);
+        if (rc) return rc;
         const unsigned blocks = (unsigned)(f4j_cdiv(M, 256) + f4j_cdiv(n, 256));
         k_finalize_pick<<<blocks, 256, 0, ctx->stream>>>(M, n, cplx ? 1 : 0, mxa, esa, cna, mxb, esb, cnb, ea, eb,
                                                          misc, k, klen_cat,
@@ -1351,17 +1393,174 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 }
 
 // ------------------------------------------------------------------ host buffers
-// C = op(A) op(B) from and to host memory (pinned for full copy speed).  For
-// a split product with op(A) = N and at least two tile rows, the slice GEMM
-// runs as F4J_HOST_PARTS launches over shrinking row parts of C on their own
-// streams, each followed by its part's download, so C's download overlaps the
-// other parts' products and each launch's CTAs fill another's last wave.  The
-// parts need not finish in order (the block scheduler interleaves the
-// streams); the small parts keep the exposed final download short.  The gated DMMA fallback (the product when an input is
-// not finite, an empty kernel otherwise) runs once before the parts: queued
-// after a part, its CTAs would wait behind the later parts' persistent CTAs,
-// and that part's download with them.  Other products upload, multiply and
-// download in turn.  Returns when C is in host memory.
+// The split product C = A op(B) from host memory with its upload pipelined
+// (f4j_dgemm_host, op(A) = N): B goes up first and is summarised; then A goes
+// up in row parts, and each part's statistics and slicing run as soon as its
+// rows are on the device, its slice GEMM on the part's own stream with its
+// rows of C going down behind it.  The slice count cannot wait for all of A,
+// so it is picked from B and A's first part (k_plan_pick on the spreads so
+// far).  Once every part's statistics are in, k_spec_check compares it with
+// the count all of A gives: *recompute is set when they differ, or when an
+// operand holds a NaN / Inf, and the caller then runs the ordinary path.  When
+// the counts agree, every slice, plan and sum is the ordinary path's, and so
+// is every bit of C.  The first part is small, so the products start soon
+// after B is up; the last part is small too, so little of C's download
+// follows the last product.  Waits for everything it queued before returning;
+// *spread_out receives the spread all of A and B give.
+static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, const double* B,
+                                int opB, double* C, double* dA, double* dB, double* dC, int parts, bool* recompute,
+                                const SplitPlan** plan_out, float* spread_out) {
+    *recompute = false;
+    const int64_t M = m, N = n;
+    const int64_t Kp = f4j_cdiv(k, BKB) * BKB;  // K padded to whole K blocks
+    const SmallLayout Lo = small_layout(M, n, N);
+    void *ws1, *ws0;
+    int rc = f4j_workspace(ctx, ctx->ws_base + 1, Lo.total, &ws1);
+    if (rc) return rc;
+    const size_t plane_a = (size_t)M * Kp, plane_b = (size_t)N * Kp;
+    rc = f4j_workspace(ctx, ctx->ws_base, al1k(plane_a * S_MAX) + al1k(plane_b * S_MAX), &ws0);
+    if (rc) return rc;
+    char* w = (char*)ws1;
+    unsigned long long* mxa = (unsigned long long*)(w + Lo.mxa);
+    long long* esa = (long long*)(w + Lo.esa);
+    int* cna = (int*)(w + Lo.cna);
+    unsigned long long* mxb = (unsigned long long*)(w + Lo.mxb);
+    long long* esb = (long long*)(w + Lo.esb);
+    int* cnb = (int*)(w + Lo.cnb);
+    int* ea = (int*)(w + Lo.ea);
+    int* eb = (int*)(w + Lo.eb);
+    int* misc = (int*)(w + Lo.misc);  // [0] non-finite, [1] spread of A so far, [2] of B, [5] the check
+    SplitPlan* plan = (SplitPlan*)(w + Lo.plan);
+    uint8_t* slA = (uint8_t*)ws0;
+    uint8_t* slB = slA + al1k(plane_a * S_MAX);
+    const bool b_rows = opB != F4J_OP_N;
+    const int s_req = env_slices();
+    // the same K-chunk cap the ordinary path plans with (no split K here)
+    int kchunks = 0;
+    const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks);
+    if (kchunks) return f4j_fail(F4J_ERR_ARG, "split-K product in row parts");
+    const cudaStream_t st = ctx->stream;
+
+    F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
+    // B first: every part's product needs all of it
+    F4J_CUDA(cudaMemcpyAsync(dB, B, (size_t)k * n * 8, cudaMemcpyHostToDevice, st));
+    if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, st>>>(dB, n, k, 0, mxb, esb, cnb, misc);
+    else launch_stats_cols(dB, k, n, 0, ctx->sm_count, mxb, esb, cnb, misc, st);
+    F4J_LAUNCHED(ctx);
+    k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, st>>>(n, 0, mxb, esb, cnb, eb, misc + 2);
+    F4J_LAUNCHED(ctx);
+    SplitPlan* tab = nullptr;
+    rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
+    if (rc) return rc;
+
+    SplitLaunch L;
+    rc = make_slice_map(&L.ta, slA, Kp, M, S_MAX);
+    if (rc) return rc;
+    rc = make_slice_map(&L.tb, slB, Kp, N, S_MAX);
+    if (rc) return rc;
+    SplitGemmParams& prm = L.prm;
+    prm = SplitGemmParams{};
+    prm.M = (int)M;
+    prm.N = (int)N;
+    prm.Kp = (int)Kp;
+    prm.cplx = 0;
+    prm.n_out = (int)n;
+    prm.ea = ea;
+    prm.eb = eb;
+    prm.C = dC;
+    prm.status = ctx->d_status + F4J_ST_TIMEOUT;
+    prm.plan = plan;
+    prm.wpart = nullptr;
+    L.tiles_m = (int)f4j_cdiv(M, BM);
+    L.tiles_n = (int)f4j_cdiv(N, BN);
+    L.kchunks = 0;
+    prm.tm0 = 0;
+    prm.tm1 = L.tiles_m;
+
+    // part boundaries in tile rows: a small first part (1/16), a small last
+    // part (1/8), the rest in equal middle parts; every part at least one tile row
+    const int tiles_m = L.tiles_m;
+    int bound[F4J_HOST_PARTS_MAX + 1];
+    bound[0] = 0;
+    bound[parts] = tiles_m;
+    {
+        const int first = tiles_m / 16 > 1 ? tiles_m / 16 : 1;
+        const int last = parts > 2 ? (tiles_m / 8 > 1 ? tiles_m / 8 : 1) : tiles_m - first;
+        bound[1] = first;
+        bound[parts - 1] = tiles_m - last;
+        for (int p = 2; p < parts - 1; p++)
+            bound[p] = first + (int)((int64_t)(bound[parts - 1] - first) * (p - 1) / (parts - 2));
+        for (int p = 1; p < parts; p++) {  // keep every part non-empty
+            const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);
+            bound[p] = bound[p] < lo ? lo : (bound[p] > hi ? hi : bound[p]);
+        }
+    }
+    int launched = 0;
+    for (int p = 0; p < parts && !rc; p++) {
+        const int64_t r0 = (int64_t)bound[p] * BM;
+        const int64_t r1 = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
+        const int64_t rows = r1 - r0;
+        F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)rows * k * 8, cudaMemcpyHostToDevice, st));
+        k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k, rows, k, 0, mxa + r0, esa + r0,
+                                                                  cna + r0, misc);
+        F4J_LAUNCHED(ctx);
+        k_stats_finalize<<<(unsigned)f4j_cdiv(rows, 256), 256, 0, st>>>(rows, 0, mxa + r0, esa + r0, cna + r0,
+                                                                         ea + r0, misc + 1);
+        F4J_LAUNCHED(ctx);
+        if (p == 0) {  // the plan from B and the first rows, then B's slices
+            k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
+            F4J_LAUNCHED(ctx);
+            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(n, SP_TR)), 256, 0, st>>>(
+                dB, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, n, k, Kp, Kp, N, eb, plan, slB);
+            F4J_LAUNCHED(ctx);
+        }
+        // this part's rows of the slice planes: target t of the part is row r0 + t
+        k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
+            dA + r0 * k, rows, k, 0, 0, 0, 0, rows, k, Kp, Kp, M, ea + r0, plan, slA + r0 * Kp);
+        F4J_LAUNCHED(ctx);
+        F4J_CUDA(cudaEventRecord(ctx->part_prep_ev[p], st));
+        const cudaStream_t ps = ctx->part_stream[p];
+        F4J_CUDA(cudaStreamWaitEvent(ps, ctx->part_prep_ev[p], 0));
+        launched = p + 1;
+        rc = split_launch(ctx, L, ps, bound[p], bound[p + 1]);
+        if (!rc) {
+            cudaError_t e = cudaMemcpyAsync(C + r0 * n, dC + r0 * n, (size_t)rows * n * 8, cudaMemcpyDeviceToHost, ps);
+            if (e == cudaSuccess) e = cudaEventRecord(ctx->part_ev[p], ps);
+            if (e != cudaSuccess) rc = f4j_cuda_fail(e, "download of a row part");
+        }
+    }
+    int hm[6] = {0, 0, 0, 0, 0, 0};
+    if (!rc) {
+        k_spec_check<<<1, 32, 0, st>>>(misc, k, k, s_req, plan);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            ctx->launches++;
+            e = cudaMemcpyAsync(hm, misc, sizeof hm, cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = f4j_cuda_fail(e, "slice count check of a host-buffer product");
+    }
+    for (int p = 0; p < launched; p++) {
+        cudaError_t e = cudaStreamSynchronize(ctx->part_stream[p]);
+        if (e != cudaSuccess && !rc) rc = f4j_cuda_fail(e, "row part of a host-buffer product");
+    }
+    if (rc) return rc;
+    *recompute = hm[5] != 0;
+    *plan_out = plan;
+    *spread_out = (float)((hm[1] > hm[2] ? hm[1] : hm[2]) / 256.0);
+    return F4J_OK;
+}
+
+// C = op(A) op(B) from and to host memory (pinned for full copy speed).  A
+// split product with op(A) = N and at least two tile rows runs pipelined
+// (host_split_pipelined): B up first, then A in F4J_HOST_PARTS row parts, each
+// part sliced and multiplied on its own stream as soon as its rows arrive and
+// its rows of C downloaded behind its product.  In the rare case that all of
+// A asks for another slice count than its first part did (or an operand holds
+// a NaN / Inf), the product runs again through the ordinary path on the
+// operands already on the device.  Either way C equals f4j_dgemm's bit for
+// bit.  Other products upload, multiply and download in turn.  Returns when C
+// is in host memory.
 extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                               const double* B, int opB, double* C, int mode, f4j_report* rep) {
     F4J_LOCK(ctx);
@@ -1388,9 +1587,6 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     if (!rc) rc = f4j_workspace(ctx, 6, bb, &dB);
     if (!rc) rc = f4j_workspace(ctx, 7, cb, &dC);
     if (rc) return rc;
-    if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
-    if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
-    const double work = 2.0 * (double)m * (double)n * (double)k;
     const bool split = k > 0 && f4j_resolve_mode(false, m, n, k, mode) == F4J_MODE_SPLIT;
     const int tiles_m = (int)f4j_cdiv(m, BM);
     const int want = env_host_parts();
@@ -1398,6 +1594,8 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     int kchunks = 0;
     split_kcb_cap(tiles_m * f4j_cdiv(n, BN), f4j_cdiv(k, BKB), &kchunks);
     if (!split || opA != F4J_OP_N || parts < 2 || kchunks) {  // split K runs as one launch
+        if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
+        if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
         rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,
                            rep);
         if (rc) return rc;
@@ -1406,63 +1604,40 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
         return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB,
                                    (const double*)dC, check_samples, check_flags, rep);
     }
-    const int64_t l0 = ctx->launches;
-    SplitLaunch L;
-    rc = split_prepare(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, 0, &L);
-    if (rc) return rc;
     if (!ctx->parts_init) {
         for (int i = 0; i < F4J_HOST_PARTS_MAX; i++) {
             F4J_CUDA(cudaStreamCreateWithFlags(&ctx->part_stream[i], cudaStreamNonBlocking));
             F4J_CUDA(cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming));
+            F4J_CUDA(cudaEventCreateWithFlags(&ctx->part_prep_ev[i], cudaEventDisableTiming));
         }
-        F4J_CUDA(cudaEventCreateWithFlags(&ctx->ev_prep, cudaEventDisableTiming));
         ctx->parts_init = true;
     }
-    // the plain product when an input is not finite (the slice launches then return at once)
-    rc = f4j_gemm_dmma(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB, (double*)dC,
-                       &L.prm.plan->nonfinite);
+    const int64_t l0 = ctx->launches;
+    bool recompute = false;
+    const SplitPlan* plan = nullptr;
+    float spread = 0.0f;
+    rc = host_split_pipelined(ctx, m, n, k, A, B, opB, C, (double*)dA, (double*)dB, (double*)dC, parts, &recompute,
+                              &plan, &spread);
     if (rc) return rc;
-    F4J_CUDA(cudaEventRecord(ctx->ev_prep, ctx->stream));
-    int launched = 0;
-    // part p gets a share 2(parts - p) - 1 of the tile rows (7:5:3:1 for four):
-    // the last part's download is the one no product hides
-    int bound[F4J_HOST_PARTS_MAX + 1];
-    bound[0] = 0;
-    for (int p = 1, wsum = 0; p <= parts; p++) {
-        wsum += 2 * (parts - p) + 1;
-        const int b = (int)((int64_t)tiles_m * wsum / (parts * parts));  // the weights sum to parts^2
-        const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);      // every part at least one tile row
-        bound[p] = b < lo ? lo : (b > hi ? hi : b);
-    }
-    for (int p = 0; p < parts && !rc; p++) {
-        const int tm0 = bound[p], tm1 = bound[p + 1];
-        const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
-        const cudaStream_t st = ctx->part_stream[p];
-        F4J_CUDA(cudaStreamWaitEvent(st, ctx->ev_prep, 0));
-        launched = p + 1;
-        rc = split_launch(ctx, L, st, tm0, tm1);
-        if (!rc) {
-            F4J_CUDA(cudaMemcpyAsync(C + r0 * n, (const double*)dC + r0 * n, (size_t)(r1 - r0) * n * 8,
-                                     cudaMemcpyDeviceToHost, st));
-            F4J_CUDA(cudaEventRecord(ctx->part_ev[p], st));
-            F4J_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->part_ev[p], 0));
-        }
-    }
-    if (rc) {
-        for (int p = 0; p < launched; p++) cudaStreamSynchronize(ctx->part_stream[p]);
-        return rc;
-    }
-    if (rep) {
-        rep->flops = work;
+    if (recompute) {
+        // all of A asks for another slice count than its first rows did, or an
+        // operand holds a NaN / Inf: the product again through the ordinary
+        // path on the operands now on the device, and all of C down
+        rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB, (double*)dC,
+                           mode, rep);
+        if (rc) return rc;
+        F4J_CUDA(cudaMemcpyAsync(C, dC, cb, cudaMemcpyDeviceToHost, ctx->stream));
+        F4J_CUDA(cudaStreamSynchronize(ctx->stream));
+    } else if (rep) {
+        rep->flops = 2.0 * (double)m * (double)n * (double)k;
         rep->mode_used = F4J_MODE_SPLIT;
-        rc = split_report(ctx, L.prm.plan, rep);
-        if (rep->slices == 0) rep->mode_used = F4J_MODE_PLAIN;
-        rep->launches = (int32_t)(ctx->launches - l0);
+        rc = split_report(ctx, plan, rep);
+        if (rc) return rc;
+        rep->exp_spread = spread;
     }
-    F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (rc) return rc;
-    return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (const double*)dC,
-                               check_samples, check_flags, rep);
+    if (rep) rep->launches = (int32_t)(ctx->launches - l0);
+    return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB,
+                               (const double*)dC, check_samples, check_flags, rep);
 }
 
 // ------------------------------------------------------------------ no-allocation variant

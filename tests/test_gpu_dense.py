@@ -430,25 +430,32 @@ def test_wrap_rejects_misaligned_and_null(f4j):
 
 
 @pytest.mark.parametrize("m,n,k,mode,opA,host", [
-    (1000, 700, 900, "split", 0, "registered"),  # 8 tile rows: four shrinking row parts (3, 3, 1, 1)
-    (2500, 900, 700, "split", 0, "allocated"),   # 20 tile rows in f4j_host_alloc memory (8, 7, 3, 2)
-    (300, 260, 520, "split", 0, "pageable"),     # 3 tile rows: three parts, pageable host memory
-    (130, 200, 300, "split", 0, "registered"),   # 2 tile rows, the last ragged
-    (100, 90, 80, "split", 0, "allocated"),      # one tile row: no parts
-    (600, 500, 400, "split", 1, "registered"),   # op(A) = T: uploaded, multiplied, downloaded in turn
+    # pipelined (B up first, A in row parts of 128-row tile rows: first 1/16, last 1/8)
+    (2500, 900, 700, "split", 0, "allocated"),   # 20 x 8 tiles in f4j_host_alloc memory: parts 1, 8, 9, 2
+    (2000, 1300, 600, "split", 0, "registered"),  # 16 x 11 tiles: parts 1, 6, 7, 2
+    (1500, 2000, 300, "split", 0, "pageable"),   # 12 x 16 tiles, pageable host memory: parts 1, 5, 5, 1
+    (300, 260, 5000, "split", 0, "registered"),  # 9 tiles but 79 K blocks (no split K): parts 1, 1, 1
+    (130, 200, 4500, "split", 0, "allocated"),   # 2 tile rows, the last ragged: parts 1, 1
+    # uploaded, multiplied and downloaded in turn
+    (1000, 700, 900, "split", 0, "registered"),  # 48 tiles, 15 K blocks: split K
+    (300, 260, 520, "split", 0, "pageable"),     # 9 tiles: split K
+    (100, 90, 80, "split", 0, "allocated"),      # one tile row
+    (600, 500, 400, "split", 1, "registered"),   # op(A) = T
     (500, 300, 200, "plain", 0, "registered"),
     (64, 48, 40, "exact", 0, "allocated"),
 ])
 def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, host):
     """f4j_dgemm_host is bitwise f4j_dgemm on the same operands, from registered, pageable or
-    f4j_host_alloc host memory."""
+    f4j_host_alloc host memory, with the same slice count and spread in the report."""
     from flag4j_gb300 import _lib, synth
     from flag4j_gb300.device import check, pinned_empty
     ctx = f4j.default_context()
     A = synth.scaled(m, k, 4, 21, "row") if opA == 0 else synth.scaled(k, m, 4, 21, "col")
     B = synth.scaled(k, n, 4, 22, "col")
     dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(8 * m * n)
-    check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, 0, dC.handle, _lib.MODES[mode], None))
+    rd = _lib.f4j_report()
+    check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, 0, dC.handle, _lib.MODES[mode],
+                            ctypes.byref(rd)))
     ref = dC.to_numpy(np.float64, m * n).reshape(m, n)
     C = np.full((m, n), np.nan)
     if host == "allocated":
@@ -467,6 +474,7 @@ def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, host):
         assert np.array_equal(C, ref)
         if mode == "split":
             assert rep.slices > 0 and rep.mode_used == _lib.MODE_SPLIT
+            assert rep.slices == rd.slices and rep.exp_spread == rd.exp_spread
     finally:
         if pinned:
             for a in arrays:
@@ -494,6 +502,51 @@ def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
     ref = oracle.dgemm(A[fin], B)
     bound = 2 * k * U * oracle.absgemm(A[fin], B)
     assert np.all(np.abs(C[fin] - ref) <= bound)
+
+
+@pytest.mark.parametrize("case", ["wider_spread_late", "nan_late", "inf_first"])
+def test_host_buffer_gemm_speculative_slice_count(f4j, case):
+    """The pipelined host-buffer product picks its slice count from B and A's
+    first row part (128 rows here).  When all of A asks for another count, or
+    an operand holds a NaN / Inf, the product runs again through the device
+    path: C, the mode used and the slice count still equal f4j_dgemm's, NaN
+    and Inf bits included."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    m, n, k = 2048, 1536, 1024   # 16 x 12 tiles, 16 K blocks: pipelined, parts of 1, 6, 7, 2 tile rows
+    A = synth.uniform(m, k, 51)
+    B = synth.uniform(k, n, 52)
+    if case == "wider_spread_late":
+        # rows past the first part: elements scaled by 2^-j, j uniform in [0, 24]
+        A[128:] *= np.ldexp(1.0, -synth.rng(53).integers(0, 25, size=(m - 128, k)))
+    elif case == "nan_late":
+        A[1500, 17] = np.nan
+    else:
+        A[3, 900] = np.inf
+
+    def device(Ad):
+        mm = Ad.shape[0]
+        dA, dB, dC = ctx.from_numpy(Ad), ctx.from_numpy(B), ctx.alloc(8 * mm * n)
+        rd = _lib.f4j_report()
+        check(ctx.lib.f4j_dgemm(ctx.handle, mm, n, k, dA.handle, 0, dB.handle, 0, dC.handle, _lib.MODE_SPLIT,
+                                ctypes.byref(rd)))
+        return dC.to_numpy(np.float64, mm * n).reshape(mm, n), rd
+
+    ref, rd = device(A)
+    C = np.zeros((m, n))
+    rep = _lib.f4j_report()
+    check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, 0, B.ctypes.data, 0, C.ctypes.data,
+                                 _lib.MODE_SPLIT, ctypes.byref(rep)))
+    assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
+    assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
+    if case == "wider_spread_late":
+        _, r_first = device(np.ascontiguousarray(A[:128]))
+        assert rd.mode_used == _lib.MODE_SPLIT and rd.slices > r_first.slices   # the first pick was too few
+        assert rep.exp_spread == rd.exp_spread
+    else:
+        assert rd.mode_used == _lib.MODE_PLAIN and rd.slices == 0
+        assert not np.isfinite(C[1500 if case == "nan_late" else 3]).any()
 
 
 def test_one_context_shared_by_threads(f4j, oracle):
