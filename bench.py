@@ -811,10 +811,11 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": ws * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes,
-                    "path": "f4j_dgemm_host (split) on page-locked host A, B, C (f4j_host_alloc): B up, then A "
-                            "in 4 row parts, each part sliced and multiplied as its rows arrive and its rows of C "
-                            "downloaded behind its product (the slice count from B and A's first part, checked "
-                            "against all of A)"},
+                    "path": "f4j_dgemm_host (split) on page-locked host A, B, C (f4j_host_alloc): uploads back "
+                            "to back (A's first 1024 rows, B in 4 column parts, the rest of A in 3 row parts), "
+                            "each part sliced as it arrives, B's column parts multiplied by A's first rows and "
+                            "A's later parts by all of B, each block of C downloaded behind its product (the "
+                            "slice count from the first parts, checked against all of A and B)"},
             "gpu_launches": launches, "clocks": clocks}
     line.update(out)
     print(json.dumps(line))

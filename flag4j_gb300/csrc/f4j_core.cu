@@ -105,12 +105,16 @@ extern "C" int f4j_destroy(f4j_ctx* ctx) {
         cudaEventDestroy(ctx->ev_join);
     }
     if (ctx->parts_init) {
-        for (int i = 0; i < F4J_HOST_PARTS_MAX; i++) {
+        for (int i = 0; i < F4J_HOST_STREAMS; i++) {
             cudaStreamSynchronize(ctx->part_stream[i]);
             cudaStreamDestroy(ctx->part_stream[i]);
             cudaEventDestroy(ctx->part_ev[i]);
             cudaEventDestroy(ctx->part_prep_ev[i]);
+            cudaEventDestroy(ctx->up_ev[i]);
         }
+        cudaStreamSynchronize(ctx->up_stream);
+        cudaStreamDestroy(ctx->up_stream);
+        cudaEventDestroy(ctx->up_start);
     }
     for (int i = 0; i < 8; i++)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);

@@ -37,12 +37,15 @@ struct f4j_csr_s {
     void* rowidx;
 };
 
-// Row parts of a host-buffer GEMM (a part's upload and slicing overlap the
-// earlier parts' products, its download the later ones'): F4J_HOST_PARTS by
-// default, up to F4J_HOST_PARTS_MAX through the F4J_HOST_PARTS environment
-// variable.
+// Parts of a host-buffer split GEMM (a part's upload and slicing overlap the
+// earlier parts' products, its download the later ones'): A in F4J_HOST_PARTS
+// row parts and B in F4J_HOST_BPARTS column parts by default, each up to
+// F4J_HOST_PARTS_MAX through the environment variables of the same names.
+// Every part's product is one launch on a stream of its own.
 #define F4J_HOST_PARTS 4
+#define F4J_HOST_BPARTS 4
 #define F4J_HOST_PARTS_MAX 8
+#define F4J_HOST_STREAMS (2 * F4J_HOST_PARTS_MAX)
 
 struct f4j_ctx {
     std::recursive_mutex mu;  // held by every C-ABI call on this context (F4J_LOCK)
@@ -59,8 +62,12 @@ struct f4j_ctx {
     // Streams of the row parts of a host-buffer GEMM (f4j_dgemm_host), created
     // on first use, with an event per part for its slices being ready
     // (part_prep_ev, on the context stream) and its download done (part_ev).
-    cudaStream_t part_stream[F4J_HOST_PARTS_MAX];
-    cudaEvent_t part_ev[F4J_HOST_PARTS_MAX], part_prep_ev[F4J_HOST_PARTS_MAX];
+    cudaStream_t part_stream[F4J_HOST_STREAMS];
+    cudaEvent_t part_ev[F4J_HOST_STREAMS], part_prep_ev[F4J_HOST_STREAMS];
+    // The uploads of a pipelined host-buffer GEMM, back to back on their own
+    // stream, with an event per uploaded part and one the stream starts behind.
+    cudaStream_t up_stream;
+    cudaEvent_t up_ev[F4J_HOST_STREAMS], up_start;
     // Split GEMM plans for every slice count, per workspace base (0 / 4), built
     // when the key (Kp, K length, band, chunk cap) changes.
     void* plan_tab[2];

@@ -129,6 +129,7 @@ struct SplitGemmParams {
     int* status;
     const SplitPlan* plan;
     int tm0, tm1;           // the launch covers tile rows [tm0, tm1) of C
+    int tn0, tn1;           // and tile columns [tn0, tn1)
     long long* wpart;       // split K: per-chunk int64 sums [nchunks][M][N] (null: whole tiles)
 };
 
@@ -179,9 +180,10 @@ __global__ void k_stats_rows(const double* __restrict__ X, int64_t rows, int64_t
     stats_rows_body(X, rows, cols, cplx, blockIdx.x, mx_out, esum_out, cnt_out, bad_out);
 }
 
-// Thread per stored column, block (bx, by) over chunks of `chunk` rows: stats of stored columns.
-__device__ __forceinline__ void stats_cols_body(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx,
-                                                int chunk, int64_t bx, int64_t by,
+// Thread per stored column, block (bx, by) over chunks of `chunk` rows: stats
+// of stored columns (cols of them, rows ld elements apart).
+__device__ __forceinline__ void stats_cols_body(const double* __restrict__ X, int64_t rows, int64_t cols, int64_t ld,
+                                                int cplx, int chunk, int64_t bx, int64_t by,
                                                 unsigned long long* __restrict__ mx_out,
                                                 long long* __restrict__ esum_out, int* __restrict__ cnt_out,
                                                 int* __restrict__ bad_out) {
@@ -193,10 +195,10 @@ __device__ __forceinline__ void stats_cols_body(const double* __restrict__ X, in
     int cnt = 0, bad = 0;
     for (int64_t r = r0; r < r1; r++) {
         if (cplx) {
-            stat_elem(X[2 * (r * cols + c)], mx, es, cnt, bad);
-            stat_elem(X[2 * (r * cols + c) + 1], mx, es, cnt, bad);
+            stat_elem(X[2 * (r * ld + c)], mx, es, cnt, bad);
+            stat_elem(X[2 * (r * ld + c) + 1], mx, es, cnt, bad);
         } else {
-            stat_elem(X[r * cols + c], mx, es, cnt, bad);
+            stat_elem(X[r * ld + c], mx, es, cnt, bad);
         }
     }
     if (mx) atomicMax(&mx_out[c], mx);
@@ -207,10 +209,10 @@ __device__ __forceinline__ void stats_cols_body(const double* __restrict__ X, in
     if (bad) atomicExch(bad_out, 1);
 }
 
-__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int cplx, int chunk,
-                             unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
+__global__ void k_stats_cols(const double* __restrict__ X, int64_t rows, int64_t cols, int64_t ld, int cplx,
+                             int chunk, unsigned long long* __restrict__ mx_out, long long* __restrict__ esum_out,
                              int* __restrict__ cnt_out, int* __restrict__ bad_out) {
-    stats_cols_body(X, rows, cols, cplx, chunk, blockIdx.x, blockIdx.y, mx_out, esum_out, cnt_out, bad_out);
+    stats_cols_body(X, rows, cols, ld, cplx, chunk, blockIdx.x, blockIdx.y, mx_out, esum_out, cnt_out, bad_out);
 }
 
 // Exponent bound e (max|x| < 2^e) of target t, and its spread (x256).
@@ -738,7 +740,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int nrounds = plan->nrounds;
     // persistent: CTA b takes tiles b, b + grid, ...; see tile_origin for the order
-    const int tiles_n = (p.N + BN - 1) / BN, tiles_m = p.tm1 - p.tm0;
+    const int tiles_n = p.tn1 - p.tn0, tiles_m = p.tm1 - p.tm0;
     const int ntiles = tiles_n * tiles_m;
 
     const int ngroups = plan->ngroups;
@@ -823,6 +825,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 int m0, n0;
                 tile_origin(tile, tiles_m, tiles_n, m0, n0);
                 m0 += p.tm0 * BM;
+                n0 += p.tn0 * BN;
                 for (int kc = kc0; kc < kc1 && kc < nkb && ok; kc += kcb) {
                     const int kend = kc + kcb < nkb ? kc + kcb : nkb;
                     for (int g = 0; g < ngroups && ok; g++) {
@@ -956,6 +959,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         int m0, n0;
         tile_origin(tile, tiles_m, tiles_n, m0, n0);
         m0 += p.tm0 * BM;
+        n0 += p.tn0 * BN;
         const int row = m0 + 32 * q + lane;
         long long acc[EPI_COLS];
 #pragma unroll
@@ -1104,10 +1108,11 @@ static int env_slices() {
     return (env && atoi(env) > 0) ? atoi(env) : 0;
 }
 
-// Row parts of a host-buffer split product (F4J_HOST_PARTS, 1..F4J_HOST_PARTS_MAX).
-static int env_host_parts() {
-    const char* e = getenv("F4J_HOST_PARTS");
-    const int v = e ? atoi(e) : F4J_HOST_PARTS;
+// Row parts of A (F4J_HOST_PARTS) and column parts of B (F4J_HOST_BPARTS) of a
+// host-buffer split product, 1..F4J_HOST_PARTS_MAX each.
+static int env_host_parts(const char* name, int dflt) {
+    const char* e = getenv(name);
+    const int v = e ? atoi(e) : dflt;
     return v < 1 ? 1 : (v > F4J_HOST_PARTS_MAX ? F4J_HOST_PARTS_MAX : v);
 }
 
@@ -1164,17 +1169,18 @@ static int split_kcb_cap(int64_t tiles, int64_t nkb, int* nchunks) {
     return (int)best;
 }
 
-// Column statistics of a stored rows x cols operand.  Row chunks of 256, halved
-// (down to 16) while the grid has fewer than four blocks per SM: a 1024-wide
-// operand otherwise runs as 16 blocks.  The chunk count stays within grid.y.
-static void launch_stats_cols(const double* X, int64_t rows, int64_t cols, int cplx, int sm_count,
+// Column statistics of a stored rows x cols operand whose rows are ld elements
+// apart.  Row chunks of 256, halved (down to 16) while the grid has fewer than
+// four blocks per SM: a 1024-wide operand otherwise runs as 16 blocks.  The
+// chunk count stays within grid.y.
+static void launch_stats_cols(const double* X, int64_t rows, int64_t cols, int64_t ld, int cplx, int sm_count,
                               unsigned long long* mx, long long* es, int* cn, int* bad, cudaStream_t st) {
     const int64_t bx = f4j_cdiv(cols, 256);
     int64_t chunk = 256;
     while (chunk > 16 && bx * f4j_cdiv(rows, chunk) < 4 * (int64_t)sm_count) chunk /= 2;
     while (f4j_cdiv(rows, chunk) > 65535) chunk *= 2;
-    k_stats_cols<<<dim3((unsigned)bx, (unsigned)f4j_cdiv(rows, chunk)), 256, 0, st>>>(X, rows, cols, cplx, (int)chunk,
-                                                                                      mx, es, cn, bad);
+    k_stats_cols<<<dim3((unsigned)bx, (unsigned)f4j_cdiv(rows, chunk)), 256, 0, st>>>(X, rows, cols, ld, cplx,
+                                                                                      (int)chunk, mx, es, cn, bad);
 }
 
 // Offsets in the small workspace of one split GEMM (M rows of op(A), n
@@ -1267,13 +1273,13 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     if (a_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, ctx->stream>>>(A, M, k, cplx, mxa, esa, cna, misc);
     } else {
-        launch_stats_cols(A, k, M, cplx, ctx->sm_count, mxa, esa, cna, misc, ctx->stream);
+        launch_stats_cols(A, k, M, M, cplx, ctx->sm_count, mxa, esa, cna, misc, ctx->stream);
     }
     F4J_LAUNCHED(ctx);
     if (b_rows) {
         k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, ctx->stream>>>(B, n, k, cplx, mxb, esb, cnb, misc);
     } else {
-        launch_stats_cols(B, k, n, cplx, ctx->sm_count, mxb, esb, cnb, misc, ctx->stream);
+        launch_stats_cols(B, k, n, n, cplx, ctx->sm_count, mxb, esb, cnb, misc, ctx->stream);
     }
     F4J_LAUNCHED(ctx);
     {   // exponents, spreads and the plan in one launch: the plan comes from the
@@ -1322,6 +1328,8 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     prm.plan = plan;
     prm.tm0 = 0;
     prm.tm1 = (int)f4j_cdiv(M, BM);
+    prm.tn0 = 0;
+    prm.tn1 = (int)f4j_cdiv(N, BN);
     prm.wpart = kchunks ? reinterpret_cast<long long*>(slB + al1k(plane_b * S_MAX)) : nullptr;
     L->tiles_m = prm.tm1;
     L->tiles_n = (int)f4j_cdiv(N, BN);
@@ -1329,17 +1337,25 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
     return F4J_OK;
 }
 
-// The slice GEMM over tile rows [tm0, tm1) of C on `stream`.
-static int split_launch(f4j_ctx* ctx, const SplitLaunch& L, cudaStream_t stream, int tm0, int tm1) {
+// The slice GEMM over tile rows [tm0, tm1) and tile columns [tn0, tn1) of C
+// on `stream` (tn1 < 0: every tile column).
+static int split_launch(f4j_ctx* ctx, const SplitLaunch& L, cudaStream_t stream, int tm0, int tm1, int tn0 = 0,
+                        int tn1 = -1) {
     SplitGemmParams prm = L.prm;
     prm.tm0 = tm0;
     prm.tm1 = tm1;
+    prm.tn0 = tn0;
+    prm.tn1 = tn1 < 0 ? L.tiles_n : tn1;
     const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     cudaError_t e = cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return f4j_cuda_fail(e, "cudaFuncSetAttribute(k_split_gemm)");
     const bool ksplit = prm.wpart != nullptr;
-    if (ksplit && (tm0 != 0 || tm1 != L.tiles_m)) return f4j_fail(F4J_ERR_ARG, "split-K slice GEMM over a row part");
-    const int64_t nunits = (int64_t)L.tiles_n * (tm1 - tm0) * (ksplit ? L.kchunks : 1);
+    if (ksplit && (tm0 != 0 || tm1 != L.tiles_m || prm.tn0 != 0 || prm.tn1 != L.tiles_n))
+        return f4j_fail(F4J_ERR_ARG, "split-K slice GEMM over part of C");
+    if (tm0 < 0 || tm1 > L.tiles_m || tm0 >= tm1 || prm.tn0 < 0 || prm.tn1 > L.tiles_n || prm.tn0 >= prm.tn1)
+        return f4j_fail(F4J_ERR_ARG, "slice GEMM tile range [%d, %d) x [%d, %d) outside %d x %d", tm0, tm1, prm.tn0,
+                        prm.tn1, L.tiles_m, L.tiles_n);
+    const int64_t nunits = (int64_t)(prm.tn1 - prm.tn0) * (tm1 - tm0) * (ksplit ? L.kchunks : 1);
     const unsigned grid = (unsigned)(nunits < ctx->sm_count ? nunits : ctx->sm_count);
     const cudaStream_t saved = ctx->stream;
     ctx->stream = stream;
@@ -1393,23 +1409,37 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 }
 
 // ------------------------------------------------------------------ host buffers
-// The split product C = A op(B) from host memory with its upload pipelined
-// (f4j_dgemm_host, op(A) = N): B goes up first and is summarised; then A goes
-// up in row parts, and each part's statistics and slicing run as soon as its
-// rows are on the device, its slice GEMM on the part's own stream with its
-// rows of C going down behind it.  The slice count cannot wait for all of A,
-// so it is picked from B and A's first part (k_plan_pick on the spreads so
-// far).  Once every part's statistics are in, k_spec_check compares it with
-// the count all of A gives: *recompute is set when they differ, or when an
-// operand holds a NaN / Inf, and the caller then runs the ordinary path.  When
-// the counts agree, every slice, plan and sum is the ordinary path's, and so
-// is every bit of C.  The first part is small, so the products start soon
-// after B is up; the last part is small too, so little of C's download
-// follows the last product.  Waits for everything it queued before returning;
-// *spread_out receives the spread all of A and B give.
+// The split product C = A op(B) from host memory with its uploads pipelined
+// (f4j_dgemm_host, op(A) = N).  The uploads go back to back on their own
+// stream: A's first row part, then B in column parts, then the rest of A in
+// row parts.  Each part's statistics and slicing run on the context stream as
+// soon as it is up; each column part of B is then multiplied by A's first
+// rows, and each later row part of A by all of B.  Every product is one launch
+// on its own stream, its block of C going down behind it.  The slice count
+// cannot wait for all of A and B, so it is picked from A's first rows and B's
+// first columns (k_plan_pick on the spreads so far).  Once every statistic is
+// in, k_spec_check compares it with the count all of A and B give: *recompute
+// is set when they differ, or when an operand holds a NaN / Inf, and the
+// caller then runs the ordinary path.  When the counts agree, every exponent,
+// slice, plan and tile sum is the ordinary path's, and so is every bit of C.
+// Waits for everything it queued before returning; *spread_out receives the
+// spread all of A and B give.
+//
+// Part sizes.  A's first part has up to 8 tile rows: its product with one of
+// F4J_HOST_BPARTS = 4 column parts of B takes about as long as the next column
+// part's upload (both scale with K and the part's width; measured at 8192^3:
+// 0.67 ms of product on 128 SMs per 0.75 ms of upload).  B's column parts go up
+// as 2D copies: 4 parts of an 8192-column B (16 KB rows) move 180 GB/s, 8
+// parts (8 KB rows) only 106 GB/s.  A's second part is as small as its first,
+// so that products follow soon after B's upload ends; the last part is 1/8 of
+// the tile rows, so that little of C's download follows the last product; the
+// rest is in equal middle parts.  A part's statistics and slicing cannot run
+// beside a slice GEMM (its CTA fills two of an SM's four register files and
+// all but ~1 KB of its shared memory), so they wait for SMs whenever the
+// products before them hold every SM; these sizes keep that wait short.
 static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, const double* B,
-                                int opB, double* C, double* dA, double* dB, double* dC, int parts, bool* recompute,
-                                const SplitPlan** plan_out, float* spread_out) {
+                                int opB, double* C, double* dA, double* dB, double* dC, int parts, int bparts,
+                                bool* recompute, const SplitPlan** plan_out, float* spread_out) {
     *recompute = false;
     const int64_t M = m, N = n;
     const int64_t Kp = f4j_cdiv(k, BKB) * BKB;  // K padded to whole K blocks
@@ -1433,25 +1463,13 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     SplitPlan* plan = (SplitPlan*)(w + Lo.plan);
     uint8_t* slA = (uint8_t*)ws0;
     uint8_t* slB = slA + al1k(plane_a * S_MAX);
-    const bool b_rows = opB != F4J_OP_N;
+    const bool b_rows = opB != F4J_OP_N;  // columns of op(B) are stored rows of B (n x k)
     const int s_req = env_slices();
     // the same K-chunk cap the ordinary path plans with (no split K here)
     int kchunks = 0;
     const int kcb_cap = split_kcb_cap(f4j_cdiv(M, BM) * f4j_cdiv(N, BN), Kp / BKB, &kchunks);
-    if (kchunks) return f4j_fail(F4J_ERR_ARG, "split-K product in row parts");
+    if (kchunks) return f4j_fail(F4J_ERR_ARG, "split-K product in parts");
     const cudaStream_t st = ctx->stream;
-
-    F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
-    // B first: every part's product needs all of it
-    F4J_CUDA(cudaMemcpyAsync(dB, B, (size_t)k * n * 8, cudaMemcpyHostToDevice, st));
-    if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(n, 8), 256, 0, st>>>(dB, n, k, 0, mxb, esb, cnb, misc);
-    else launch_stats_cols(dB, k, n, 0, ctx->sm_count, mxb, esb, cnb, misc, st);
-    F4J_LAUNCHED(ctx);
-    k_stats_finalize<<<(unsigned)f4j_cdiv(n, 256), 256, 0, st>>>(n, 0, mxb, esb, cnb, eb, misc + 2);
-    F4J_LAUNCHED(ctx);
-    SplitPlan* tab = nullptr;
-    rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
-    if (rc) return rc;
 
     SplitLaunch L;
     rc = make_slice_map(&L.ta, slA, Kp, M, S_MAX);
@@ -1476,58 +1494,142 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     L.kchunks = 0;
     prm.tm0 = 0;
     prm.tm1 = L.tiles_m;
+    prm.tn0 = 0;
+    prm.tn1 = L.tiles_n;
 
-    // part boundaries in tile rows: a small first part (1/16), a small last
-    // part (1/8), the rest in equal middle parts; every part at least one tile row
-    const int tiles_m = L.tiles_m;
+    // A's row parts and B's column parts, in tile rows / columns
+    const int tiles_m = L.tiles_m, tiles_n = L.tiles_n;
+    if (parts < 2 || parts > tiles_m || parts > F4J_HOST_PARTS_MAX)
+        return f4j_fail(F4J_ERR_ARG, "%d row parts of %d tile rows", parts, tiles_m);
     int bound[F4J_HOST_PARTS_MAX + 1];
-    bound[0] = 0;
-    bound[parts] = tiles_m;
     {
-        const int first = tiles_m / 16 > 1 ? tiles_m / 16 : 1;
-        const int last = parts > 2 ? (tiles_m / 8 > 1 ? tiles_m / 8 : 1) : tiles_m - first;
-        bound[1] = first;
-        bound[parts - 1] = tiles_m - last;
-        for (int p = 2; p < parts - 1; p++)
-            bound[p] = first + (int)((int64_t)(bound[parts - 1] - first) * (p - 1) / (parts - 2));
+        const int a0 = tiles_m / 4 < 1 ? 1 : (tiles_m / 4 > 8 ? 8 : tiles_m / 4);
+        const int last = tiles_m / 8 < 1 ? 1 : tiles_m / 8;
+        bound[0] = 0;
+        bound[parts] = tiles_m;
+        bound[1] = a0;
+        if (parts >= 3) bound[parts - 1] = tiles_m - last;
+        if (parts >= 4) bound[2] = 2 * a0;
+        for (int p = 3; p < parts - 1; p++)
+            bound[p] = bound[2] + (int)((int64_t)(bound[parts - 1] - bound[2]) * (p - 2) / (parts - 3));
         for (int p = 1; p < parts; p++) {  // keep every part non-empty
             const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);
             bound[p] = bound[p] < lo ? lo : (bound[p] > hi ? hi : bound[p]);
         }
     }
-    int launched = 0;
-    for (int p = 0; p < parts && !rc; p++) {
-        const int64_t r0 = (int64_t)bound[p] * BM;
-        const int64_t r1 = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
-        const int64_t rows = r1 - r0;
-        F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)rows * k * 8, cudaMemcpyHostToDevice, st));
+    const int qb = bparts < tiles_n ? bparts : tiles_n;
+    int cbound[F4J_HOST_PARTS_MAX + 1];
+    for (int j = 0; j <= qb; j++) cbound[j] = (int)((int64_t)tiles_n * j / qb);
+
+    F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
+    SplitPlan* tab = nullptr;
+    rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
+    if (rc) return rc;
+
+    // Every upload goes up back to back on the upload stream, in the order the
+    // parts are used (A's first rows, B's column parts, the rest of A); the
+    // kernels of part u wait on its event up_ev[u] on the context stream.
+    const cudaStream_t up = ctx->up_stream;
+    F4J_CUDA(cudaEventRecord(ctx->up_start, st));
+    F4J_CUDA(cudaStreamWaitEvent(up, ctx->up_start, 0));
+    {
+        int u = 0;
+        const int64_t r1 = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
+        F4J_CUDA(cudaMemcpyAsync(dA, A, (size_t)r1 * k * 8, cudaMemcpyHostToDevice, up));
+        F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+        for (int j = 0; j < qb; j++) {
+            const int64_t c0 = (int64_t)cbound[j] * BN;
+            const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
+            if (b_rows)  // stored rows [c0, c1) of B (n x k)
+                F4J_CUDA(cudaMemcpyAsync(dB + c0 * k, B + c0 * k, (size_t)(c1 - c0) * k * 8, cudaMemcpyHostToDevice,
+                                         up));
+            else         // stored columns [c0, c1) of B (k x n)
+                F4J_CUDA(cudaMemcpy2DAsync(dB + c0, (size_t)n * 8, B + c0, (size_t)n * 8, (size_t)(c1 - c0) * 8,
+                                           (size_t)k, cudaMemcpyHostToDevice, up));
+            F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+        }
+        for (int p = 1; p < parts; p++) {
+            const int64_t r0 = (int64_t)bound[p] * BM;
+            const int64_t re = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
+            F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)(re - r0) * k * 8, cudaMemcpyHostToDevice, up));
+            F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+        }
+    }
+
+    // one row part of A (upload u): statistics, exponents (spread into misc[1])
+    auto a_part_stats = [&](int u, int64_t r0, int64_t rows) -> int {
+        F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[u], 0));
         k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k, rows, k, 0, mxa + r0, esa + r0,
                                                                   cna + r0, misc);
         F4J_LAUNCHED(ctx);
         k_stats_finalize<<<(unsigned)f4j_cdiv(rows, 256), 256, 0, st>>>(rows, 0, mxa + r0, esa + r0, cna + r0,
                                                                          ea + r0, misc + 1);
         F4J_LAUNCHED(ctx);
-        if (p == 0) {  // the plan from B and the first rows, then B's slices
-            k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
-            F4J_LAUNCHED(ctx);
-            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(n, SP_TR)), 256, 0, st>>>(
-                dB, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, n, k, Kp, Kp, N, eb, plan, slB);
-            F4J_LAUNCHED(ctx);
-        }
-        // this part's rows of the slice planes: target t of the part is row r0 + t
+        return F4J_OK;
+    };
+    // its slice planes: target t of the part is row r0 + t
+    auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
         k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
             dA + r0 * k, rows, k, 0, 0, 0, 0, rows, k, Kp, Kp, M, ea + r0, plan, slA + r0 * Kp);
         F4J_LAUNCHED(ctx);
-        F4J_CUDA(cudaEventRecord(ctx->part_prep_ev[p], st));
-        const cudaStream_t ps = ctx->part_stream[p];
-        F4J_CUDA(cudaStreamWaitEvent(ps, ctx->part_prep_ev[p], 0));
-        launched = p + 1;
-        rc = split_launch(ctx, L, ps, bound[p], bound[p + 1]);
-        if (!rc) {
-            cudaError_t e = cudaMemcpyAsync(C + r0 * n, dC + r0 * n, (size_t)rows * n * 8, cudaMemcpyDeviceToHost, ps);
-            if (e == cudaSuccess) e = cudaEventRecord(ctx->part_ev[p], ps);
-            if (e != cudaSuccess) rc = f4j_cuda_fail(e, "download of a row part");
+        return F4J_OK;
+    };
+    // launch `id`: its stream waits for the slicing queued so far, runs the
+    // slice GEMM over tile rows [tm0, tm1) x tile columns [tn0, tn1), and
+    // downloads that block of C
+    int launched = 0;
+    auto product = [&](int id, int tm0, int tm1, int tn0, int tn1) -> int {
+        F4J_CUDA(cudaEventRecord(ctx->part_prep_ev[id], st));
+        const cudaStream_t ps = ctx->part_stream[id];
+        F4J_CUDA(cudaStreamWaitEvent(ps, ctx->part_prep_ev[id], 0));
+        launched = id + 1;
+        int r = split_launch(ctx, L, ps, tm0, tm1, tn0, tn1);
+        if (r) return r;
+        const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
+        const int64_t c0 = (int64_t)tn0 * BN, c1 = (int64_t)tn1 * BN < n ? (int64_t)tn1 * BN : n;
+        F4J_CUDA(cudaMemcpy2DAsync(C + r0 * n + c0, (size_t)n * 8, dC + r0 * n + c0, (size_t)n * 8,
+                                   (size_t)(c1 - c0) * 8, (size_t)(r1 - r0), cudaMemcpyDeviceToHost, ps));
+        F4J_CUDA(cudaEventRecord(ctx->part_ev[id], ps));
+        return F4J_OK;
+    };
+
+    // A's first rows, then B's column parts, each multiplied by those rows
+    const int64_t a0_rows = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
+    rc = a_part_stats(0, 0, a0_rows);
+    for (int j = 0; j < qb && !rc; j++) {
+        const int64_t c0 = (int64_t)cbound[j] * BN;
+        const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
+        const int64_t cw = c1 - c0;
+        F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[1 + j], 0));
+        if (b_rows) {  // stored rows [c0, c1) of B (n x k)
+            k_stats_rows<<<(unsigned)f4j_cdiv(cw, 8), 256, 0, st>>>(dB + c0 * k, cw, k, 0, mxb + c0, esb + c0,
+                                                                    cnb + c0, misc);
+        } else {       // stored columns [c0, c1) of B (k x n)
+            launch_stats_cols(dB + c0, k, cw, n, 0, ctx->sm_count, mxb + c0, esb + c0, cnb + c0, misc, st);
         }
+        F4J_LAUNCHED(ctx);
+        k_stats_finalize<<<(unsigned)f4j_cdiv(cw, 256), 256, 0, st>>>(cw, 0, mxb + c0, esb + c0, cnb + c0, eb + c0,
+                                                                       misc + 2);
+        F4J_LAUNCHED(ctx);
+        if (j == 0) {  // the plan from A's first rows and B's first columns, then those rows' slices
+            k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
+            F4J_LAUNCHED(ctx);
+            rc = a_part_split(0, a0_rows);
+            if (rc) break;
+        }
+        k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
+            b_rows ? dB + c0 * k : dB + c0, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, cw, k, Kp, Kp,
+            N, eb + c0, plan, slB + c0 * Kp);
+        F4J_LAUNCHED(ctx);
+        rc = product(j, 0, bound[1], cbound[j], cbound[j + 1]);
+    }
+    // the rest of A, each row part multiplied by all of B
+    for (int p = 1; p < parts && !rc; p++) {
+        const int64_t r0 = (int64_t)bound[p] * BM;
+        const int64_t r1 = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
+        rc = a_part_stats(qb + p, r0, r1 - r0);
+        if (!rc) rc = a_part_split(r0, r1 - r0);
+        if (!rc) rc = product(qb + p - 1, bound[p], bound[p + 1], 0, tiles_n);
     }
     int hm[6] = {0, 0, 0, 0, 0, 0};
     if (!rc) {
@@ -1539,10 +1641,16 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = f4j_cuda_fail(e, "slice count check of a host-buffer product");
+    } else {
+        cudaStreamSynchronize(st);
     }
-    for (int p = 0; p < launched; p++) {
-        cudaError_t e = cudaStreamSynchronize(ctx->part_stream[p]);
-        if (e != cudaSuccess && !rc) rc = f4j_cuda_fail(e, "row part of a host-buffer product");
+    {
+        cudaError_t e = cudaStreamSynchronize(up);
+        if (e != cudaSuccess && !rc) rc = f4j_cuda_fail(e, "upload of a host-buffer product");
+    }
+    for (int i = 0; i < launched; i++) {
+        cudaError_t e = cudaStreamSynchronize(ctx->part_stream[i]);
+        if (e != cudaSuccess && !rc) rc = f4j_cuda_fail(e, "part of a host-buffer product");
     }
     if (rc) return rc;
     *recompute = hm[5] != 0;
@@ -1553,10 +1661,11 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
 
 // C = op(A) op(B) from and to host memory (pinned for full copy speed).  A
 // split product with op(A) = N and at least two tile rows runs pipelined
-// (host_split_pipelined): B up first, then A in F4J_HOST_PARTS row parts, each
-// part sliced and multiplied on its own stream as soon as its rows arrive and
-// its rows of C downloaded behind its product.  In the rare case that all of
-// A asks for another slice count than its first part did (or an operand holds
+// (host_split_pipelined): A's first rows up, then B in F4J_HOST_BPARTS column
+// parts, then the rest of A in row parts (F4J_HOST_PARTS in all), each part
+// sliced and multiplied on its own stream as soon as it arrives and its block
+// of C downloaded behind its product.  In the rare case that all of A and B
+// ask for another slice count than their first parts did (or an operand holds
 // a NaN / Inf), the product runs again through the ordinary path on the
 // operands already on the device.  Either way C equals f4j_dgemm's bit for
 // bit.  Other products upload, multiply and download in turn.  Returns when C
@@ -1589,8 +1698,9 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     if (rc) return rc;
     const bool split = k > 0 && f4j_resolve_mode(false, m, n, k, mode) == F4J_MODE_SPLIT;
     const int tiles_m = (int)f4j_cdiv(m, BM);
-    const int want = env_host_parts();
+    const int want = env_host_parts("F4J_HOST_PARTS", F4J_HOST_PARTS);
     const int parts = tiles_m < want ? tiles_m : want;
+    const int bparts = env_host_parts("F4J_HOST_BPARTS", F4J_HOST_BPARTS);
     int kchunks = 0;
     split_kcb_cap(tiles_m * f4j_cdiv(n, BN), f4j_cdiv(k, BKB), &kchunks);
     if (!split || opA != F4J_OP_N || parts < 2 || kchunks) {  // split K runs as one launch
@@ -1605,19 +1715,22 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
                                    (const double*)dC, check_samples, check_flags, rep);
     }
     if (!ctx->parts_init) {
-        for (int i = 0; i < F4J_HOST_PARTS_MAX; i++) {
+        for (int i = 0; i < F4J_HOST_STREAMS; i++) {
             F4J_CUDA(cudaStreamCreateWithFlags(&ctx->part_stream[i], cudaStreamNonBlocking));
             F4J_CUDA(cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming));
             F4J_CUDA(cudaEventCreateWithFlags(&ctx->part_prep_ev[i], cudaEventDisableTiming));
+            F4J_CUDA(cudaEventCreateWithFlags(&ctx->up_ev[i], cudaEventDisableTiming));
         }
+        F4J_CUDA(cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+        F4J_CUDA(cudaEventCreateWithFlags(&ctx->up_start, cudaEventDisableTiming));
         ctx->parts_init = true;
     }
     const int64_t l0 = ctx->launches;
     bool recompute = false;
     const SplitPlan* plan = nullptr;
     float spread = 0.0f;
-    rc = host_split_pipelined(ctx, m, n, k, A, B, opB, C, (double*)dA, (double*)dB, (double*)dC, parts, &recompute,
-                              &plan, &spread);
+    rc = host_split_pipelined(ctx, m, n, k, A, B, opB, C, (double*)dA, (double*)dB, (double*)dC, parts, bparts,
+                              &recompute, &plan, &spread);
     if (rc) return rc;
     if (recompute) {
         // all of A asks for another slice count than its first rows did, or an
@@ -1740,9 +1853,9 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
 
     const bool a_rows = (opA == F4J_OP_N), b_rows = (opB != F4J_OP_N);
     if (a_rows) k_stats_rows<<<(unsigned)f4j_cdiv(M, 8), 256, 0, st>>>(A, M, k, 0, mxa, esa, cna, misc);
-    else launch_stats_cols(A, k, M, 0, sms, mxa, esa, cna, misc, st);
+    else launch_stats_cols(A, k, M, M, 0, sms, mxa, esa, cna, misc, st);
     if (b_rows) k_stats_rows<<<(unsigned)f4j_cdiv(N, 8), 256, 0, st>>>(B, N, k, 0, mxb, esb, cnb, misc);
-    else launch_stats_cols(B, k, N, 0, sms, mxb, esb, cnb, misc, st);
+    else launch_stats_cols(B, k, N, N, 0, sms, mxb, esb, cnb, misc, st);
     k_stats_finalize<<<(unsigned)f4j_cdiv(M, 256), 256, 0, st>>>(M, 0, mxa, esa, cna, ea, misc + 1);
     k_stats_finalize<<<(unsigned)f4j_cdiv(N, 256), 256, 0, st>>>(N, 0, mxb, esb, cnb, eb, misc + 2);
     int kchunks_na = 0;  // the same chunks as f4j_dgemm plans for this shape, run in turn
@@ -1776,6 +1889,8 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     prm.plan = plan;
     prm.tm0 = 0;
     prm.tm1 = (int)f4j_cdiv(M, BM);
+    prm.tn0 = 0;
+    prm.tn1 = (int)f4j_cdiv(N, BN);
     const size_t smem = (size_t)RING * TILE_BYTES + 1024 + sizeof(SplitPlan) + (size_t)NSTAGE * MAX_OPS * sizeof(Op);
     F4J_CUDA(cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t ntiles = f4j_cdiv(N, BN) * f4j_cdiv(M, BM);

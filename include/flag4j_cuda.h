@@ -238,11 +238,13 @@ int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
 /* f4j_dgemm from and to host memory: A, B, C are host pointers (row-major;
  * page-locked by f4j_host_alloc or f4j_host_register for full copy speed,
  * pageable works), and the call returns when C is in host memory.  A split
- * product with opA = N is pipelined: B is uploaded first, then A in row parts,
- * each part sliced and multiplied on its own stream as its rows arrive and its
- * rows of C downloaded behind its product.  The slice count is taken from B
- * and A's first part; when all of A asks for another count (or an operand
- * holds a NaN / Inf) the product runs again through the f4j_dgemm path.  A
+ * product with opA = N is pipelined: A's first rows are uploaded first, then B
+ * in column parts, then the rest of A in row parts, back to back; each part is
+ * sliced as it arrives and each product (B's column parts by A's first rows,
+ * then A's later row parts by all of B) runs on its own stream, its block of C
+ * downloaded behind it.  The slice count is taken from the first parts of A
+ * and B; when all of A and B ask for another count (or an operand holds a
+ * NaN / Inf) the product runs again through the f4j_dgemm path.  A
  * product that splits K (fewer than 152 output tiles and K <= 4096) uploads,
  * multiplies and downloads in turn.  The result is bitwise the f4j_dgemm
  * result.  This is

@@ -429,32 +429,32 @@ def test_wrap_rejects_misaligned_and_null(f4j):
         check(ctx.lib.f4j_buf_wrap(ctx.handle, None, 64, ctypes.byref(h)))
 
 
-@pytest.mark.parametrize("m,n,k,mode,opA,host", [
-    # pipelined (B up first, A in row parts of 128-row tile rows: first 1/16, last 1/8)
-    (2500, 900, 700, "split", 0, "allocated"),   # 20 x 8 tiles in f4j_host_alloc memory: parts 1, 8, 9, 2
-    (2000, 1300, 600, "split", 0, "registered"),  # 16 x 11 tiles: parts 1, 6, 7, 2
-    (1500, 2000, 300, "split", 0, "pageable"),   # 12 x 16 tiles, pageable host memory: parts 1, 5, 5, 1
-    (300, 260, 5000, "split", 0, "registered"),  # 9 tiles but 79 K blocks (no split K): parts 1, 1, 1
-    (130, 200, 4500, "split", 0, "allocated"),   # 2 tile rows, the last ragged: parts 1, 1
+@pytest.mark.parametrize("m,n,k,mode,opA,opB,host", [
+    # pipelined: A's first row part, B's column parts, the rest of A (parts in 128-row tile rows / columns)
+    (2500, 900, 700, "split", 0, 0, "allocated"),   # 20 x 8 tiles, f4j_host_alloc memory: A 5, 5, 8, 2; B 2 x 4
+    (2000, 1300, 600, "split", 0, 1, "registered"),  # 16 x 11 tiles, B stored n x k: A 4, 4, 6, 2; B 2, 3, 3, 3
+    (1500, 2000, 300, "split", 0, 0, "pageable"),   # 12 x 16 tiles, ragged last column: A 3, 3, 5, 1; B 4 x 4
+    (300, 260, 5000, "split", 0, 1, "registered"),  # 3 x 3 tiles, 79 K blocks (no split K): A 1, 1, 1; B 1, 1, 1
+    (130, 200, 4500, "split", 0, 0, "allocated"),   # 2 x 2 tiles, the last row ragged: A 1, 1; B 1, 1
     # uploaded, multiplied and downloaded in turn
-    (1000, 700, 900, "split", 0, "registered"),  # 48 tiles, 15 K blocks: split K
-    (300, 260, 520, "split", 0, "pageable"),     # 9 tiles: split K
-    (100, 90, 80, "split", 0, "allocated"),      # one tile row
-    (600, 500, 400, "split", 1, "registered"),   # op(A) = T
-    (500, 300, 200, "plain", 0, "registered"),
-    (64, 48, 40, "exact", 0, "allocated"),
+    (1000, 700, 900, "split", 0, 0, "registered"),  # 48 tiles, 15 K blocks: split K
+    (300, 260, 520, "split", 0, 0, "pageable"),     # 9 tiles: split K
+    (100, 90, 80, "split", 0, 0, "allocated"),      # one tile row
+    (600, 500, 400, "split", 1, 0, "registered"),   # op(A) = T
+    (500, 300, 200, "plain", 0, 0, "registered"),
+    (64, 48, 40, "exact", 0, 1, "allocated"),
 ])
-def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, host):
+def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, opB, host):
     """f4j_dgemm_host is bitwise f4j_dgemm on the same operands, from registered, pageable or
     f4j_host_alloc host memory, with the same slice count and spread in the report."""
     from flag4j_gb300 import _lib, synth
     from flag4j_gb300.device import check, pinned_empty
     ctx = f4j.default_context()
     A = synth.scaled(m, k, 4, 21, "row") if opA == 0 else synth.scaled(k, m, 4, 21, "col")
-    B = synth.scaled(k, n, 4, 22, "col")
+    B = synth.scaled(k, n, 4, 22, "col") if opB == 0 else synth.scaled(n, k, 4, 22, "row")
     dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(8 * m * n)
     rd = _lib.f4j_report()
-    check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, 0, dC.handle, _lib.MODES[mode],
+    check(ctx.lib.f4j_dgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, opB, dC.handle, _lib.MODES[mode],
                             ctypes.byref(rd)))
     ref = dC.to_numpy(np.float64, m * n).reshape(m, n)
     C = np.full((m, n), np.nan)
@@ -469,7 +469,7 @@ def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, host):
             check(ctx.lib.f4j_host_register(a.ctypes.data, a.nbytes))
     try:
         rep = _lib.f4j_report()
-        check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, opA, B.ctypes.data, 0, C.ctypes.data,
+        check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, opA, B.ctypes.data, opB, C.ctypes.data,
                                      _lib.MODES[mode], ctypes.byref(rep)))
         assert np.array_equal(C, ref)
         if mode == "split":
@@ -504,44 +504,47 @@ def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
     assert np.all(np.abs(C[fin] - ref) <= bound)
 
 
-@pytest.mark.parametrize("case", ["wider_spread_late", "nan_late", "inf_first"])
+@pytest.mark.parametrize("case", ["wider_a_late", "wider_b_late", "nan_late", "inf_first"])
 def test_host_buffer_gemm_speculative_slice_count(f4j, case):
-    """The pipelined host-buffer product picks its slice count from B and A's
-    first row part (128 rows here).  When all of A asks for another count, or
-    an operand holds a NaN / Inf, the product runs again through the device
-    path: C, the mode used and the slice count still equal f4j_dgemm's, NaN
-    and Inf bits included."""
+    """The pipelined host-buffer product picks its slice count from A's first
+    row part and B's first column part (512 rows and 384 columns here).  When
+    all of A and B ask for another count, or an operand holds a NaN / Inf, the
+    product runs again through the device path: C, the mode used and the slice
+    count still equal f4j_dgemm's, NaN and Inf bits included."""
     from flag4j_gb300 import _lib, synth
     from flag4j_gb300.device import check
     ctx = f4j.default_context()
-    m, n, k = 2048, 1536, 1024   # 16 x 12 tiles, 16 K blocks: pipelined, parts of 1, 6, 7, 2 tile rows
+    m, n, k = 2048, 1536, 1024   # 16 x 12 tiles, 16 K blocks: A parts of 4, 4, 6, 2 tile rows, B parts of 3 x 4
+    a0, b0 = 512, 384
     A = synth.uniform(m, k, 51)
     B = synth.uniform(k, n, 52)
-    if case == "wider_spread_late":
-        # rows past the first part: elements scaled by 2^-j, j uniform in [0, 24]
-        A[128:] *= np.ldexp(1.0, -synth.rng(53).integers(0, 25, size=(m - 128, k)))
+    g = synth.rng(53)
+    if case == "wider_a_late":   # rows past A's first part: elements scaled by 2^-j, j uniform in [0, 24]
+        A[a0:] *= np.ldexp(1.0, -g.integers(0, 25, size=(m - a0, k)))
+    elif case == "wider_b_late":  # the same for the columns past B's first part
+        B[:, b0:] *= np.ldexp(1.0, -g.integers(0, 25, size=(k, n - b0)))
     elif case == "nan_late":
         A[1500, 17] = np.nan
     else:
         A[3, 900] = np.inf
 
-    def device(Ad):
-        mm = Ad.shape[0]
-        dA, dB, dC = ctx.from_numpy(Ad), ctx.from_numpy(B), ctx.alloc(8 * mm * n)
+    def device(Ad, Bd):
+        mm, nn = Ad.shape[0], Bd.shape[1]
+        dA, dB, dC = ctx.from_numpy(Ad), ctx.from_numpy(Bd), ctx.alloc(8 * mm * nn)
         rd = _lib.f4j_report()
-        check(ctx.lib.f4j_dgemm(ctx.handle, mm, n, k, dA.handle, 0, dB.handle, 0, dC.handle, _lib.MODE_SPLIT,
+        check(ctx.lib.f4j_dgemm(ctx.handle, mm, nn, k, dA.handle, 0, dB.handle, 0, dC.handle, _lib.MODE_SPLIT,
                                 ctypes.byref(rd)))
-        return dC.to_numpy(np.float64, mm * n).reshape(mm, n), rd
+        return dC.to_numpy(np.float64, mm * nn).reshape(mm, nn), rd
 
-    ref, rd = device(A)
+    ref, rd = device(A, B)
     C = np.zeros((m, n))
     rep = _lib.f4j_report()
     check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, 0, B.ctypes.data, 0, C.ctypes.data,
                                  _lib.MODE_SPLIT, ctypes.byref(rep)))
     assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
     assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
-    if case == "wider_spread_late":
-        _, r_first = device(np.ascontiguousarray(A[:128]))
+    if case.startswith("wider"):
+        _, r_first = device(np.ascontiguousarray(A[:a0]), np.ascontiguousarray(B[:, :b0]))
         assert rd.mode_used == _lib.MODE_SPLIT and rd.slices > r_first.slices   # the first pick was too few
         assert rep.exp_spread == rd.exp_spread
     else:
