@@ -1521,116 +1521,123 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     int cbound[F4J_HOST_PARTS_MAX + 1];
     for (int j = 0; j <= qb; j++) cbound[j] = (int)((int64_t)tiles_n * j / qb);
 
-    F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
-    SplitPlan* tab = nullptr;
-    rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
-    if (rc) return rc;
+    // everything is queued by `queue`; whatever it returns, every stream that
+    // holds queued work is waited for before this function returns, so no
+    // copy still reads A or B, or writes C, after an error
+    int launched = 0;
+    auto queue = [&]() -> int {
+        F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
+        SplitPlan* tab = nullptr;
+        rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
+        if (rc) return rc;
 
-    // Every upload goes up back to back on the upload stream, in the order the
-    // parts are used (A's first rows, B's column parts, the rest of A); the
-    // kernels of part u wait on its event up_ev[u] on the context stream.
-    const cudaStream_t up = ctx->up_stream;
-    F4J_CUDA(cudaEventRecord(ctx->up_start, st));
-    F4J_CUDA(cudaStreamWaitEvent(up, ctx->up_start, 0));
-    {
-        int u = 0;
-        const int64_t r1 = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
-        F4J_CUDA(cudaMemcpyAsync(dA, A, (size_t)r1 * k * 8, cudaMemcpyHostToDevice, up));
-        F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
-        for (int j = 0; j < qb; j++) {
+        // Every upload goes up back to back on the upload stream, in the order the
+        // parts are used (A's first rows, B's column parts, the rest of A); the
+        // kernels of part u wait on its event up_ev[u] on the context stream.
+        const cudaStream_t up = ctx->up_stream;
+        F4J_CUDA(cudaEventRecord(ctx->up_start, st));
+        F4J_CUDA(cudaStreamWaitEvent(up, ctx->up_start, 0));
+        {
+            int u = 0;
+            const int64_t r1 = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
+            F4J_CUDA(cudaMemcpyAsync(dA, A, (size_t)r1 * k * 8, cudaMemcpyHostToDevice, up));
+            F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+            for (int j = 0; j < qb; j++) {
+                const int64_t c0 = (int64_t)cbound[j] * BN;
+                const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
+                if (b_rows)  // stored rows [c0, c1) of B (n x k)
+                    F4J_CUDA(cudaMemcpyAsync(dB + c0 * k, B + c0 * k, (size_t)(c1 - c0) * k * 8, cudaMemcpyHostToDevice,
+                                             up));
+                else         // stored columns [c0, c1) of B (k x n)
+                    F4J_CUDA(cudaMemcpy2DAsync(dB + c0, (size_t)n * 8, B + c0, (size_t)n * 8, (size_t)(c1 - c0) * 8,
+                                               (size_t)k, cudaMemcpyHostToDevice, up));
+                F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+            }
+            for (int p = 1; p < parts; p++) {
+                const int64_t r0 = (int64_t)bound[p] * BM;
+                const int64_t re = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
+                F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)(re - r0) * k * 8, cudaMemcpyHostToDevice, up));
+                F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
+            }
+        }
+
+        // one row part of A (upload u): statistics, exponents (spread into misc[1])
+        auto a_part_stats = [&](int u, int64_t r0, int64_t rows) -> int {
+            F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[u], 0));
+            k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k, rows, k, 0, mxa + r0, esa + r0,
+                                                                      cna + r0, misc);
+            F4J_LAUNCHED(ctx);
+            k_stats_finalize<<<(unsigned)f4j_cdiv(rows, 256), 256, 0, st>>>(rows, 0, mxa + r0, esa + r0, cna + r0,
+                                                                             ea + r0, misc + 1);
+            F4J_LAUNCHED(ctx);
+            return F4J_OK;
+        };
+        // its slice planes: target t of the part is row r0 + t
+        auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
+            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
+                dA + r0 * k, rows, k, 0, 0, 0, 0, rows, k, Kp, Kp, M, ea + r0, plan, slA + r0 * Kp);
+            F4J_LAUNCHED(ctx);
+            return F4J_OK;
+        };
+        // launch `id`: its stream waits for the slicing queued so far, runs the
+        // slice GEMM over tile rows [tm0, tm1) x tile columns [tn0, tn1), and
+        // downloads that block of C
+        auto product = [&](int id, int tm0, int tm1, int tn0, int tn1) -> int {
+            F4J_CUDA(cudaEventRecord(ctx->part_prep_ev[id], st));
+            const cudaStream_t ps = ctx->part_stream[id];
+            F4J_CUDA(cudaStreamWaitEvent(ps, ctx->part_prep_ev[id], 0));
+            launched = id + 1;
+            int r = split_launch(ctx, L, ps, tm0, tm1, tn0, tn1);
+            if (r) return r;
+            const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
+            const int64_t c0 = (int64_t)tn0 * BN, c1 = (int64_t)tn1 * BN < n ? (int64_t)tn1 * BN : n;
+            F4J_CUDA(cudaMemcpy2DAsync(C + r0 * n + c0, (size_t)n * 8, dC + r0 * n + c0, (size_t)n * 8,
+                                       (size_t)(c1 - c0) * 8, (size_t)(r1 - r0), cudaMemcpyDeviceToHost, ps));
+            F4J_CUDA(cudaEventRecord(ctx->part_ev[id], ps));
+            return F4J_OK;
+        };
+
+        // A's first rows, then B's column parts, each multiplied by those rows
+        const int64_t a0_rows = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
+        rc = a_part_stats(0, 0, a0_rows);
+        for (int j = 0; j < qb && !rc; j++) {
             const int64_t c0 = (int64_t)cbound[j] * BN;
             const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
-            if (b_rows)  // stored rows [c0, c1) of B (n x k)
-                F4J_CUDA(cudaMemcpyAsync(dB + c0 * k, B + c0 * k, (size_t)(c1 - c0) * k * 8, cudaMemcpyHostToDevice,
-                                         up));
-            else         // stored columns [c0, c1) of B (k x n)
-                F4J_CUDA(cudaMemcpy2DAsync(dB + c0, (size_t)n * 8, B + c0, (size_t)n * 8, (size_t)(c1 - c0) * 8,
-                                           (size_t)k, cudaMemcpyHostToDevice, up));
-            F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
-        }
-        for (int p = 1; p < parts; p++) {
-            const int64_t r0 = (int64_t)bound[p] * BM;
-            const int64_t re = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
-            F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)(re - r0) * k * 8, cudaMemcpyHostToDevice, up));
-            F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
-        }
-    }
-
-    // one row part of A (upload u): statistics, exponents (spread into misc[1])
-    auto a_part_stats = [&](int u, int64_t r0, int64_t rows) -> int {
-        F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[u], 0));
-        k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k, rows, k, 0, mxa + r0, esa + r0,
-                                                                  cna + r0, misc);
-        F4J_LAUNCHED(ctx);
-        k_stats_finalize<<<(unsigned)f4j_cdiv(rows, 256), 256, 0, st>>>(rows, 0, mxa + r0, esa + r0, cna + r0,
-                                                                         ea + r0, misc + 1);
-        F4J_LAUNCHED(ctx);
-        return F4J_OK;
-    };
-    // its slice planes: target t of the part is row r0 + t
-    auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
-        k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
-            dA + r0 * k, rows, k, 0, 0, 0, 0, rows, k, Kp, Kp, M, ea + r0, plan, slA + r0 * Kp);
-        F4J_LAUNCHED(ctx);
-        return F4J_OK;
-    };
-    // launch `id`: its stream waits for the slicing queued so far, runs the
-    // slice GEMM over tile rows [tm0, tm1) x tile columns [tn0, tn1), and
-    // downloads that block of C
-    int launched = 0;
-    auto product = [&](int id, int tm0, int tm1, int tn0, int tn1) -> int {
-        F4J_CUDA(cudaEventRecord(ctx->part_prep_ev[id], st));
-        const cudaStream_t ps = ctx->part_stream[id];
-        F4J_CUDA(cudaStreamWaitEvent(ps, ctx->part_prep_ev[id], 0));
-        launched = id + 1;
-        int r = split_launch(ctx, L, ps, tm0, tm1, tn0, tn1);
-        if (r) return r;
-        const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
-        const int64_t c0 = (int64_t)tn0 * BN, c1 = (int64_t)tn1 * BN < n ? (int64_t)tn1 * BN : n;
-        F4J_CUDA(cudaMemcpy2DAsync(C + r0 * n + c0, (size_t)n * 8, dC + r0 * n + c0, (size_t)n * 8,
-                                   (size_t)(c1 - c0) * 8, (size_t)(r1 - r0), cudaMemcpyDeviceToHost, ps));
-        F4J_CUDA(cudaEventRecord(ctx->part_ev[id], ps));
-        return F4J_OK;
-    };
-
-    // A's first rows, then B's column parts, each multiplied by those rows
-    const int64_t a0_rows = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
-    rc = a_part_stats(0, 0, a0_rows);
-    for (int j = 0; j < qb && !rc; j++) {
-        const int64_t c0 = (int64_t)cbound[j] * BN;
-        const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
-        const int64_t cw = c1 - c0;
-        F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[1 + j], 0));
-        if (b_rows) {  // stored rows [c0, c1) of B (n x k)
-            k_stats_rows<<<(unsigned)f4j_cdiv(cw, 8), 256, 0, st>>>(dB + c0 * k, cw, k, 0, mxb + c0, esb + c0,
-                                                                    cnb + c0, misc);
-        } else {       // stored columns [c0, c1) of B (k x n)
-            launch_stats_cols(dB + c0, k, cw, n, 0, ctx->sm_count, mxb + c0, esb + c0, cnb + c0, misc, st);
-        }
-        F4J_LAUNCHED(ctx);
-        k_stats_finalize<<<(unsigned)f4j_cdiv(cw, 256), 256, 0, st>>>(cw, 0, mxb + c0, esb + c0, cnb + c0, eb + c0,
-                                                                       misc + 2);
-        F4J_LAUNCHED(ctx);
-        if (j == 0) {  // the plan from A's first rows and B's first columns, then those rows' slices
-            k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
+            const int64_t cw = c1 - c0;
+            F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[1 + j], 0));
+            if (b_rows) {  // stored rows [c0, c1) of B (n x k)
+                k_stats_rows<<<(unsigned)f4j_cdiv(cw, 8), 256, 0, st>>>(dB + c0 * k, cw, k, 0, mxb + c0, esb + c0,
+                                                                        cnb + c0, misc);
+            } else {       // stored columns [c0, c1) of B (k x n)
+                launch_stats_cols(dB + c0, k, cw, n, 0, ctx->sm_count, mxb + c0, esb + c0, cnb + c0, misc, st);
+            }
             F4J_LAUNCHED(ctx);
-            rc = a_part_split(0, a0_rows);
-            if (rc) break;
+            k_stats_finalize<<<(unsigned)f4j_cdiv(cw, 256), 256, 0, st>>>(cw, 0, mxb + c0, esb + c0, cnb + c0, eb + c0,
+                                                                           misc + 2);
+            F4J_LAUNCHED(ctx);
+            if (j == 0) {  // the plan from A's first rows and B's first columns, then those rows' slices
+                k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
+                F4J_LAUNCHED(ctx);
+                rc = a_part_split(0, a0_rows);
+                if (rc) break;
+            }
+            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
+                b_rows ? dB + c0 * k : dB + c0, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, cw, k, Kp, Kp,
+                N, eb + c0, plan, slB + c0 * Kp);
+            F4J_LAUNCHED(ctx);
+            rc = product(j, 0, bound[1], cbound[j], cbound[j + 1]);
         }
-        k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
-            b_rows ? dB + c0 * k : dB + c0, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, cw, k, Kp, Kp,
-            N, eb + c0, plan, slB + c0 * Kp);
-        F4J_LAUNCHED(ctx);
-        rc = product(j, 0, bound[1], cbound[j], cbound[j + 1]);
-    }
-    // the rest of A, each row part multiplied by all of B
-    for (int p = 1; p < parts && !rc; p++) {
-        const int64_t r0 = (int64_t)bound[p] * BM;
-        const int64_t r1 = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
-        rc = a_part_stats(qb + p, r0, r1 - r0);
-        if (!rc) rc = a_part_split(r0, r1 - r0);
-        if (!rc) rc = product(qb + p - 1, bound[p], bound[p + 1], 0, tiles_n);
-    }
+        // the rest of A, each row part multiplied by all of B
+        for (int p = 1; p < parts && !rc; p++) {
+            const int64_t r0 = (int64_t)bound[p] * BM;
+            const int64_t r1 = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
+            rc = a_part_stats(qb + p, r0, r1 - r0);
+            if (!rc) rc = a_part_split(r0, r1 - r0);
+            if (!rc) rc = product(qb + p - 1, bound[p], bound[p + 1], 0, tiles_n);
+        }
+        return rc;
+    };
+    rc = queue();
     int hm[6] = {0, 0, 0, 0, 0, 0};
     if (!rc) {
         k_spec_check<<<1, 32, 0, st>>>(misc, k, k, s_req, plan);
@@ -1645,7 +1652,7 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
         cudaStreamSynchronize(st);
     }
     {
-        cudaError_t e = cudaStreamSynchronize(up);
+        cudaError_t e = cudaStreamSynchronize(ctx->up_stream);
         if (e != cudaSuccess && !rc) rc = f4j_cuda_fail(e, "upload of a host-buffer product");
     }
     for (int i = 0; i < launched; i++) {
