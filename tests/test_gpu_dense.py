@@ -436,6 +436,8 @@ def test_wrap_rejects_misaligned_and_null(f4j):
     (1500, 2000, 300, "split", 0, 0, "pageable"),   # 12 x 16 tiles, ragged last column: A 3, 3, 5, 1; B 4 x 4
     (300, 260, 5000, "split", 0, 1, "registered"),  # 3 x 3 tiles, 79 K blocks (no split K): A 1, 1, 1; B 1, 1, 1
     (130, 200, 4500, "split", 0, 0, "allocated"),   # 2 x 2 tiles, the last row ragged: A 1, 1; B 1, 1
+    (3000, 100, 4200, "split", 0, 0, "registered"),  # 24 x 1 tiles, 66 K blocks: A 6, 6, 9, 3; B in one part
+    (2200, 90, 4300, "split", 0, 1, "pageable"),    # 18 x 1 tiles, B stored n x k: A 4, 4, 8, 2; B in one part
     # uploaded, multiplied and downloaded in turn
     (1000, 700, 900, "split", 0, 0, "registered"),  # 48 tiles, 15 K blocks: split K
     (300, 260, 520, "split", 0, 0, "pageable"),     # 9 tiles: split K
