@@ -1425,7 +1425,8 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 // Waits for everything it queued before returning; *spread_out receives the
 // spread all of A and B give.
 //
-// Part sizes.  A's first part has up to 8 tile rows: its product with one of
+// Part sizes.  A's first part has up to 8 tile rows (all of A in one part
+// when parts == 1): its product with one of
 // F4J_HOST_BPARTS = 4 column parts of B takes about as long as the next column
 // part's upload (both scale with K and the part's width; measured at 8192^3:
 // 0.67 ms of product on 128 SMs per 0.75 ms of upload).  B's column parts go up
@@ -1499,13 +1500,14 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
 
     // A's row parts and B's column parts, in tile rows / columns
     const int tiles_m = L.tiles_m, tiles_n = L.tiles_n;
-    if (parts < 2 || parts > tiles_m || parts > F4J_HOST_PARTS_MAX)
+    if (parts < 1 || parts > tiles_m || parts > F4J_HOST_PARTS_MAX)
         return f4j_fail(F4J_ERR_ARG, "%d row parts of %d tile rows", parts, tiles_m);
     int bound[F4J_HOST_PARTS_MAX + 1];
-    {
+    bound[0] = 0;
+    bound[1] = tiles_m;  // one part: all of A is the first part
+    if (parts >= 2) {
         const int a0 = tiles_m / 4 < 1 ? 1 : (tiles_m / 4 > 8 ? 8 : tiles_m / 4);
         const int last = tiles_m / 8 < 1 ? 1 : tiles_m / 8;
-        bound[0] = 0;
         bound[parts] = tiles_m;
         bound[1] = a0;
         if (parts >= 3) bound[parts - 1] = tiles_m - last;
@@ -1667,9 +1669,10 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
 }
 
 // C = op(A) op(B) from and to host memory (pinned for full copy speed).  A
-// split product with op(A) = N and at least two tile rows runs pipelined
-// (host_split_pipelined): A's first rows up, then B in F4J_HOST_BPARTS column
-// parts, then the rest of A in row parts (F4J_HOST_PARTS in all), each part
+// split product with op(A) = N, no split K and at least two tile rows or two
+// tile columns runs pipelined (host_split_pipelined): A's first rows up (all
+// of A when it has one tile row), then B in F4J_HOST_BPARTS column parts, then
+// the rest of A in row parts (F4J_HOST_PARTS in all), each part
 // sliced and multiplied on its own stream as soon as it arrives and its block
 // of C downloaded behind its product.  In the rare case that all of A and B
 // ask for another slice count than their first parts did (or an operand holds
@@ -1708,9 +1711,12 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     const int want = env_host_parts("F4J_HOST_PARTS", F4J_HOST_PARTS);
     const int parts = tiles_m < want ? tiles_m : want;
     const int bparts = env_host_parts("F4J_HOST_BPARTS", F4J_HOST_BPARTS);
+    const int tiles_n = (int)f4j_cdiv(n, BN);
+    // pipelined when A has two row parts or B two column parts
+    const bool piped = parts >= 2 || (bparts >= 2 && tiles_n >= 2);
     int kchunks = 0;
     split_kcb_cap(tiles_m * f4j_cdiv(n, BN), f4j_cdiv(k, BKB), &kchunks);
-    if (!split || opA != F4J_OP_N || parts < 2 || kchunks) {  // split K runs as one launch
+    if (!split || opA != F4J_OP_N || !piped || kchunks) {  // split K runs as one launch
         if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
         if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
         rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,

@@ -245,9 +245,9 @@ int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
  * downloaded behind it.  The slice count is taken from the first parts of A
  * and B; when all of A and B ask for another count (or an operand holds a
  * NaN / Inf) the product runs again through the f4j_dgemm path.  A
- * product that splits K (fewer than 152 output tiles and K <= 4096) uploads,
- * multiplies and downloads in turn.  The result is bitwise the f4j_dgemm
- * result.  This is
+ * product that splits K (fewer than 152 output tiles and K <= 4096), fits one
+ * 128 x 128 tile of C, or has opA != N uploads, multiplies and downloads in
+ * turn.  The result is bitwise the f4j_dgemm result.  This is
  * the entry a JVM binding calls with its arrays' native copies for Flag4j's
  * Matrix.mult(Matrix) (src/main/java/org/flag4j/arrays/dense/Matrix.java:638-640),
  * same arguments and result. */

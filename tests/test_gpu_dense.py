@@ -430,7 +430,8 @@ def test_wrap_rejects_misaligned_and_null(f4j):
 
 
 @pytest.mark.parametrize("m,n,k,mode,opA,opB,host", [
-    # pipelined: A's first row part, B's column parts, the rest of A (parts in 128-row tile rows / columns)
+    # pipelined: A's first row part, B's column parts, the rest of A (parts in 128-row tile rows / columns);
+    # no split K, and two tile rows or two tile columns
     (2500, 900, 700, "split", 0, 0, "allocated"),   # 20 x 8 tiles, f4j_host_alloc memory: A 5, 5, 8, 2; B 2 x 4
     (2000, 1300, 600, "split", 0, 1, "registered"),  # 16 x 11 tiles, B stored n x k: A 4, 4, 6, 2; B 2, 3, 3, 3
     (1500, 2000, 300, "split", 0, 0, "pageable"),   # 12 x 16 tiles, ragged last column: A 3, 3, 5, 1; B 4 x 4
@@ -438,6 +439,8 @@ def test_wrap_rejects_misaligned_and_null(f4j):
     (130, 200, 4500, "split", 0, 0, "allocated"),   # 2 x 2 tiles, the last row ragged: A 1, 1; B 1, 1
     (3000, 100, 4200, "split", 0, 0, "registered"),  # 24 x 1 tiles, 66 K blocks: A 6, 6, 9, 3; B in one part
     (2200, 90, 4300, "split", 0, 1, "pageable"),    # 18 x 1 tiles, B stored n x k: A 4, 4, 8, 2; B in one part
+    (100, 2000, 4200, "split", 0, 0, "registered"),  # 1 x 16 tiles, 66 K blocks: A in one part; B 4 x 4
+    (128, 1000, 5000, "split", 0, 1, "allocated"),  # 1 x 8 tiles, B stored n x k: A in one part; B 2 x 4
     # uploaded, multiplied and downloaded in turn
     (1000, 700, 900, "split", 0, 0, "registered"),  # 48 tiles, 15 K blocks: split K
     (300, 260, 520, "split", 0, 0, "pageable"),     # 9 tiles: split K
