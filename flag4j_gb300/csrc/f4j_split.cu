@@ -1410,9 +1410,10 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 
 // ------------------------------------------------------------------ host buffers
 // The split product C = A op(B) from host memory with its uploads pipelined
-// (f4j_dgemm_host, op(A) = N).  The uploads go back to back on their own
-// stream: A's first row part, then B in column parts, then the rest of A in
-// row parts.  Each part's statistics and slicing run on the context stream as
+// (f4j_dgemm_host / f4j_zgemm_host, op(A) = N).  The uploads go back to back
+// on their own stream: A's first row part, then B in column parts (complex: B
+// whole, since a column part of B lands in both halves of the [Re | Im]
+// concatenation), then the rest of A in row parts.  Each part's statistics and slicing run on the context stream as
 // soon as it is up; each column part of B is then multiplied by A's first
 // rows, and each later row part of A by all of B.  Every product is one launch
 // on its own stream, its block of C going down behind it.  The slice count
@@ -1438,12 +1439,19 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 // beside a slice GEMM (its CTA fills two of an SM's four register files and
 // all but ~1 KB of its shared memory), so they wait for SMs whenever the
 // products before them hold every SM; these sizes keep that wait short.
-static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, const double* B,
-                                int opB, double* C, double* dA, double* dB, double* dC, int parts, int bparts,
-                                bool* recompute, const SplitPlan** plan_out, float* spread_out) {
+static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A,
+                                const double* B, int opB, double* C, double* dA, double* dB, double* dC, int parts,
+                                int bparts, bool* recompute, const SplitPlan** plan_out, float* spread_out) {
     *recompute = false;
-    const int64_t M = m, N = n;
-    const int64_t Kp = f4j_cdiv(k, BKB) * BKB;  // K padded to whole K blocks
+    // complex: the [Re | Im] concatenation of the ordinary path (2n slice rows
+    // of B, K of 2 Kh), interleaved (re, im) doubles in host and device memory
+    const int64_t M = m, N = cplx ? 2 * n : n;
+    const int64_t Kh = f4j_cdiv(k, BKB) * BKB;  // K of one part, padded to whole K blocks
+    const int64_t Kp = cplx ? 2 * Kh : Kh;
+    const int64_t klen_cat = cplx ? 2 * k : k;
+    const int64_t w2 = cplx ? 2 : 1;  // doubles per element
+    if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX || f4j_cdiv(m > n ? m : n, SP_TR) > 65535)
+        return f4j_fail(F4J_ERR_ARG, "host-buffer split GEMM too large");
     const SmallLayout Lo = small_layout(M, n, N);
     void *ws1, *ws0;
     int rc = f4j_workspace(ctx, ctx->ws_base + 1, Lo.total, &ws1);
@@ -1465,6 +1473,7 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     uint8_t* slA = (uint8_t*)ws0;
     uint8_t* slB = slA + al1k(plane_a * S_MAX);
     const bool b_rows = opB != F4J_OP_N;  // columns of op(B) are stored rows of B (n x k)
+    const int conjb = cplx && opB == F4J_OP_C ? 1 : 0;
     const int s_req = env_slices();
     // the same K-chunk cap the ordinary path plans with (no split K here)
     int kchunks = 0;
@@ -1482,7 +1491,7 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     prm.M = (int)M;
     prm.N = (int)N;
     prm.Kp = (int)Kp;
-    prm.cplx = 0;
+    prm.cplx = cplx ? 1 : 0;
     prm.n_out = (int)n;
     prm.ea = ea;
     prm.eb = eb;
@@ -1519,7 +1528,9 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
             bound[p] = bound[p] < lo ? lo : (bound[p] > hi ? hi : bound[p]);
         }
     }
-    const int qb = bparts < tiles_n ? bparts : tiles_n;
+    // complex: B whole (its column parts would fall on both halves of the
+    // concatenation)
+    const int qb = cplx ? 1 : (bparts < tiles_n ? bparts : tiles_n);
     int cbound[F4J_HOST_PARTS_MAX + 1];
     for (int j = 0; j <= qb; j++) cbound[j] = (int)((int64_t)tiles_n * j / qb);
 
@@ -1530,7 +1541,7 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     auto queue = [&]() -> int {
         F4J_CUDA(cudaMemsetAsync(w, 0, Lo.plan, st));
         SplitPlan* tab = nullptr;
-        rc = plan_table(ctx, Kp, k, kcb_cap, &tab);
+        rc = plan_table(ctx, Kp, klen_cat, kcb_cap, &tab);
         if (rc) return rc;
 
         // Every upload goes up back to back on the upload stream, in the order the
@@ -1542,23 +1553,24 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
         {
             int u = 0;
             const int64_t r1 = (int64_t)bound[1] * BM < m ? (int64_t)bound[1] * BM : m;
-            F4J_CUDA(cudaMemcpyAsync(dA, A, (size_t)r1 * k * 8, cudaMemcpyHostToDevice, up));
+            F4J_CUDA(cudaMemcpyAsync(dA, A, (size_t)r1 * k * 8 * w2, cudaMemcpyHostToDevice, up));
             F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
             for (int j = 0; j < qb; j++) {
                 const int64_t c0 = (int64_t)cbound[j] * BN;
                 const int64_t c1 = (int64_t)cbound[j + 1] * BN < n ? (int64_t)cbound[j + 1] * BN : n;
                 if (b_rows)  // stored rows [c0, c1) of B (n x k)
-                    F4J_CUDA(cudaMemcpyAsync(dB + c0 * k, B + c0 * k, (size_t)(c1 - c0) * k * 8, cudaMemcpyHostToDevice,
-                                             up));
+                    F4J_CUDA(cudaMemcpyAsync(dB + c0 * k * w2, B + c0 * k * w2, (size_t)(c1 - c0) * k * 8 * w2,
+                                             cudaMemcpyHostToDevice, up));
                 else         // stored columns [c0, c1) of B (k x n)
-                    F4J_CUDA(cudaMemcpy2DAsync(dB + c0, (size_t)n * 8, B + c0, (size_t)n * 8, (size_t)(c1 - c0) * 8,
-                                               (size_t)k, cudaMemcpyHostToDevice, up));
+                    F4J_CUDA(cudaMemcpy2DAsync(dB + c0 * w2, (size_t)n * 8 * w2, B + c0 * w2, (size_t)n * 8 * w2,
+                                               (size_t)(c1 - c0) * 8 * w2, (size_t)k, cudaMemcpyHostToDevice, up));
                 F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
             }
             for (int p = 1; p < parts; p++) {
                 const int64_t r0 = (int64_t)bound[p] * BM;
                 const int64_t re = (int64_t)bound[p + 1] * BM < m ? (int64_t)bound[p + 1] * BM : m;
-                F4J_CUDA(cudaMemcpyAsync(dA + r0 * k, A + r0 * k, (size_t)(re - r0) * k * 8, cudaMemcpyHostToDevice, up));
+                F4J_CUDA(cudaMemcpyAsync(dA + r0 * k * w2, A + r0 * k * w2, (size_t)(re - r0) * k * 8 * w2,
+                                         cudaMemcpyHostToDevice, up));
                 F4J_CUDA(cudaEventRecord(ctx->up_ev[u++], up));
             }
         }
@@ -1566,8 +1578,8 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
         // one row part of A (upload u): statistics, exponents (spread into misc[1])
         auto a_part_stats = [&](int u, int64_t r0, int64_t rows) -> int {
             F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[u], 0));
-            k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k, rows, k, 0, mxa + r0, esa + r0,
-                                                                      cna + r0, misc);
+            k_stats_rows<<<(unsigned)f4j_cdiv(rows, 8), 256, 0, st>>>(dA + r0 * k * w2, rows, k, cplx ? 1 : 0,
+                                                                      mxa + r0, esa + r0, cna + r0, misc);
             F4J_LAUNCHED(ctx);
             k_stats_finalize<<<(unsigned)f4j_cdiv(rows, 256), 256, 0, st>>>(rows, 0, mxa + r0, esa + r0, cna + r0,
                                                                              ea + r0, misc + 1);
@@ -1576,8 +1588,8 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
         };
         // its slice planes: target t of the part is row r0 + t
         auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
-            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
-                dA + r0 * k, rows, k, 0, 0, 0, 0, rows, k, Kp, Kp, M, ea + r0, plan, slA + r0 * Kp);
+            k_split<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
+                dA + r0 * k * w2, rows, k, 0, cplx ? 1 : 0, 0, 0, rows, k, Kh, Kp, M, ea + r0, plan, slA + r0 * Kp);
             F4J_LAUNCHED(ctx);
             return F4J_OK;
         };
@@ -1593,8 +1605,9 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
             if (r) return r;
             const int64_t r0 = (int64_t)tm0 * BM, r1 = (int64_t)tm1 * BM < m ? (int64_t)tm1 * BM : m;
             const int64_t c0 = (int64_t)tn0 * BN, c1 = (int64_t)tn1 * BN < n ? (int64_t)tn1 * BN : n;
-            F4J_CUDA(cudaMemcpy2DAsync(C + r0 * n + c0, (size_t)n * 8, dC + r0 * n + c0, (size_t)n * 8,
-                                       (size_t)(c1 - c0) * 8, (size_t)(r1 - r0), cudaMemcpyDeviceToHost, ps));
+            F4J_CUDA(cudaMemcpy2DAsync(C + (r0 * n + c0) * w2, (size_t)n * 8 * w2, dC + (r0 * n + c0) * w2,
+                                       (size_t)n * 8 * w2, (size_t)(c1 - c0) * 8 * w2, (size_t)(r1 - r0),
+                                       cudaMemcpyDeviceToHost, ps));
             F4J_CUDA(cudaEventRecord(ctx->part_ev[id], ps));
             return F4J_OK;
         };
@@ -1608,24 +1621,26 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
             const int64_t cw = c1 - c0;
             F4J_CUDA(cudaStreamWaitEvent(st, ctx->up_ev[1 + j], 0));
             if (b_rows) {  // stored rows [c0, c1) of B (n x k)
-                k_stats_rows<<<(unsigned)f4j_cdiv(cw, 8), 256, 0, st>>>(dB + c0 * k, cw, k, 0, mxb + c0, esb + c0,
-                                                                        cnb + c0, misc);
+                k_stats_rows<<<(unsigned)f4j_cdiv(cw, 8), 256, 0, st>>>(dB + c0 * k * w2, cw, k, cplx ? 1 : 0,
+                                                                        mxb + c0, esb + c0, cnb + c0, misc);
             } else {       // stored columns [c0, c1) of B (k x n)
-                launch_stats_cols(dB + c0, k, cw, n, 0, ctx->sm_count, mxb + c0, esb + c0, cnb + c0, misc, st);
+                launch_stats_cols(dB + c0 * w2, k, cw, n, cplx ? 1 : 0, ctx->sm_count, mxb + c0, esb + c0, cnb + c0,
+                                  misc, st);
             }
             F4J_LAUNCHED(ctx);
-            k_stats_finalize<<<(unsigned)f4j_cdiv(cw, 256), 256, 0, st>>>(cw, 0, mxb + c0, esb + c0, cnb + c0, eb + c0,
-                                                                           misc + 2);
+            // complex (B whole): each target's exponent also for its row in B_cat^T's second half
+            k_stats_finalize<<<(unsigned)f4j_cdiv(cw, 256), 256, 0, st>>>(cw, cplx ? 1 : 0, mxb + c0, esb + c0,
+                                                                           cnb + c0, eb + c0, misc + 2);
             F4J_LAUNCHED(ctx);
             if (j == 0) {  // the plan from A's first rows and B's first columns, then those rows' slices
-                k_plan_pick<<<1, 128, 0, st>>>(misc, k, k, s_req, tab, plan);
+                k_plan_pick<<<1, 128, 0, st>>>(misc, k, klen_cat, s_req, tab, plan);
                 F4J_LAUNCHED(ctx);
                 rc = a_part_split(0, a0_rows);
                 if (rc) break;
             }
-            k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
-                b_rows ? dB + c0 * k : dB + c0, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, 0, 0, 1, cw, k, Kp, Kp,
-                N, eb + c0, plan, slB + c0 * Kp);
+            k_split<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
+                b_rows ? dB + c0 * k * w2 : dB + c0 * w2, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1,
+                cplx ? 1 : 0, conjb, 1, cw, k, Kh, Kp, N, eb + c0, plan, slB + c0 * Kp);
             F4J_LAUNCHED(ctx);
             rc = product(j, 0, bound[1], cbound[j], cbound[j + 1]);
         }
@@ -1642,7 +1657,7 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
     rc = queue();
     int hm[6] = {0, 0, 0, 0, 0, 0};
     if (!rc) {
-        k_spec_check<<<1, 32, 0, st>>>(misc, k, k, s_req, plan);
+        k_spec_check<<<1, 32, 0, st>>>(misc, k, klen_cat, s_req, plan);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) {
             ctx->launches++;
@@ -1669,19 +1684,21 @@ static int host_split_pipelined(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, c
 }
 
 // C = op(A) op(B) from and to host memory (pinned for full copy speed).  A
-// split product with op(A) = N, no split K and at least two tile rows or two
-// tile columns runs pipelined (host_split_pipelined): A's first rows up (all
-// of A when it has one tile row), then B in F4J_HOST_BPARTS column parts, then
-// the rest of A in row parts (F4J_HOST_PARTS in all), each part
-// sliced and multiplied on its own stream as soon as it arrives and its block
-// of C downloaded behind its product.  In the rare case that all of A and B
-// ask for another slice count than their first parts did (or an operand holds
-// a NaN / Inf), the product runs again through the ordinary path on the
-// operands already on the device.  Either way C equals f4j_dgemm's bit for
-// bit.  Other products upload, multiply and download in turn.  Returns when C
-// is in host memory.
-extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
-                              const double* B, int opB, double* C, int mode, f4j_report* rep) {
+// split product with op(A) = N, n > 1, no split K and at least two tile rows
+// (or, real, two tile columns) runs pipelined (host_split_pipelined): A's
+// first rows up (all of A when it has one tile row), then B (real: in
+// F4J_HOST_BPARTS column parts; complex: whole), then the rest of A in row
+// parts (F4J_HOST_PARTS in all), each part sliced and multiplied on its own
+// stream as soon as it arrives and its block of C downloaded behind its
+// product.  In the rare case that all of A and B ask for another slice count
+// than their first parts did (or an operand holds a NaN / Inf), the product
+// runs again through the ordinary path on the operands already on the device.
+// Either way C equals f4j_dgemm's (f4j_zgemm's) bit for bit.  Other products
+// upload, multiply and download in turn.  Returns when C is in host memory.
+// f4j_dgemm_host (cplx false) and f4j_zgemm_host (cplx true): the same
+// pipeline for both; complex operands and C are interleaved (re, im) doubles.
+static int gemm_host(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                     const double* B, int opB, double* C, int mode, f4j_report* rep) {
     F4J_LOCK(ctx);
     F4J_CHECK_CTX(ctx);
     if (!A || !B || !C) return f4j_fail(F4J_ERR_ARG, "null host pointer");
@@ -1698,33 +1715,36 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
         rep->max_abs_err = rep->max_rel_err = rep->plain_max_abs_err = rep->plain_max_rel_err = -1.0;
     }
     if (m == 0 || n == 0) return F4J_OK;
-    if (opA == F4J_OP_C) opA = F4J_OP_T;  // real data
-    if (opB == F4J_OP_C) opB = F4J_OP_T;
-    const size_t ab = (size_t)m * k * 8, bb = (size_t)k * n * 8, cb = (size_t)m * n * 8;
+    if (!cplx && opA == F4J_OP_C) opA = F4J_OP_T;  // conjugation is the identity for real data
+    if (!cplx && opB == F4J_OP_C) opB = F4J_OP_T;
+    const size_t es = cplx ? 16 : 8;  // bytes per element
+    const size_t ab = (size_t)m * k * es, bb = (size_t)k * n * es, cb = (size_t)m * n * es;
     void *dA, *dB, *dC;
     int rc = f4j_workspace(ctx, 3, ab, &dA);
     if (!rc) rc = f4j_workspace(ctx, 6, bb, &dB);
     if (!rc) rc = f4j_workspace(ctx, 7, cb, &dC);
     if (rc) return rc;
-    const bool split = k > 0 && f4j_resolve_mode(false, m, n, k, mode) == F4J_MODE_SPLIT;
+    // n == 1 runs the device path's matrix-vector kernel
+    const bool split = k > 0 && n > 1 && f4j_resolve_mode(cplx, m, n, k, mode) == F4J_MODE_SPLIT;
     const int tiles_m = (int)f4j_cdiv(m, BM);
     const int want = env_host_parts("F4J_HOST_PARTS", F4J_HOST_PARTS);
     const int parts = tiles_m < want ? tiles_m : want;
     const int bparts = env_host_parts("F4J_HOST_BPARTS", F4J_HOST_BPARTS);
-    const int tiles_n = (int)f4j_cdiv(n, BN);
-    // pipelined when A has two row parts or B two column parts
-    const bool piped = parts >= 2 || (bparts >= 2 && tiles_n >= 2);
+    const int64_t ncat = cplx ? 2 * n : n;  // slice rows of B (the [Re | Im] concatenation when complex)
+    const int tiles_n = (int)f4j_cdiv(ncat, BN);
+    // pipelined when A has two row parts or B two column parts (real only)
+    const bool piped = parts >= 2 || (!cplx && bparts >= 2 && tiles_n >= 2);
     int kchunks = 0;
-    split_kcb_cap(tiles_m * f4j_cdiv(n, BN), f4j_cdiv(k, BKB), &kchunks);
+    split_kcb_cap(tiles_m * (int64_t)tiles_n, (cplx ? 2 : 1) * f4j_cdiv(k, BKB), &kchunks);
     if (!split || opA != F4J_OP_N || !piped || kchunks) {  // split K runs as one launch
         if (ab) F4J_CUDA(cudaMemcpyAsync(dA, A, ab, cudaMemcpyHostToDevice, ctx->stream));
         if (bb) F4J_CUDA(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, ctx->stream));
-        rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,
+        rc = f4j_gemm_impl(ctx, cplx, m, n, k, (const double*)dA, opA, (const double*)dB, opB, (double*)dC, mode,
                            rep);
         if (rc) return rc;
         F4J_CUDA(cudaMemcpyAsync(C, dC, cb, cudaMemcpyDeviceToHost, ctx->stream));
         F4J_CUDA(cudaStreamSynchronize(ctx->stream));
-        return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, opA, (const double*)dB, opB,
+        return f4j_report_accuracy(ctx, cplx, m, n, k, (const double*)dA, opA, (const double*)dB, opB,
                                    (const double*)dC, check_samples, check_flags, rep);
     }
     if (!ctx->parts_init) {
@@ -1742,28 +1762,38 @@ extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, con
     bool recompute = false;
     const SplitPlan* plan = nullptr;
     float spread = 0.0f;
-    rc = host_split_pipelined(ctx, m, n, k, A, B, opB, C, (double*)dA, (double*)dB, (double*)dC, parts, bparts,
+    rc = host_split_pipelined(ctx, cplx, m, n, k, A, B, opB, C, (double*)dA, (double*)dB, (double*)dC, parts, bparts,
                               &recompute, &plan, &spread);
     if (rc) return rc;
     if (recompute) {
-        // all of A asks for another slice count than its first rows did, or an
-        // operand holds a NaN / Inf: the product again through the ordinary
-        // path on the operands now on the device, and all of C down
-        rc = f4j_gemm_impl(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB, (double*)dC,
+        // all of A and B ask for another slice count than their first parts
+        // did, or an operand holds a NaN / Inf: the product again through the
+        // ordinary path on the operands now on the device, and all of C down
+        rc = f4j_gemm_impl(ctx, cplx, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB, (double*)dC,
                            mode, rep);
         if (rc) return rc;
         F4J_CUDA(cudaMemcpyAsync(C, dC, cb, cudaMemcpyDeviceToHost, ctx->stream));
         F4J_CUDA(cudaStreamSynchronize(ctx->stream));
     } else if (rep) {
-        rep->flops = 2.0 * (double)m * (double)n * (double)k;
+        rep->flops = (cplx ? 8.0 : 2.0) * (double)m * (double)n * (double)k;
         rep->mode_used = F4J_MODE_SPLIT;
         rc = split_report(ctx, plan, rep);
         if (rc) return rc;
         rep->exp_spread = spread;
     }
     if (rep) rep->launches = (int32_t)(ctx->launches - l0);
-    return f4j_report_accuracy(ctx, false, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB,
+    return f4j_report_accuracy(ctx, cplx, m, n, k, (const double*)dA, F4J_OP_N, (const double*)dB, opB,
                                (const double*)dC, check_samples, check_flags, rep);
+}
+
+extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                              const double* B, int opB, double* C, int mode, f4j_report* rep) {
+    return gemm_host(ctx, false, m, n, k, A, opA, B, opB, C, mode, rep);
+}
+
+extern "C" int f4j_zgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
+                              const double* B, int opB, double* C, int mode, f4j_report* rep) {
+    return gemm_host(ctx, true, m, n, k, A, opA, B, opB, C, mode, rep);
 }
 
 // ------------------------------------------------------------------ no-allocation variant

@@ -253,6 +253,21 @@ int f4j_dgemm(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, f4j_buf A, int opA,
  * same arguments and result. */
 int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
                    int opB, double* C, int mode, f4j_report* report);
+/* f4j_zgemm from and to host memory: A, B, C are interleaved (re, im) complex
+ * host arrays (Flag4j's Complex128[] marshalled to double[2n]), opA, opB in
+ * {N, T, C}; same contract as f4j_dgemm_host.  A split product with opA = N
+ * is pipelined with B uploaded whole (its column parts would fall on both
+ * halves of the [Re | Im] concatenation) and A in row parts; the result is
+ * bitwise the f4j_zgemm result.  This is the entry a JVM binding calls with
+ * the marshalled arrays for CMatrix.mult(CMatrix)
+ * (src/main/java/org/flag4j/arrays/dense/CMatrix.java:463-465) and, with
+ * opB = F4J_OP_T, CMatrix.multTranspose (this.mult(b.T()),
+ * src/main/java/org/flag4j/arrays/backend/semiring_arrays/
+ * AbstractDenseSemiringMatrix.java:330-334); non-square results are returned
+ * correctly where the reference's kernels mis-size them
+ * (Cm128DeMatMultKernels.java:46-77). */
+int f4j_zgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
+                   int opB, double* C, int mode, f4j_report* report);
 
 /* Complex128 C = op(A) * op(B), interleaved (re, im); op may be N, T or C.
  * Replaces CMatrix.mult -> Cm128DeMatMultDispatcher.dispatch

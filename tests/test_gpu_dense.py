@@ -445,6 +445,7 @@ def test_wrap_rejects_misaligned_and_null(f4j):
     (1000, 700, 900, "split", 0, 0, "registered"),  # 48 tiles, 15 K blocks: split K
     (300, 260, 520, "split", 0, 0, "pageable"),     # 9 tiles: split K
     (100, 90, 80, "split", 0, 0, "allocated"),      # one tile row
+    (3000, 1, 4200, "split", 0, 0, "registered"),   # n = 1: the matrix-vector kernel, as f4j_dgemm
     (600, 500, 400, "split", 1, 0, "registered"),   # op(A) = T
     (500, 300, 200, "plain", 0, 0, "registered"),
     (64, 48, 40, "exact", 0, 1, "allocated"),
@@ -477,11 +478,65 @@ def test_host_buffer_gemm_matches_device_gemm(f4j, m, n, k, mode, opA, opB, host
         check(ctx.lib.f4j_dgemm_host(ctx.handle, m, n, k, A.ctypes.data, opA, B.ctypes.data, opB, C.ctypes.data,
                                      _lib.MODES[mode], ctypes.byref(rep)))
         assert np.array_equal(C, ref)
-        if mode == "split":
-            assert rep.slices > 0 and rep.mode_used == _lib.MODE_SPLIT
-            assert rep.slices == rd.slices and rep.exp_spread == rd.exp_spread
+        assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
+        if rd.mode_used == _lib.MODE_SPLIT:
+            assert rep.slices > 0 and rep.exp_spread == rd.exp_spread
+        assert (rep.mode_used == _lib.MODE_SPLIT) == (mode == "split" and n > 1)
     finally:
         if pinned:
+            for a in arrays:
+                check(ctx.lib.f4j_host_unregister(a.ctypes.data))
+
+
+@pytest.mark.parametrize("m,n,k,opA,opB,host,poison", [
+    # pipelined (B whole, A in row parts; tiles over the 2n-column [Re | Im] concatenation)
+    (1000, 600, 5000, 0, 0, "registered", False),  # 8 x 10 tiles, 158 K blocks: A 2, 2, 3, 1
+    (2000, 700, 600, 0, 2, "allocated", False),    # 16 x 11 tiles, B stored n x k and conjugated: A 4, 4, 6, 2
+    (1000, 600, 5000, 0, 0, "pageable", True),     # a NaN in A's last part: the device path again
+    # uploaded, multiplied and downloaded in turn
+    (1500, 300, 1000, 0, 1, "pageable", False),    # 60 tiles, 32 K blocks: split K
+    (700, 500, 400, 2, 0, "registered", False),    # op(A) = A^H
+    (900, 1, 3000, 0, 0, "allocated", False),      # n = 1: the matrix-vector kernel
+])
+def test_host_buffer_zgemm_matches_device_zgemm(f4j, m, n, k, opA, opB, host, poison):
+    """f4j_zgemm_host is bitwise f4j_zgemm on the same interleaved complex operands
+    (CMatrix.mult / multTranspose from marshalled host arrays), NaN bits included,
+    with the same mode, slice count and spread in the report."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check, pinned_empty
+    ctx = f4j.default_context()
+    A = (synth.scaled(m, k, 4, 61, "row", cplx=True) if opA == 0 else
+         synth.scaled(k, m, 4, 61, "col", cplx=True))
+    B = synth.scaled(k, n, 4, 62, "col", cplx=True) if opB == 0 else synth.scaled(n, k, 4, 62, "row", cplx=True)
+    if poison:
+        A[m - 5, 7] = complex(np.nan, 1.0)
+    dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(16 * m * n)
+    rd = _lib.f4j_report()
+    check(ctx.lib.f4j_zgemm(ctx.handle, m, n, k, dA.handle, opA, dB.handle, opB, dC.handle, _lib.MODE_SPLIT,
+                            ctypes.byref(rd)))
+    ref = dC.to_numpy(np.complex128, m * n).reshape(m, n)
+    C = np.zeros((m, n), np.complex128)
+    if host == "allocated":
+        pa, pb, pc = pinned_empty(A.shape, np.complex128), pinned_empty(B.shape, np.complex128), \
+            pinned_empty(C.shape, np.complex128)
+        pa[...], pb[...], pc[...] = A, B, C
+        A, B, C = pa, pb, pc
+    arrays = (A, B, C)
+    if host == "registered":
+        for a in arrays:
+            check(ctx.lib.f4j_host_register(a.ctypes.data, a.nbytes))
+    try:
+        rep = _lib.f4j_report()
+        check(ctx.lib.f4j_zgemm_host(ctx.handle, m, n, k, A.ctypes.data, opA, B.ctypes.data, opB, C.ctypes.data,
+                                     _lib.MODE_SPLIT, ctypes.byref(rep)))
+        assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
+        assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
+        if rd.mode_used == _lib.MODE_SPLIT:
+            assert rep.exp_spread == rd.exp_spread
+        if poison:
+            assert rep.mode_used == _lib.MODE_PLAIN and np.isnan(C[m - 5]).all()
+    finally:
+        if host == "registered":
             for a in arrays:
                 check(ctx.lib.f4j_host_unregister(a.ctypes.data))
 
