@@ -1409,6 +1409,30 @@ int f4j_gemm_split(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, con
 }
 
 // ------------------------------------------------------------------ host buffers
+// Row parts of A for a pipelined host-buffer product, in tile rows: part p
+// is [bound[p], bound[p + 1]), 1 <= parts <= min(tiles_m, F4J_HOST_PARTS_MAX).
+// One part is all of A.  Otherwise the first part has up to 8 tile rows (a
+// quarter of A when that is less), the second as many, the last 1/8 of the
+// tile rows and the rest is cut into equal middle parts; every part keeps at
+// least one tile row.
+static void host_part_bounds(int tiles_m, int parts, int* bound) {
+    bound[0] = 0;
+    bound[1] = tiles_m;
+    if (parts < 2) return;
+    const int a0 = tiles_m / 4 < 1 ? 1 : (tiles_m / 4 > 8 ? 8 : tiles_m / 4);
+    const int last = tiles_m / 8 < 1 ? 1 : tiles_m / 8;
+    bound[parts] = tiles_m;
+    bound[1] = a0;
+    if (parts >= 3) bound[parts - 1] = tiles_m - last;
+    if (parts >= 4) bound[2] = 2 * a0;
+    for (int p = 3; p < parts - 1; p++)
+        bound[p] = bound[2] + (int)((int64_t)(bound[parts - 1] - bound[2]) * (p - 2) / (parts - 3));
+    for (int p = 1; p < parts; p++) {  // keep every part non-empty
+        const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);
+        bound[p] = bound[p] < lo ? lo : (bound[p] > hi ? hi : bound[p]);
+    }
+}
+
 // The split product C = A op(B) from host memory with its uploads pipelined
 // (f4j_dgemm_host / f4j_zgemm_host, op(A) = N).  The uploads go back to back
 // on their own stream: A's first row part, then B in column parts (complex: B
@@ -1512,22 +1536,7 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
     if (parts < 1 || parts > tiles_m || parts > F4J_HOST_PARTS_MAX)
         return f4j_fail(F4J_ERR_ARG, "%d row parts of %d tile rows", parts, tiles_m);
     int bound[F4J_HOST_PARTS_MAX + 1];
-    bound[0] = 0;
-    bound[1] = tiles_m;  // one part: all of A is the first part
-    if (parts >= 2) {
-        const int a0 = tiles_m / 4 < 1 ? 1 : (tiles_m / 4 > 8 ? 8 : tiles_m / 4);
-        const int last = tiles_m / 8 < 1 ? 1 : tiles_m / 8;
-        bound[parts] = tiles_m;
-        bound[1] = a0;
-        if (parts >= 3) bound[parts - 1] = tiles_m - last;
-        if (parts >= 4) bound[2] = 2 * a0;
-        for (int p = 3; p < parts - 1; p++)
-            bound[p] = bound[2] + (int)((int64_t)(bound[parts - 1] - bound[2]) * (p - 2) / (parts - 3));
-        for (int p = 1; p < parts; p++) {  // keep every part non-empty
-            const int lo = bound[p - 1] + 1, hi = tiles_m - (parts - p);
-            bound[p] = bound[p] < lo ? lo : (bound[p] > hi ? hi : bound[p]);
-        }
-    }
+    host_part_bounds(tiles_m, parts, bound);
     // complex: B whole (its column parts would fall on both halves of the
     // concatenation)
     const int qb = cplx ? 1 : (bparts < tiles_n ? bparts : tiles_n);

@@ -8,8 +8,9 @@
 // that continuation chains between groups are well formed, and that within a
 // band every TMEM buffer is acquired once before its first MMA and released
 // once after its last, and that the split-K chunk cap for products with few
-// output tiles yields the chunk count the host expects.  Exit status 0 on
-// success.  Launches no kernel.
+// output tiles yields the chunk count the host expects, and that the row
+// parts of a pipelined host-buffer product tile A in order, none empty.  Exit
+// status 0 on success.  Launches no kernel.
 #include "../../flag4j_gb300/csrc/f4j_split.cu"
 #include <cstdio>
 #include <set>
@@ -105,6 +106,20 @@ int main() {
     for (int g = 0; g < P.ngroups; g++) { ops += P.groups[g].nop; tiles += P.groups[g].nload; }
     printf("s=%d: %d groups, %d MMA instructions for %d products, %d tiles per K block; kcb %d of %d\n", s, P.ngroups, ops, s*(s+1)/2, tiles, P.kcb, P.nkb);
   }
+  // row parts of a pipelined host-buffer product: every tile-row count and
+  // part count gives parts that tile [0, tiles_m) in order, none empty; the
+  // first part has min(8, max(1, tiles_m / 4)) tile rows where that leaves a
+  // row for each later part
+  for (int tm = 1; tm <= 300; tm++)
+    for (int parts = 1; parts <= F4J_HOST_PARTS_MAX && parts <= tm; parts++) {
+      int b[F4J_HOST_PARTS_MAX + 1];
+      host_part_bounds(tm, parts, b);
+      if (b[0] != 0 || b[parts] != tm) { printf("parts %d of %d: ends %d, %d\n", parts, tm, b[0], b[parts]); bad++; }
+      for (int p = 0; p < parts; p++)
+        if (b[p + 1] <= b[p]) { printf("parts %d of %d: part %d empty\n", parts, tm, p); bad++; }
+      const int a0 = tm / 4 < 1 ? 1 : (tm / 4 > 8 ? 8 : tm / 4);
+      if (parts >= 2 && a0 <= tm - (parts - 1) && b[1] != a0) { printf("parts %d of %d: first %d\n", parts, tm, b[1]); bad++; }
+    }
   printf("plan check: %s (%d problems)\n", bad ? "FAIL" : "ok", bad);
   return bad != 0;
 }
