@@ -338,6 +338,16 @@ def dense_cpu_baselines(nz, ma, ka, seconds=1.5):
                         "sample": "row samples of A B (%d rows), W B^T (%d rows), A^T W (%d rows), scaled" % (rf, ra, rb)}}
 
 
+def headline_config(n, ws):
+    """The headline workload's config, the same dict on both arms."""
+    return {"workload": "FP64-accurate GEMM %d^3 (split path), A u*2^e per row, B per column, "
+                        "u~U[-1,1), e~U[-8,8]" % n,
+            "l2": ("inputs larger than L2 (A, B %d MiB each), no flush" % (8 * n * n >> 20)
+                   if 8 * n * n > (129 << 20) else
+                   "A, B %d MiB each: L2-resident across steps" % (8 * n * n >> 20)),
+            "parallelism": "replicas" if ws > 1 else "1 GPU"}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -372,12 +382,12 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
             "impl": "reference",
-            "config": {"workload": "FP64 GEMM %d^3, u*2^e, e~U[-8,8] per row/col" % n, "cpu": "host cores"},
+            "config": headline_config(n, ws),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "notes": "Flag4j is pure Java and neither machine has a JVM; the reference arm is the C "
-                     "restatement of its GEMM loop (bit-identical to the Java kernel on the golden vectors), "
-                     "timed on a row sample of the workload each step."}
+                     "restatement of its GEMM loop (bit-identical to the Java kernel on the golden vectors) on "
+                     "all host cores, timed on a row sample of the workload each step."}
     print(json.dumps(line))
 
 
@@ -817,12 +827,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (FP8 E4M3 slices, exact FP32/int64 accumulation)",
             "data": "synthetic (seeded PCG64)",
-            "config": {"workload": "FP64-accurate GEMM %d^3 (split path), A u*2^e per row, B per column, "
-                                   "u~U[-1,1), e~U[-8,8]" % n,
-                       "l2": ("inputs larger than L2 (A, B %d MiB each), no flush" % (8 * n * n >> 20)
-                              if 8 * n * n > (129 << 20) else
-                              "A, B %d MiB each: L2-resident across steps" % (8 * n * n >> 20)),
-                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "config": headline_config(n, ws),
             "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": ws * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": Ah.nbytes + Bh.nbytes, "d2h_bytes_per_step": Ch.nbytes,

@@ -65,3 +65,7 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank0():
     assert d["impl"] == "reference" and d["n_gpus"] == 2
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["value"] > 0
+    # the same config as the GPU arm's line at the same size and rank count
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.headline_config(2048, 2)
