@@ -555,13 +555,15 @@ constexpr int SP_TR = 32, SP_TQ = 64;  // tile: 32 target rows x 64 k-indices
 //   role 0 (A_cat): complex value (re, im) -> out[r][q] = re, out[r][Kh+q] = im
 //   role 1 (B_cat^T): -> out[r][q] = re, out[r][Kh+q] = -im,
 //                        out[n+r][q] = im, out[n+r][Kh+q] = re
+// CPLX is the operand's kind (the imaginary parts' staging exists only then).
+template <bool CPLX>
 __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t srows, int64_t scols,
-                                           int transposed, int cplx, int conj, int role, int64_t targets,
+                                           int transposed, int conj, int role, int64_t targets,
                                            int64_t klen, int64_t Kh, int64_t Kp, int64_t rows_out,
                                            const int* __restrict__ e_t, const SplitPlan* __restrict__ plan,
                                            uint8_t* __restrict__ out, int64_t bx, int64_t by) {
     __shared__ double sre[SP_TR][SP_TQ + 1];
-    __shared__ double sim[SP_TR][SP_TQ + 1];
+    __shared__ double sim[CPLX ? SP_TR : 1][SP_TQ + 1];
     if (plan->nonfinite) return;
     const int s = plan->s;
     const int64_t r0 = by * SP_TR, q0 = bx * SP_TQ;
@@ -574,7 +576,7 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
         double re = 0, im = 0;
         if (r < targets && q < klen) {
             int64_t idx = transposed ? (q * scols + r) : (r * scols + q);
-            if (cplx) {
+            if constexpr (CPLX) {
                 re = X[2 * idx];
                 im = X[2 * idx + 1];
                 if (conj) im = -im;
@@ -583,7 +585,7 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
             }
         }
         sre[rr][qq] = re;
-        sim[rr][qq] = im;
+        if constexpr (CPLX) sim[rr][qq] = im;
     }
     __syncthreads();
     // ---- each thread: one target row, 8 consecutive q
@@ -592,7 +594,7 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
     if (r >= targets) return;
     const int e = e_t[r];
     const int F = 4 + 5 * (s - 1);
-    const int nparts = cplx ? (role == 0 ? 2 : 4) : 1;
+    const int nparts = CPLX ? (role == 0 ? 2 : 4) : 1;
     for (int part = 0; part < nparts; part++) {
         // part: 0 -> (row r, col q) ; 1 -> (row r, col Kh+q) ; 2 -> (row n+r, col q) ; 3 -> (row n+r, col Kh+q)
         // Y = H * 2^30 + L with 0 <= L < 2^30: the low six digits come from L,
@@ -601,7 +603,9 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             double v;
-            double a = sre[rr][qs + j], b = sim[rr][qs + j];
+            const double a = sre[rr][qs + j];
+            double b = 0.0;
+            if constexpr (CPLX) b = sim[rr][qs + j];
             if (role == 0) v = (part == 0) ? a : b;
             else v = (part == 0) ? a : (part == 1) ? -b : (part == 2) ? b : a;
             const long long y = fixed_of(v, e, F);
@@ -643,13 +647,18 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
     }
 }
 
-__global__ void __launch_bounds__(256) k_split(const double* __restrict__ X, int64_t srows, int64_t scols,
-                                               int transposed, int cplx, int conj, int role,
-                                               int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
-                                               int64_t rows_out, const int* __restrict__ e_t,
-                                               const SplitPlan* __restrict__ plan, uint8_t* __restrict__ out) {
-    split_body(X, srows, scols, transposed, cplx, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
-               blockIdx.x, blockIdx.y);
+// Real operands: 17 KB of staging and at most 32 registers, so 8 blocks (64
+// warps) fit an SM and hide the staging loads; complex: 34 KB and 60
+// registers (tighter caps spill), 4 blocks.
+template <bool CPLX>
+__global__ void __launch_bounds__(256, CPLX ? 4 : 8) k_split(const double* __restrict__ X, int64_t srows,
+                                                             int64_t scols, int transposed, int conj, int role,
+                                                             int64_t targets, int64_t klen, int64_t Kh, int64_t Kp,
+                                                             int64_t rows_out, const int* __restrict__ e_t,
+                                                             const SplitPlan* __restrict__ plan,
+                                                             uint8_t* __restrict__ out) {
+    split_body<CPLX>(X, srows, scols, transposed, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
+                     blockIdx.x, blockIdx.y);
 }
 
 // One operand of k_split_pair (the arguments k_split takes for it).
@@ -664,19 +673,21 @@ struct SplitOperand {
 
 // Both operands' slice planes in one launch: blockIdx.z = 0 slices op(A), 1
 // op(B)_cat^T; blocks past an operand's targets return at once.
-__global__ void __launch_bounds__(256) k_split_pair(const SplitOperand a, const SplitOperand b, int cplx, int64_t klen,
-                                                    int64_t Kh, int64_t Kp, const SplitPlan* __restrict__ plan) {
+template <bool CPLX>
+__global__ void __launch_bounds__(256, CPLX ? 6 : 8) k_split_pair(const SplitOperand a, const SplitOperand b,
+                                                                  int64_t klen, int64_t Kh, int64_t Kp,
+                                                                  const SplitPlan* __restrict__ plan) {
     // one inlined copy of the body per operand, each reading its own kernel
     // parameters directly (selecting the operand first kept every field in
     // registers: 60 registers against 35, and fewer blocks per SM)
     if (blockIdx.z == 0) {
         if ((int64_t)blockIdx.y * SP_TR >= a.targets) return;
-        split_body(a.X, a.srows, a.scols, a.transposed, cplx, a.conj, a.role, a.targets, klen, Kh, Kp, a.rows_out,
-                   a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
+        split_body<CPLX>(a.X, a.srows, a.scols, a.transposed, a.conj, a.role, a.targets, klen, Kh, Kp, a.rows_out,
+                         a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
     } else {
         if ((int64_t)blockIdx.y * SP_TR >= b.targets) return;
-        split_body(b.X, b.srows, b.scols, b.transposed, cplx, b.conj, b.role, b.targets, klen, Kh, Kp, b.rows_out,
-                   b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
+        split_body<CPLX>(b.X, b.srows, b.scols, b.transposed, b.conj, b.role, b.targets, klen, Kh, Kp, b.rows_out,
+                         b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
     }
 }
 
@@ -1303,8 +1314,8 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
                               eb, slB};
         const int64_t gy = f4j_cdiv(M > n ? M : n, SP_TR);
         if (gy > 65535) return f4j_fail(F4J_ERR_ARG, "split GEMM: %lld rows exceed the slicing grid", (long long)(M > n ? M : n));
-        k_split_pair<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)gy, 2), 256, 0, ctx->stream>>>(sa, sb, cplx, k, Kh, Kp,
-                                                                                          plan);
+        auto pair = cplx ? k_split_pair<true> : k_split_pair<false>;
+        pair<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)gy, 2), 256, 0, ctx->stream>>>(sa, sb, k, Kh, Kp, plan);
         F4J_LAUNCHED(ctx);
     }
     f4j_prof_end(ctx);
@@ -1498,6 +1509,7 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
     uint8_t* slB = slA + al1k(plane_a * S_MAX);
     const bool b_rows = opB != F4J_OP_N;  // columns of op(B) are stored rows of B (n x k)
     const int conjb = cplx && opB == F4J_OP_C ? 1 : 0;
+    const auto split_k = cplx ? k_split<true> : k_split<false>;
     const int s_req = env_slices();
     // the same K-chunk cap the ordinary path plans with (no split K here)
     int kchunks = 0;
@@ -1597,8 +1609,8 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
         };
         // its slice planes: target t of the part is row r0 + t
         auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
-            k_split<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
-                dA + r0 * k * w2, rows, k, 0, cplx ? 1 : 0, 0, 0, rows, k, Kh, Kp, M, ea + r0, plan, slA + r0 * Kp);
+            split_k<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
+                dA + r0 * k * w2, rows, k, 0, 0, 0, rows, k, Kh, Kp, M, ea + r0, plan, slA + r0 * Kp);
             F4J_LAUNCHED(ctx);
             return F4J_OK;
         };
@@ -1647,9 +1659,9 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
                 rc = a_part_split(0, a0_rows);
                 if (rc) break;
             }
-            k_split<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
-                b_rows ? dB + c0 * k * w2 : dB + c0 * w2, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1,
-                cplx ? 1 : 0, conjb, 1, cw, k, Kh, Kp, N, eb + c0, plan, slB + c0 * Kp);
+            split_k<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
+                b_rows ? dB + c0 * k * w2 : dB + c0 * w2, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, conjb, 1,
+                cw, k, Kh, Kp, N, eb + c0, plan, slB + c0 * Kp);
             F4J_LAUNCHED(ctx);
             rc = product(j, 0, bound[1], cbound[j], cbound[j + 1]);
         }
@@ -1918,10 +1930,10 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     // and return at once for a NaN/Inf operand or a plan that does not fit.
     uint8_t* slA = (uint8_t*)(w + off_sl);
     uint8_t* slB = slA + al1k((size_t)M * Kp * S_MAX);
-    k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
-        A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, 0, M, k, Kp, Kp, M, ea, plan, slA);
-    k_split<<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(N, SP_TR)), 256, 0, st>>>(
-        B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 0, 1, N, k, Kp, Kp, N, eb, plan, slB);
+    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
+        A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, M, k, Kp, Kp, M, ea, plan, slA);
+    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(N, SP_TR)), 256, 0, st>>>(
+        B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 1, N, k, Kp, Kp, N, eb, plan, slB);
     F4J_CUDA(cudaGetLastError());
     CUtensorMap ta{}, tb{};
     rc = make_slice_map(&ta, slA, Kp, M, S_MAX);
