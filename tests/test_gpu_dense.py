@@ -541,6 +541,39 @@ def test_host_buffer_zgemm_matches_device_zgemm(f4j, m, n, k, opA, opB, host, po
                 check(ctx.lib.f4j_host_unregister(a.ctypes.data))
 
 
+@pytest.mark.parametrize("seed", range(16))
+def test_host_buffer_gemm_random_shapes_and_parts(f4j, seed, monkeypatch):
+    """Seeded random shapes, operand kinds, op(B) and part counts
+    (F4J_HOST_PARTS, F4J_HOST_BPARTS): the host-buffer product is bitwise the
+    device product, whichever path (pipelined or in turn) the shape takes."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    g = np.random.default_rng(1000 + seed)
+    cplx = bool(g.integers(0, 2))
+    m, n = int(g.integers(1, 2600)), int(g.integers(1, 1800))
+    k = int(g.choice([int(g.integers(1, 700)), int(g.integers(4100, 5200))]))  # with and without split K
+    opB = int(g.integers(0, 3 if cplx else 2))
+    monkeypatch.setenv("F4J_HOST_PARTS", str(int(g.choice([1, 2, 3, 4, 8]))))
+    monkeypatch.setenv("F4J_HOST_BPARTS", str(int(g.choice([1, 2, 4, 8]))))
+    A = synth.scaled(m, k, 4, 70 + seed, "row", cplx=cplx)
+    B = synth.scaled(k, n, 4, 90 + seed, "col", cplx=cplx) if opB == 0 else \
+        synth.scaled(n, k, 4, 90 + seed, "row", cplx=cplx)
+    ctx = f4j.default_context()
+    es, dt = (16, np.complex128) if cplx else (8, np.float64)
+    dA, dB, dC = ctx.from_numpy(A), ctx.from_numpy(B), ctx.alloc(es * m * n)
+    dev = ctx.lib.f4j_zgemm if cplx else ctx.lib.f4j_dgemm
+    host = ctx.lib.f4j_zgemm_host if cplx else ctx.lib.f4j_dgemm_host
+    rd = _lib.f4j_report()
+    check(dev(ctx.handle, m, n, k, dA.handle, 0, dB.handle, opB, dC.handle, _lib.MODE_SPLIT, ctypes.byref(rd)))
+    ref = dC.to_numpy(dt, m * n).reshape(m, n)
+    C = np.zeros((m, n), dt)
+    rep = _lib.f4j_report()
+    check(host(ctx.handle, m, n, k, A.ctypes.data, 0, B.ctypes.data, opB, C.ctypes.data, _lib.MODE_SPLIT,
+               ctypes.byref(rep)))
+    assert np.array_equal(C.view(np.uint64), ref.view(np.uint64)), (m, n, k, cplx, opB)
+    assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
+
+
 def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
     """NaN / Inf in A: every row part falls back to DMMA, which propagates them
     like the reference; finite rows stay within the bound."""
