@@ -546,6 +546,41 @@ __device__ __forceinline__ long long fixed_of(double x, int e, int F) {
     return neg ? -(long long)Y : (long long)Y;
 }
 
+// The s balanced base-32 digits of eight fixed-point integers Y = H 2^30 + L
+// (0 <= L < 2^30) as E4M3 bytes: digit p (0 = most significant) of element j
+// to base[p * plane + j].
+__device__ __forceinline__ void store_digits8(int (&L)[8], int (&H)[8], int s, uint8_t* base, int64_t plane) {
+    // balanced base-32 digits from the least significant slice (p = s - 1) up
+#pragma unroll
+    for (int c = 0; c < S_MAX - 1; c++) {
+        if (c >= s - 1) break;
+        float f[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            // with t = x + 16 the balanced digit is (t & 31) - 16 and the
+            // rest (x - digit) / 32 is t >> 5; the -16 is folded into the
+            // float conversion's constant
+            int t;
+            if (c < 6) {
+                t = L[j] + 16;
+                L[j] = t >> 5;
+                if (c == 5) H[j] += L[j];  // carry out of the low 30 bits: 0 or 1
+            } else {
+                t = H[j] + 16;
+                H[j] = t >> 5;
+            }
+            f[j] = float_of_small_int((t & 31) - 16);
+        }
+        store_e4m3x8(base + (int64_t)(s - 1 - c) * plane, f);
+    }
+    // the most significant digit is what remains
+    float f[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        f[j] = float_of_small_int(s - 1 < 6 ? L[j] + H[j] * (1 << (30 - 5 * (s - 1))) : H[j]);
+    store_e4m3x8(base, f);
+}
+
 constexpr int SP_TR = 32, SP_TQ = 64;  // tile: 32 target rows x 64 k-indices
 
 // Writes slices of one operand.  Output plane p (0-based slice) is
@@ -614,37 +649,36 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
         }
         const int64_t orow = (part >= 2) ? (targets + r) : r;
         const int64_t ocol = ((part & 1) ? Kh : 0) + q0 + qs;
-        uint8_t* base = out + orow * Kp + ocol;
-        // balanced base-32 digits from the least significant slice (p = s - 1) up
-#pragma unroll
-        for (int c = 0; c < S_MAX - 1; c++) {
-            if (c >= s - 1) break;
-            float f[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                // with t = x + 16 the balanced digit is (t & 31) - 16 and the
-                // rest (x - digit) / 32 is t >> 5; the -16 is folded into the
-                // float conversion's constant
-                int t;
-                if (c < 6) {
-                    t = L[j] + 16;
-                    L[j] = t >> 5;
-                    if (c == 5) H[j] += L[j];  // carry out of the low 30 bits: 0 or 1
-                } else {
-                    t = H[j] + 16;
-                    H[j] = t >> 5;
-                }
-                f[j] = float_of_small_int((t & 31) - 16);
-            }
-            store_e4m3x8(base + (int64_t)(s - 1 - c) * rows_out * Kp, f);
-        }
-        // the most significant digit is what remains
-        float f[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++)
-            f[j] = float_of_small_int(s - 1 < 6 ? L[j] + H[j] * (1 << (30 - 5 * (s - 1))) : H[j]);
-        store_e4m3x8(base, f);
+        store_digits8(L, H, s, out + orow * Kp + ocol, rows_out * Kp);
     }
+}
+
+// k_split's body for real targets stored as rows (transposed = 0), without
+// staging: thread (rr, qs) of the 32 x 64 tile reads its 8 consecutive
+// elements of row r0 + rr straight from global memory (the 8 threads of a row
+// together read its 512 contiguous bytes) and writes the same bytes the
+// staged body does.
+__device__ __forceinline__ void split_rows_body(const double* __restrict__ X, int64_t scols, int64_t targets,
+                                                int64_t klen, int64_t Kp, int64_t rows_out,
+                                                const int* __restrict__ e_t, const SplitPlan* __restrict__ plan,
+                                                uint8_t* __restrict__ out, int64_t bx, int64_t by) {
+    if (plan->nonfinite) return;
+    const int s = plan->s;
+    const int64_t r = by * SP_TR + threadIdx.x / 8;
+    const int64_t q0 = bx * SP_TQ + (threadIdx.x % 8) * 8;
+    if (r >= targets) return;
+    const double* row = X + r * scols;
+    const int e = e_t[r];
+    const int F = 4 + 5 * (s - 1);
+    int L[8], H[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const double v = q0 + j < klen ? __ldg(row + q0 + j) : 0.0;
+        const long long y = fixed_of(v, e, F);
+        L[j] = (int)(y & 0x3FFFFFFFll);
+        H[j] = (int)(y >> 30);
+    }
+    store_digits8(L, H, s, out + r * Kp + q0, rows_out * Kp);
 }
 
 // Real operands: 17 KB of staging and at most 32 registers, so 8 blocks (64
@@ -657,8 +691,11 @@ __global__ void __launch_bounds__(256, CPLX ? 4 : 8) k_split(const double* __res
                                                              int64_t rows_out, const int* __restrict__ e_t,
                                                              const SplitPlan* __restrict__ plan,
                                                              uint8_t* __restrict__ out) {
-    split_body<CPLX>(X, srows, scols, transposed, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
-                     blockIdx.x, blockIdx.y);
+    if (!CPLX && !transposed)
+        split_rows_body(X, scols, targets, klen, Kp, rows_out, e_t, plan, out, blockIdx.x, blockIdx.y);
+    else
+        split_body<CPLX>(X, srows, scols, transposed, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
+                         blockIdx.x, blockIdx.y);
 }
 
 // One operand of k_split_pair (the arguments k_split takes for it).
@@ -682,12 +719,20 @@ __global__ void __launch_bounds__(256, CPLX ? 6 : 8) k_split_pair(const SplitOpe
     // registers: 60 registers against 35, and fewer blocks per SM)
     if (blockIdx.z == 0) {
         if ((int64_t)blockIdx.y * SP_TR >= a.targets) return;
-        split_body<CPLX>(a.X, a.srows, a.scols, a.transposed, a.conj, a.role, a.targets, klen, Kh, Kp, a.rows_out,
-                         a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
+        if (!CPLX && !a.transposed)  // rows of a real operand: no staging
+            split_rows_body(a.X, a.scols, a.targets, klen, Kp, a.rows_out, a.e_t, plan, a.out, blockIdx.x,
+                            blockIdx.y);
+        else
+            split_body<CPLX>(a.X, a.srows, a.scols, a.transposed, a.conj, a.role, a.targets, klen, Kh, Kp,
+                             a.rows_out, a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
     } else {
         if ((int64_t)blockIdx.y * SP_TR >= b.targets) return;
-        split_body<CPLX>(b.X, b.srows, b.scols, b.transposed, b.conj, b.role, b.targets, klen, Kh, Kp, b.rows_out,
-                         b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
+        if (!CPLX && !b.transposed)  // rows of a real operand: no staging
+            split_rows_body(b.X, b.scols, b.targets, klen, Kp, b.rows_out, b.e_t, plan, b.out, blockIdx.x,
+                            blockIdx.y);
+        else
+            split_body<CPLX>(b.X, b.srows, b.scols, b.transposed, b.conj, b.role, b.targets, klen, Kh, Kp,
+                             b.rows_out, b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
     }
 }
 
