@@ -225,8 +225,11 @@ __device__ __forceinline__ int finalize_target(int64_t t, int64_t targets, int d
         unsigned long long b = mx[t];
         int e = 0;
         if (b) {
+            // max|x| < 2^e, tight: for a subnormal maximum (E = 0) from its
+            // highest mantissa bit, so a row of subnormals keeps all its bits
+            // in the fixed-point form instead of being rounded at 2^(-1022 - F)
             int E = (int)(b >> 52);
-            e = E ? E - 1022 : -1022;
+            e = E ? E - 1022 : (63 - __clzll((long long)b)) - 1073;
             double mean = (double)esum[t] / (double)cnt[t];
             double s = (double)(e - 1) - mean;
             sp = s > 0 ? (int)(s * 256.0 + 0.5) : 0;
