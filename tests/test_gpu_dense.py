@@ -300,8 +300,9 @@ def test_split_with_wide_spread_picks_more_slices(f4j, oracle):
     check_bound(C, *ref_bound(oracle, A, B, False), 256, "wide spread")
 
 
+@pytest.mark.parametrize("cp", [False, True])
 @pytest.mark.parametrize("mode", ["split", "plain", "auto"])
-def test_extreme_magnitudes(f4j, oracle, mode):
+def test_extreme_magnitudes(f4j, oracle, mode, cp):
     """Rows of A scaled by 2^e for e from the subnormal range (-1060) to 2^980,
     columns of B by 2^-20 .. 2^20: the split path's per-row and per-column
     exponents and its two-step rescale of the result stay within
@@ -312,17 +313,24 @@ def test_extreme_magnitudes(f4j, oracle, mode):
     g = np.random.default_rng(77)
     ea = g.choice([-1060, -1040, -1000, -600, -30, 0, 30, 600, 980], size=m)
     eb = g.integers(-20, 21, size=n)
-    A = synth.uniform(m, k, 78) * np.ldexp(1.0, ea)[:, None]
-    B = synth.uniform(k, n, 79) * np.ldexp(1.0, eb)[None, :]
+    A = synth.uniform(m, k, 78)
+    B = synth.uniform(k, n, 79)
+    if cp:
+        A = A + 1j * synth.uniform(m, k, 80)
+        B = B + 1j * synth.uniform(k, n, 81)
+    A = A * np.ldexp(1.0, ea)[:, None]
+    B = B * np.ldexp(1.0, eb)[None, :]
     assert np.isfinite(A).all() and (np.abs(A[ea == -1060]) < 2.0 ** -1022).all()   # subnormal rows
     C, rep = run_gemm(f4j, A, B, mode=mode)
-    ref, ab = ref_bound(oracle, A, B, False)
-    slack = k * 2.0 ** -1074
-    err = np.abs(C - ref)
-    bound = 2.0 * k * U * ab + slack
-    assert np.isfinite(C).all()
-    assert not np.any(err > bound), "%d entries outside the bound, worst excess %g" % (
-        int((err > bound).sum()), float((err - bound)[err > bound].max()))
+    ref, ab = ref_bound(oracle, A, B, cp)
+    slack = 2 * k * 2.0 ** -1074
+    parts = [(C.real, ref.real, ab.real), (C.imag, ref.imag, ab.imag)] if cp else [(C, ref, ab)]
+    for c, r, a in parts:
+        err = np.abs(c - r)
+        bound = 2.0 * (2 * k if cp else k) * U * a + slack
+        assert np.isfinite(c).all()
+        assert not np.any(err > bound), "%d entries outside the bound, worst excess %g" % (
+            int((err > bound).sum()), float((err - bound)[err > bound].max()))
 
 
 def test_auto_mode_routes_nonfinite_to_dmma(f4j):
