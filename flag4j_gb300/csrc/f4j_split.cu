@@ -599,60 +599,68 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
                                            int transposed, int conj, int role, int64_t targets,
                                            int64_t klen, int64_t Kh, int64_t Kp, int64_t rows_out,
                                            const int* __restrict__ e_t, const SplitPlan* __restrict__ plan,
-                                           uint8_t* __restrict__ out, int64_t bx, int64_t by) {
+                                           uint8_t* __restrict__ out, int64_t bx, int by0, int by_step) {
     __shared__ double sre[SP_TR][SP_TQ + 1];
     __shared__ double sim[CPLX ? SP_TR : 1][SP_TQ + 1];
-    if (plan->nonfinite) return;
+    if (plan->nonfinite) return;  // the same for every thread of the block
     const int s = plan->s;
-    const int64_t r0 = by * SP_TR, q0 = bx * SP_TQ;
-    // ---- stage the tile (zeros outside the matrix)
-    for (int e = threadIdx.x; e < SP_TR * SP_TQ; e += 256) {
-        int rr, qq;
-        if (!transposed) { rr = e / SP_TQ; qq = e % SP_TQ; }
-        else { qq = e / SP_TR; rr = e % SP_TR; }
-        int64_t r = r0 + rr, q = q0 + qq;
-        double re = 0, im = 0;
-        if (r < targets && q < klen) {
-            int64_t idx = transposed ? (q * scols + r) : (r * scols + q);
-            if constexpr (CPLX) {
-                re = X[2 * idx];
-                im = X[2 * idx + 1];
-                if (conj) im = -im;
-            } else {
-                re = X[idx];
+    const int64_t q0 = bx * SP_TQ;
+    // tile rows by0, by0 + by_step, ... (more than grid.y's limit of 65535
+    // when there are over 2 M targets): the bound is the same for the whole
+    // block, and every thread meets both barriers of every tile
+    for (int by = by0; (int64_t)by * SP_TR < targets; by += by_step) {
+        const int64_t r0 = (int64_t)by * SP_TR;
+        // ---- stage the tile (zeros outside the matrix)
+        for (int e = threadIdx.x; e < SP_TR * SP_TQ; e += 256) {
+            int rr, qq;
+            if (!transposed) { rr = e / SP_TQ; qq = e % SP_TQ; }
+            else { qq = e / SP_TR; rr = e % SP_TR; }
+            int64_t r = r0 + rr, q = q0 + qq;
+            double re = 0, im = 0;
+            if (r < targets && q < klen) {
+                int64_t idx = transposed ? (q * scols + r) : (r * scols + q);
+                if constexpr (CPLX) {
+                    re = X[2 * idx];
+                    im = X[2 * idx + 1];
+                    if (conj) im = -im;
+                } else {
+                    re = X[idx];
+                }
+            }
+            sre[rr][qq] = re;
+            if constexpr (CPLX) sim[rr][qq] = im;
+        }
+        __syncthreads();
+        // ---- each thread: one target row, 8 consecutive q
+        const int rr = threadIdx.x / 8, qs = (threadIdx.x % 8) * 8;
+        const int64_t r = r0 + rr;
+        if (r < targets) {
+            const int e = e_t[r];
+            const int F = 4 + 5 * (s - 1);
+            const int nparts = CPLX ? (role == 0 ? 2 : 4) : 1;
+            for (int part = 0; part < nparts; part++) {
+                // part: 0 -> (row r, col q) ; 1 -> (row r, col Kh+q) ; 2 -> (row n+r, col q) ; 3 -> (row n+r, col Kh+q)
+                // Y = H * 2^30 + L with 0 <= L < 2^30: the low six digits come from L,
+                // the rest from H (plus the carry out of L), all in 32-bit arithmetic
+                int L[8], H[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    double v;
+                    const double a = sre[rr][qs + j];
+                    double b = 0.0;
+                    if constexpr (CPLX) b = sim[rr][qs + j];
+                    if (role == 0) v = (part == 0) ? a : b;
+                    else v = (part == 0) ? a : (part == 1) ? -b : (part == 2) ? b : a;
+                    const long long y = fixed_of(v, e, F);
+                    L[j] = (int)(y & 0x3FFFFFFFll);
+                    H[j] = (int)(y >> 30);
+                }
+                const int64_t orow = (part >= 2) ? (targets + r) : r;
+                const int64_t ocol = ((part & 1) ? Kh : 0) + q0 + qs;
+                store_digits8(L, H, s, out + orow * Kp + ocol, rows_out * Kp);
             }
         }
-        sre[rr][qq] = re;
-        if constexpr (CPLX) sim[rr][qq] = im;
-    }
-    __syncthreads();
-    // ---- each thread: one target row, 8 consecutive q
-    const int rr = threadIdx.x / 8, qs = (threadIdx.x % 8) * 8;
-    const int64_t r = r0 + rr;
-    if (r >= targets) return;
-    const int e = e_t[r];
-    const int F = 4 + 5 * (s - 1);
-    const int nparts = CPLX ? (role == 0 ? 2 : 4) : 1;
-    for (int part = 0; part < nparts; part++) {
-        // part: 0 -> (row r, col q) ; 1 -> (row r, col Kh+q) ; 2 -> (row n+r, col q) ; 3 -> (row n+r, col Kh+q)
-        // Y = H * 2^30 + L with 0 <= L < 2^30: the low six digits come from L,
-        // the rest from H (plus the carry out of L), all in 32-bit arithmetic
-        int L[8], H[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            double v;
-            const double a = sre[rr][qs + j];
-            double b = 0.0;
-            if constexpr (CPLX) b = sim[rr][qs + j];
-            if (role == 0) v = (part == 0) ? a : b;
-            else v = (part == 0) ? a : (part == 1) ? -b : (part == 2) ? b : a;
-            const long long y = fixed_of(v, e, F);
-            L[j] = (int)(y & 0x3FFFFFFFll);
-            H[j] = (int)(y >> 30);
-        }
-        const int64_t orow = (part >= 2) ? (targets + r) : r;
-        const int64_t ocol = ((part & 1) ? Kh : 0) + q0 + qs;
-        store_digits8(L, H, s, out + orow * Kp + ocol, rows_out * Kp);
+        __syncthreads();  // the next tile's staging overwrites sre / sim
     }
 }
 
@@ -664,24 +672,26 @@ __device__ __forceinline__ void split_body(const double* __restrict__ X, int64_t
 __device__ __forceinline__ void split_rows_body(const double* __restrict__ X, int64_t scols, int64_t targets,
                                                 int64_t klen, int64_t Kp, int64_t rows_out,
                                                 const int* __restrict__ e_t, const SplitPlan* __restrict__ plan,
-                                                uint8_t* __restrict__ out, int64_t bx, int64_t by) {
+                                                uint8_t* __restrict__ out, int64_t bx, int by0, int by_step) {
     if (plan->nonfinite) return;
     const int s = plan->s;
-    const int64_t r = by * SP_TR + threadIdx.x / 8;
     const int64_t q0 = bx * SP_TQ + (threadIdx.x % 8) * 8;
-    if (r >= targets) return;
-    const double* row = X + r * scols;
-    const int e = e_t[r];
-    const int F = 4 + 5 * (s - 1);
-    int L[8], H[8];
+    for (int by = by0; (int64_t)by * SP_TR < targets; by += by_step) {  // tile rows, as in split_body
+        const int64_t r = (int64_t)by * SP_TR + threadIdx.x / 8;
+        if (r >= targets) continue;
+        const double* row = X + r * scols;
+        const int e = e_t[r];
+        const int F = 4 + 5 * (s - 1);
+        int L[8], H[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-        const double v = q0 + j < klen ? __ldg(row + q0 + j) : 0.0;
-        const long long y = fixed_of(v, e, F);
-        L[j] = (int)(y & 0x3FFFFFFFll);
-        H[j] = (int)(y >> 30);
+        for (int j = 0; j < 8; j++) {
+            const double v = q0 + j < klen ? __ldg(row + q0 + j) : 0.0;
+            const long long y = fixed_of(v, e, F);
+            L[j] = (int)(y & 0x3FFFFFFFll);
+            H[j] = (int)(y >> 30);
+        }
+        store_digits8(L, H, s, out + r * Kp + q0, rows_out * Kp);
     }
-    store_digits8(L, H, s, out + r * Kp + q0, rows_out * Kp);
 }
 
 // Real operands: 17 KB of staging and at most 32 registers, so 8 blocks (64
@@ -695,10 +705,10 @@ __global__ void __launch_bounds__(256, CPLX ? 4 : 8) k_split(const double* __res
                                                              const SplitPlan* __restrict__ plan,
                                                              uint8_t* __restrict__ out) {
     if (!CPLX && !transposed)
-        split_rows_body(X, scols, targets, klen, Kp, rows_out, e_t, plan, out, blockIdx.x, blockIdx.y);
+        split_rows_body(X, scols, targets, klen, Kp, rows_out, e_t, plan, out, blockIdx.x, blockIdx.y, gridDim.y);
     else
         split_body<CPLX>(X, srows, scols, transposed, conj, role, targets, klen, Kh, Kp, rows_out, e_t, plan, out,
-                         blockIdx.x, blockIdx.y);
+                         blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // One operand of k_split_pair (the arguments k_split takes for it).
@@ -724,18 +734,18 @@ __global__ void __launch_bounds__(256, CPLX ? 6 : 8) k_split_pair(const SplitOpe
         if ((int64_t)blockIdx.y * SP_TR >= a.targets) return;
         if (!CPLX && !a.transposed)  // rows of a real operand: no staging
             split_rows_body(a.X, a.scols, a.targets, klen, Kp, a.rows_out, a.e_t, plan, a.out, blockIdx.x,
-                            blockIdx.y);
+                            blockIdx.y, gridDim.y);
         else
             split_body<CPLX>(a.X, a.srows, a.scols, a.transposed, a.conj, a.role, a.targets, klen, Kh, Kp,
-                             a.rows_out, a.e_t, plan, a.out, blockIdx.x, blockIdx.y);
+                             a.rows_out, a.e_t, plan, a.out, blockIdx.x, blockIdx.y, gridDim.y);
     } else {
         if ((int64_t)blockIdx.y * SP_TR >= b.targets) return;
         if (!CPLX && !b.transposed)  // rows of a real operand: no staging
             split_rows_body(b.X, b.scols, b.targets, klen, Kp, b.rows_out, b.e_t, plan, b.out, blockIdx.x,
-                            blockIdx.y);
+                            blockIdx.y, gridDim.y);
         else
             split_body<CPLX>(b.X, b.srows, b.scols, b.transposed, b.conj, b.role, b.targets, klen, Kh, Kp,
-                             b.rows_out, b.e_t, plan, b.out, blockIdx.x, blockIdx.y);
+                             b.rows_out, b.e_t, plan, b.out, blockIdx.x, blockIdx.y, gridDim.y);
     }
 }
 
@@ -1184,6 +1194,13 @@ static int env_band() {
 
 static size_t al1k(size_t x) { return (x + 1023) & ~size_t(1023); }
 
+// grid.y of a slicing launch over `targets` rows of slices: one block row per
+// 32 targets, at most 65535 (the kernels then loop over the remaining tile rows)
+static unsigned slice_grid_y(int64_t targets) {
+    const int64_t t = f4j_cdiv(targets, SP_TR);
+    return (unsigned)(t < 65535 ? (t > 0 ? t : 1) : 65535);
+}
+
 // Asynchronous split GEMM: statistics -> device plan -> slicing -> slice GEMM,
 // all queued on the context stream with no host synchronisation.  *gate
 // receives the device flag that is non-zero when the plan stood down (NaN/Inf
@@ -1360,10 +1377,9 @@ static int split_prepare(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t 
                               ea, slA};
         const SplitOperand sb{B, b_rows ? n : k, b_rows ? k : n, b_rows ? 0 : 1, opB == F4J_OP_C ? 1 : 0, 1, n, N,
                               eb, slB};
-        const int64_t gy = f4j_cdiv(M > n ? M : n, SP_TR);
-        if (gy > 65535) return f4j_fail(F4J_ERR_ARG, "split GEMM: %lld rows exceed the slicing grid", (long long)(M > n ? M : n));
+        const unsigned gy = slice_grid_y(M > n ? M : n);
         auto pair = cplx ? k_split_pair<true> : k_split_pair<false>;
-        pair<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)gy, 2), 256, 0, ctx->stream>>>(sa, sb, k, Kh, Kp, plan);
+        pair<<<dim3((unsigned)(Kh / SP_TQ), gy, 2), 256, 0, ctx->stream>>>(sa, sb, k, Kh, Kp, plan);
         F4J_LAUNCHED(ctx);
     }
     f4j_prof_end(ctx);
@@ -1533,8 +1549,7 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
     const int64_t Kp = cplx ? 2 * Kh : Kh;
     const int64_t klen_cat = cplx ? 2 * k : k;
     const int64_t w2 = cplx ? 2 : 1;  // doubles per element
-    if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX || f4j_cdiv(m > n ? m : n, SP_TR) > 65535)
-        return f4j_fail(F4J_ERR_ARG, "host-buffer split GEMM too large");
+    if (M > INT32_MAX || N > INT32_MAX || Kp > INT32_MAX) return f4j_fail(F4J_ERR_ARG, "host-buffer split GEMM too large");
     const SmallLayout Lo = small_layout(M, n, N);
     void *ws1, *ws0;
     int rc = f4j_workspace(ctx, ctx->ws_base + 1, Lo.total, &ws1);
@@ -1657,7 +1672,7 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
         };
         // its slice planes: target t of the part is row r0 + t
         auto a_part_split = [&](int64_t r0, int64_t rows) -> int {
-            split_k<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(rows, SP_TR)), 256, 0, st>>>(
+            split_k<<<dim3((unsigned)(Kh / SP_TQ), slice_grid_y(rows)), 256, 0, st>>>(
                 dA + r0 * k * w2, rows, k, 0, 0, 0, rows, k, Kh, Kp, M, ea + r0, plan, slA + r0 * Kp);
             F4J_LAUNCHED(ctx);
             return F4J_OK;
@@ -1707,7 +1722,7 @@ static int host_split_pipelined(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, i
                 rc = a_part_split(0, a0_rows);
                 if (rc) break;
             }
-            split_k<<<dim3((unsigned)(Kh / SP_TQ), (unsigned)f4j_cdiv(cw, SP_TR)), 256, 0, st>>>(
+            split_k<<<dim3((unsigned)(Kh / SP_TQ), slice_grid_y(cw)), 256, 0, st>>>(
                 b_rows ? dB + c0 * k * w2 : dB + c0 * w2, b_rows ? cw : k, b_rows ? k : n, b_rows ? 0 : 1, conjb, 1,
                 cw, k, Kh, Kp, N, eb + c0, plan, slB + c0 * Kp);
             F4J_LAUNCHED(ctx);
@@ -1978,9 +1993,9 @@ extern "C" int f4j_dgemm_split_noalloc(int64_t m, int64_t n, int64_t k, const do
     // and return at once for a NaN/Inf operand or a plan that does not fit.
     uint8_t* slA = (uint8_t*)(w + off_sl);
     uint8_t* slB = slA + al1k((size_t)M * Kp * S_MAX);
-    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(M, SP_TR)), 256, 0, st>>>(
+    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), slice_grid_y(M)), 256, 0, st>>>(
         A, a_rows ? M : k, a_rows ? k : M, a_rows ? 0 : 1, 0, 0, M, k, Kp, Kp, M, ea, plan, slA);
-    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), (unsigned)f4j_cdiv(N, SP_TR)), 256, 0, st>>>(
+    k_split<false><<<dim3((unsigned)(Kp / SP_TQ), slice_grid_y(N)), 256, 0, st>>>(
         B, b_rows ? N : k, b_rows ? k : N, b_rows ? 0 : 1, 0, 1, N, k, Kp, Kp, N, eb, plan, slB);
     F4J_CUDA(cudaGetLastError());
     CUtensorMap ta{}, tb{};

@@ -333,6 +333,29 @@ def test_extreme_magnitudes(f4j, oracle, mode, cp):
             int((err > bound).sum()), float((err - bound)[err > bound].max()))
 
 
+@pytest.mark.parametrize("tall", [True, False])
+def test_split_beyond_two_million_rows_or_columns(f4j, oracle, tall):
+    """More than 2^21 rows of A (tall) or columns of B (wide): the slicing
+    kernels cover them with grid.y at its limit of 65535 blocks of 32 targets,
+    looping over the rest.  Sampled rows (including the last ones) are within
+    2 k u |A||B| of the reference's order."""
+    from flag4j_gb300 import synth
+    big, small, k = 2_200_000, 64, 100
+    m, n = (big, small) if tall else (small, big)
+    A = synth.uniform(m, k, 91)
+    B = synth.uniform(k, n, 92)
+    C, rep = run_gemm(f4j, A, B, mode="split")
+    assert rep.mode_used == 1 and rep.slices > 0
+    if tall:
+        rows = np.r_[0:64, m - 2048:m]   # the last ones are past 65535 x 32 targets
+        ref, ab = ref_bound(oracle, A[rows], B, False)
+        assert_within_bound(C[rows], ref, ab, k, "tall")
+    else:
+        cols = np.r_[0:64, n - 2048:n]
+        ref, ab = ref_bound(oracle, A, np.ascontiguousarray(B[:, cols]), False)
+        assert_within_bound(C[:, cols], ref, ab, k, "wide")
+
+
 def test_auto_mode_routes_nonfinite_to_dmma(f4j):
     A = np.ones((256, 256))
     A[3, 4] = np.nan
