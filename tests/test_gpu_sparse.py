@@ -545,6 +545,44 @@ def test_spmm_exact_rounding_adversarial_operands(f4j, oracle, specials, ncols):
     assert _same_bits(S.multTransposeLeft(f4j.Matrix(X)).toNumpy(), oracle.spmm(trp, tci, tv, X))
 
 
+@pytest.mark.parametrize("specials", [False, True])
+def test_spmv_exact_rounding_adversarial_operands(f4j, oracle, specials):
+    """The matrix-vector kernel (k_spmv) on the same adversarial values: every
+    entry of S x, signed zeros, subnormals and NaN positions included, is the
+    oracle's storage-order multiply-then-add result bit for bit."""
+    from flag4j_gb300 import synth
+    rows = cols = 20000
+    rng = np.random.default_rng(7 + specials)
+    rp, ci, _ = synth.csr_poisson(rows, cols, lam=12.0, hi=300, seed=33)
+    v = _adversarial_values(rng, len(ci), specials)
+    x = _adversarial_values(rng, cols, specials)
+    S = f4j.CsrMatrix((rows, cols), v, rp, ci)
+    assert _same_bits(S.mult(f4j.Vector(x)).data, oracle.spmv(rp, ci, v, x))
+
+
+@pytest.mark.parametrize("specials", [False, True])
+@pytest.mark.parametrize("cp", [False, True])
+def test_dense_exact_rounding_adversarial_operands(f4j, oracle, specials, cp):
+    """EXACT dense products on the same adversarial values (ties, cancellation,
+    overflow, subnormals, signed zeros, and with specials Inf / NaN): bit for
+    bit the reference's k-ascending order, real and complex."""
+    rng = np.random.default_rng(11 + specials + 2 * cp)
+    m, n, k = 150, 70, 260
+    A = _adversarial_values(rng, m * k, specials).reshape(m, k)
+    B = _adversarial_values(rng, k * n, specials).reshape(k, n)
+    if cp:  # real and imaginary parts set directly (1j * inf would also make the real part NaN)
+        Az, Bz = np.empty((m, k), np.complex128), np.empty((k, n), np.complex128)
+        Az.real, Az.imag = A, _adversarial_values(rng, m * k, specials).reshape(m, k)
+        Bz.real, Bz.imag = B, _adversarial_values(rng, k * n, specials).reshape(k, n)
+        A, B = Az, Bz
+        got = f4j.CMatrix(A).mult(f4j.CMatrix(B), mode="exact").toNumpy()
+        ref = oracle.zgemm(A, B)
+        assert _same_bits(got.real.copy(), ref.real.copy()) and _same_bits(got.imag.copy(), ref.imag.copy())
+    else:
+        got = f4j.Matrix(A).mult(f4j.Matrix(B), mode="exact").toNumpy()
+        assert _same_bits(got, oracle.dgemm(A, B))
+
+
 def test_coo_to_csr_range_checks_report_first_bad_entry(f4j):
     """CooMatrix.toCsr checks the indices inside the row count and the column copy: the first
     out-of-range entry by position is reported as SparseValidation.validateCoo words it, for rows
