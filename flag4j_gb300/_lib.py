@@ -94,6 +94,7 @@ SIGNATURES = {
     "f4j_dgemm": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),
     "f4j_dgemm_host": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),
     "f4j_zgemm_host": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),
+    "f4j_set_host_pinning": (_i, [_v, _i]),
     "f4j_zgemm": (_i, [_v, _i64, _i64, _i64, _v, _i, _v, _i, _v, _i, _rep]),
     "f4j_dgemm_adjoint": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _v, _v, _i, _rep]),
     "f4j_zgemm_adjoint": (_i, [_v, _i64, _i64, _i64, _v, _v, _v, _v, _v, _i, _rep]),

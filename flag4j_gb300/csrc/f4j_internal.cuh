@@ -74,6 +74,7 @@ struct f4j_ctx {
     long long plan_key[2][4];
     bool plan_valid[2];
     bool parts_init;
+    bool host_pin;     // host-buffer products page-lock their arrays per call (f4j_set_host_pinning)
     int* d_status;     // device status words (bounded-wait timeouts, validation)
     cudaEvent_t ev[16];
     bool ev_init[16];

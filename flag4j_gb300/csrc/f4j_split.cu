@@ -1803,6 +1803,30 @@ static int gemm_host(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, c
     if (!cplx && opB == F4J_OP_C) opB = F4J_OP_T;
     const size_t es = cplx ? 16 : 8;  // bytes per element
     const size_t ab = (size_t)m * k * es, bb = (size_t)k * n * es, cb = (size_t)m * n * es;
+    // With host pinning on, the caller's arrays are page-locked for this call
+    // and released on every way out (after the context's streams have
+    // drained).  An array that is already page-locked, or that cannot be
+    // registered (e.g. it shares a page with one that is), is used as it is.
+    struct HostPins {
+        f4j_ctx* ctx;
+        void* p[3];
+        int n = 0;
+        ~HostPins() {
+            if (!n) return;
+            cudaStreamSynchronize(ctx->stream);
+            for (int i = 0; i < n; i++) cudaHostUnregister(p[i]);
+            cudaGetLastError();
+        }
+    } pins{ctx, {nullptr, nullptr, nullptr}};
+    if (ctx->host_pin) {
+        void* const ptrs[3] = {(void*)A, (void*)B, (void*)C};
+        const size_t bytes[3] = {ab, bb, cb};
+        for (int i = 0; i < 3; i++) {
+            if (!bytes[i]) continue;
+            if (cudaHostRegister(ptrs[i], bytes[i], cudaHostRegisterDefault) == cudaSuccess) pins.p[pins.n++] = ptrs[i];
+            else cudaGetLastError();  // stays pageable; clear the error so later launch checks do not see it
+        }
+    }
     void *dA, *dB, *dC;
     int rc = f4j_workspace(ctx, 3, ab, &dA);
     if (!rc) rc = f4j_workspace(ctx, 6, bb, &dB);
@@ -1873,6 +1897,13 @@ static int gemm_host(f4j_ctx* ctx, bool cplx, int64_t m, int64_t n, int64_t k, c
 extern "C" int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,
                               const double* B, int opB, double* C, int mode, f4j_report* rep) {
     return gemm_host(ctx, false, m, n, k, A, opA, B, opB, C, mode, rep);
+}
+
+extern "C" int f4j_set_host_pinning(f4j_ctx* ctx, int on) {
+    F4J_LOCK(ctx);
+    F4J_CHECK_CTX(ctx);
+    ctx->host_pin = on != 0;
+    return F4J_OK;
 }
 
 extern "C" int f4j_zgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA,

@@ -268,6 +268,16 @@ int f4j_dgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* 
  * (Cm128DeMatMultKernels.java:46-77). */
 int f4j_zgemm_host(f4j_ctx* ctx, int64_t m, int64_t n, int64_t k, const double* A, int opA, const double* B,
                    int opB, double* C, int mode, f4j_report* report);
+/* Host pinning for the host-buffer products (f4j_dgemm_host, f4j_zgemm_host;
+ * off by default, no counterpart in Flag4j).  On, each call page-locks A, B
+ * and C for its duration (cudaHostRegister) and releases them before it
+ * returns; arrays already page-locked, or whose pages cannot be registered,
+ * are used as they are.  For callers whose arrays are pageable and live only
+ * for the call: a JVM binding passing Java heap arrays through a critical
+ * downcall (Linker.Option.critical(true)), where registering costs about 1-2
+ * ms per 512 MiB operand against about 37 ms to copy it into native memory,
+ * and the copies then run at the page-locked rate. */
+int f4j_set_host_pinning(f4j_ctx* ctx, int on);
 
 /* Complex128 C = op(A) * op(B), interleaved (re, im); op may be N, T or C.
  * Replaces CMatrix.mult -> Cm128DeMatMultDispatcher.dispatch

@@ -630,6 +630,39 @@ def test_host_buffer_gemm_random_shapes_and_parts(f4j, seed, monkeypatch):
     assert rep.mode_used == rd.mode_used and rep.slices == rd.slices
 
 
+@pytest.mark.parametrize("cp", [False, True])
+def test_host_pinning_per_call(f4j, cp):
+    """f4j_set_host_pinning: pageable arrays are page-locked for each host-buffer
+    call and released after it; the same array passed as A and B (registered
+    once, the second registration refused and used as it is) and arrays that
+    are already page-locked still give f4j_dgemm's / f4j_zgemm's bits."""
+    from flag4j_gb300 import _lib, synth
+    from flag4j_gb300.device import check
+    ctx = f4j.default_context()
+    n = 1536  # 12 x 12 tiles (24 for complex), 24 K blocks: pipelined
+    A = synth.scaled(n, n, 4, 31, "row", cplx=cp)
+    dt, es = (np.complex128, 16) if cp else (np.float64, 8)
+    dev = ctx.lib.f4j_zgemm if cp else ctx.lib.f4j_dgemm
+    host = ctx.lib.f4j_zgemm_host if cp else ctx.lib.f4j_dgemm_host
+    dA, dC = ctx.from_numpy(A), ctx.alloc(es * n * n)
+    check(dev(ctx.handle, n, n, n, dA.handle, 0, dA.handle, 0, dC.handle, _lib.MODE_SPLIT, None))
+    ref = dC.to_numpy(dt, n * n).reshape(n, n)
+    check(ctx.lib.f4j_set_host_pinning(ctx.handle, 1))
+    try:
+        for _ in range(2):
+            C = np.zeros((n, n), dt)
+            check(host(ctx.handle, n, n, n, A.ctypes.data, 0, A.ctypes.data, 0, C.ctypes.data, _lib.MODE_SPLIT, None))
+            assert np.array_equal(C, ref)
+        # the arrays were released: registering them now succeeds
+        check(ctx.lib.f4j_host_register(A.ctypes.data, A.nbytes))
+        C = np.zeros((n, n), dt)
+        check(host(ctx.handle, n, n, n, A.ctypes.data, 0, A.ctypes.data, 0, C.ctypes.data, _lib.MODE_SPLIT, None))
+        assert np.array_equal(C, ref)
+        check(ctx.lib.f4j_host_unregister(A.ctypes.data))
+    finally:
+        check(ctx.lib.f4j_set_host_pinning(ctx.handle, 0))
+
+
 def test_host_buffer_gemm_nonfinite_parts(f4j, oracle):
     """NaN / Inf in A: every row part falls back to DMMA, which propagates them
     like the reference; finite rows stay within the bound."""
