@@ -798,6 +798,17 @@ def run_ours(args):
                                      L.MODE_SPLIT, None))
     e2e_ms = E.timed(e2e, max(3, args.steps // 3), 2)
     e2e_ms = dist.max(e2e_ms)
+    # the same call on pageable arrays page-locked per call (f4j_set_host_pinning): what a JVM binding
+    # passing its heap arrays through a critical downcall gets
+    Ahp, Bhp, Chp = np.array(A_h), np.array(B_h), np.empty((n, n))
+    E.check(E.lib.f4j_set_host_pinning(E.ctx.handle, 1))
+
+    def e2e_pageable():
+        E.check(E.lib.f4j_dgemm_host(E.ctx.handle, n, n, n, Ahp.ctypes.data, 0, Bhp.ctypes.data, 0,
+                                     Chp.ctypes.data, L.MODE_SPLIT, None))
+    e2e_pg_ms = dist.max(E.timed(e2e_pageable, 3, 1))
+    E.check(E.lib.f4j_set_host_pinning(E.ctx.handle, 0))
+    del Ahp, Bhp, Chp
 
     cb = None
     if rank == 0 and ws == 1:
@@ -836,6 +847,12 @@ def run_ours(args):
                             "each part sliced as it arrives, B's column parts multiplied by A's first rows and "
                             "A's later parts by all of B, each block of C downloaded behind its product (the "
                             "slice count from the first parts, checked against all of A and B)"},
+            "e2e_pageable_pinned_per_call": {"value": ws * flops / (e2e_pg_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                                             "ms_per_step": e2e_pg_ms,
+                                             "path": "f4j_dgemm_host on pageable host A, B, C with "
+                                                     "f4j_set_host_pinning on (each call page-locks and "
+                                                     "releases them), as a JVM binding passing heap arrays "
+                                                     "through a critical downcall"},
             "gpu_launches": launches, "clocks": clocks}
     line.update(out)
     print(json.dumps(line))
